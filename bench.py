@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 simulation step.
+
+Workload (default): the 3D PBF dam break of 131,072 particles (32 x 64 x 64 jittered
+lattice, d = 0.0125 in a unit box, h = 2d, substep dt = 1/240 s, 3 Jacobi iterations,
+vorticity confinement + XSPH).  One step = one Model::update() (one substep).
+Metric: particle-steps/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value: K device-timed steps (CUDA events around each graph replay on the model's
+  stream), inputs resident in HBM, L2 flushed before every step by a 256 MiB write.
+* e2e: K steps through the public API with host buffers: upload pos/vel from pinned
+  host memory, update(1), download pos/vel, timed on the host clock.
+* roofline: the dominant kernel's algorithmic bytes / its mean CUDA-event duration
+  (captured event nodes inside the same graph replays), against MEASURED_PEAKS.json.
+* cpu_baseline: the CPU oracle (the reference's kernels restated in C++/OpenMP) on
+  the host cores, on a bounded sample of the same workload.
+* --impl reference: the CPU implementation alone (rank 0), same metric and config.
+Under torchrun (N > 1) each rank runs an independent replica of the workload on its
+own GPU (one scene does not shard): barrier + max-over-ranks timing.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from realtimeparticles_gb300 import abi, scenes  # noqa: E402
+
+L2_FLUSH_BYTES = 256 << 20
+REF_BUDGET_S = 150.0
+WORKLOAD = "pbf_dam_break_131k"
+
+# Algorithmic bytes per particle of each kernel of the PBF substep (minimal dataflow of
+# the fused kernels: every array a kernel must read or write once).
+KERNEL_BYTES = {
+    "fld_predict": 16 + 16 + 16 + 4,          # pos, vel in; predPos, key out
+    "sort_pass": 4 + 4 + 4,                   # key in; key, index out
+    "sort_pass_gather": 4 + 4 + 4 + 3 * 32 + 8,  # key, index in; key out; 3 float4 gathered; id
+    "cellTable": 4 + 8,                       # sorted key in; table entries out (upper bound)
+    "fld_lambda": 16 + 4 + 4,                 # predPos in; lambda, density out
+    "fld_deltap": 16 + 4 + 16,                # predPos, lambda in; predPos out
+    "fld_deltap_vel": 16 + 4 + 16 + 16 + 16,  # + pos in, vel out
+    "fld_vorticity": 16 + 16 + 16,            # predPos, vel in; vorticity out
+    "fld_confine": 16 + 16 + 16 + 16,         # predPos, vorticity, vel in; vel out
+    "fld_xsph_final": 16 + 16 + 16 + 16 + 8,  # predPos, vel in; pos, vel out; ids
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(value, ws):
+    """Max of a float over all ranks (identity for one rank)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(steps_sample=None, budget_s=20.0, iters=3):
+    """The oracle on the host cores, on a bounded sample of the workload."""
+    import oracle
+    oracle.set_threads(0)
+    cores = oracle.get_threads()
+    sc = scenes.dam_break(lattice=(32, 64, 64))
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    st = oracle.new_state(sc["pos"].shape[0], c)
+    st["pos"][:] = sc["pos"]
+    st["vel"][:] = sc["vel"]
+    oracle.fluids_step(c, sc["fluid_params"], iters, st)  # warm-up
+    n = sc["pos"].shape[0]
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+        k += 1
+        el = time.perf_counter() - t0
+        if (steps_sample and k >= steps_sample) or (not steps_sample and el >= budget_s):
+            break
+    return {"value": n * k / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d steps of the %d-particle dam break (I=%d), %.1f s" % (k, n, iters, el)}
+
+
+def run_reference(args):
+    """The CPU implementation of the step (the oracle: the reference's kernels restated in
+    C++/OpenMP) on all host cores: W warm-up updates, then K timed updates of the same
+    131k workload (stopping early after REF_BUDGET_S, reported in the sample)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.set_threads(0)
+    cores = oracle.get_threads()
+    iters = 3
+    sc = scenes.dam_break(lattice=(32, 64, 64))
+    n = sc["pos"].shape[0]
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    st = oracle.new_state(n, c)
+    st["pos"][:] = sc["pos"]
+    st["vel"][:] = sc["vel"]
+    for _ in range(args.warmup):
+        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+    t0 = time.perf_counter()
+    k = 0
+    while k < args.steps:
+        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+        k += 1
+        if time.perf_counter() - t0 > REF_BUDGET_S:
+            break
+    el = time.perf_counter() - t0
+    value = n * k / el
+    sample = "%d of %d requested updates of the %d-particle dam break (I=%d) in %.1f s" % (k, args.steps, n, iters, el)
+    line = {"metric": "PBF particle-steps/s @131k (plain, 3 Jacobi iterations)", "value": value,
+            "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * el / k, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from realtimeparticles_gb300 import model
+    from realtimeparticles_gb300._lib import lib
+    if ws > 1:
+        # The library uses the current device of the calling thread.
+        import torch
+        torch.cuda.set_device(local)
+    iters = 3
+    sc = scenes.dam_break(lattice=(32, 64, 64))
+    n = sc["pos"].shape[0]
+    m = model.Fluids(sc["model_params"])
+    m.setFluidParams(sc["fluid_params"])
+    m.setJacobiIterations(iters)
+    m.upload(abi.BUF_POS, sc["pos"])
+    m.upload(abi.BUF_VEL, sc["vel"])
+
+    # Warm-up (graph capture happens here).
+    m.update(max(3, args.warmup))
+    m.synchronize()
+
+    # Device-timed steps with an L2 flush before each.
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws)
+    ms = m.timeSteps(args.steps, flush_bytes=L2_FLUSH_BYTES)
+    barrier(ws)
+    clk = clocks.stop()
+    ms = max_over_ranks(ms, ws)
+    value = n * args.steps * ws / (ms / 1000.0)
+
+    # Per-kernel times from captured events inside the same kind of graph replays.
+    m.enableProfiling(True)
+    m.resetKernelTimes()
+    m.timeSteps(args.steps, flush_bytes=L2_FLUSH_BYTES)
+    kt = m.kernelTimes()
+    m.enableProfiling(False)
+    launches_per_step = sum(v[0] for v in kt.values()) / max(1, args.steps)
+    dom = max(kt.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    dom_avg_ms = dom_ms / dom_launches
+    peak, peak_kind = load_peaks()
+    alg = KERNEL_BYTES.get(dom_name, 0) * n
+    achieved = alg / (dom_avg_ms / 1000.0) / 1e9
+    share = {k: round(v[1] / sum(x[1] for x in kt.values()), 4) for k, v in kt.items()}
+
+    # End to end through the public API with pinned host buffers.
+    try:
+        import torch
+        hpos = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+        hvel = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+        pinned = True
+    except Exception:
+        hpos = np.empty((n, 4), np.float32)
+        hvel = np.empty((n, 4), np.float32)
+        pinned = False
+    hpos[:] = m.download(abi.BUF_POS)
+    hvel[:] = m.download(abi.BUF_VEL)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.upload(abi.BUF_POS, hpos)
+        m.upload(abi.BUF_VEL, hvel)
+        m.update(1)
+        lib().rtp_download(m.handle, abi.BUF_POS, hpos.ctypes.data_as(C.c_void_p), n)
+        lib().rtp_download(m.handle, abi.BUF_VEL, hvel.ctypes.data_as(C.c_void_p), n)
+    t_e2e = time.perf_counter() - t0
+    barrier(ws)
+    t_e2e = max_over_ranks(t_e2e, ws)
+    e2e = n * args.steps * ws / t_e2e
+    metrics = m.metrics()
+    m.close()
+
+    out = None
+    if rank == 0:
+        cb = cpu_baseline(budget_s=args.cpu_seconds) if not args.no_cpu else None
+        out = {
+            "metric": "PBF particle-steps/s @131k (plain, 3 Jacobi iterations)",
+            "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0,
+                       "l2": "flushed before every timed step (256 MiB write)",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": 2 * 16 * n,
+                    "d2h_bytes_per_step": 2 * 16 * n, "pinned_host": pinned},
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None, "algorithmic_bytes_per_launch": alg,
+                         "mean_launch_ms": dom_avg_ms},
+            "kernel_share": share,
+            "clocks": clk,
+            "state_check": {"mean_density_error": metrics.meanDensityError, "kinetic_energy": metrics.kineticEnergy},
+        }
+        if cb:
+            out["cpu_baseline"] = cb
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,288 @@
+/*
+ * rtp.h - C ABI of the GB300 (sm_103a) RealTimeParticles simulation step.
+ *
+ * This library replaces the OpenCL compute path that sits behind the reference's
+ * `Physics::Model` interface (physics/Model.hpp:81-216, created by
+ * `Physics::CreateModel`, physics/Model.cpp:10-24).  Every entry point below names the
+ * reference interface it replaces.  The ABI is plain C: POD structs, plain pointers and
+ * sizes, `int` status codes (`rtp_status`), no exceptions and no C++ or torch types.
+ *
+ * Threading: one handle per host thread.  All work of a handle is ordered on the
+ * handle's own CUDA stream; `rtp_download` and `rtp_synchronize` wait for it.
+ * Errors: every function returns RTP_OK or an error code; `rtp_last_error()` returns a
+ * thread-local message describing the last failure on the calling thread.
+ *
+ * There is no CPU fallback and no multi-backend dispatch: without a CUDA device every
+ * compute call fails with RTP_ERR_NO_DEVICE.
+ */
+#ifndef RTP_H
+#define RTP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTP_ABI_VERSION 1
+
+/* Status codes.  The reference reports errors as `bool` + log lines and throws
+ * std::runtime_error on bad JSON paths (physics/ocl/Fluids.cpp:245-250); across a C ABI
+ * they become return codes. */
+typedef enum rtp_status {
+  RTP_OK = 0,
+  RTP_ERR_INVALID_ARGUMENT = 1,
+  RTP_ERR_OUT_OF_MEMORY = 2,
+  RTP_ERR_CUDA = 3,
+  RTP_ERR_NOT_SUPPORTED = 4,
+  RTP_ERR_STATE = 5,
+  RTP_ERR_NO_DEVICE = 6,
+  RTP_ERR_CAPACITY = 7
+} rtp_status;
+
+/* Physics::ModelType, physics/Model.hpp:16-21 (same values). */
+typedef enum rtp_model_type {
+  RTP_MODEL_BOIDS = 0,
+  RTP_MODEL_FLUIDS = 1,
+  RTP_MODEL_CLOUDS = 2
+} rtp_model_type;
+
+/* Physics::Boundary, physics/Model.hpp:38-44 (same order). */
+typedef enum rtp_boundary {
+  RTP_BOUNDARY_BOUNCING_WALL = 0,
+  RTP_BOUNDARY_CYCLIC_WALL = 1
+} rtp_boundary;
+
+/* Utils::PhysicsCase, utils/Parameters.hpp:17-39 (same values). */
+typedef enum rtp_case {
+  RTP_CASE_BOIDS_SMALL = 1,
+  RTP_CASE_BOIDS_MEDIUM = 2,
+  RTP_CASE_BOIDS_LARGE = 3,
+  RTP_CASE_BOIDS_XLARGE = 4,
+  RTP_CASE_FLUIDS_DAM = 7,
+  RTP_CASE_FLUIDS_BOMB = 8,
+  RTP_CASE_FLUIDS_DROP = 9,
+  RTP_CASE_CLOUDS_CUMULUS = 12,
+  RTP_CASE_CLOUDS_HOMOGENEOUS = 13,
+  RTP_CASE_INVALID = -1
+} rtp_case;
+
+/* Physics::ModelParams, physics/Model.hpp:60-73.  The four GL VBO ids are replaced by
+ * headless device buffers owned by the handle (see rtp_device_ptr).  Box extents are
+ * float (the reference's Geometry::BoxSize3D is size_t, utils/Geometry.hpp:42-47), so
+ * non-integer boxes are expressible.  `maxNbPartsInCell` is the constructor constant
+ * m_maxNbPartsInCell (Fluids.cpp:79, Boids.cpp:78, Clouds.cpp:107); 0 selects the
+ * reference value for the model. */
+typedef struct rtp_model_params {
+  uint64_t currNbParticles;
+  uint64_t maxNbParticles;
+  float boxSize[3];
+  uint32_t gridRes[3];
+  float velocity;
+  uint32_t dimension; /* 2 or 3 */
+  int32_t pCase;      /* rtp_case */
+  uint32_t maxNbPartsInCell;
+} rtp_model_params;
+
+/* FluidKernelInputs, physics/ocl/Fluids.hpp:17-32 == FluidParams, kernels/define.cl:13-25.
+ * Same field order and types (44 bytes). */
+typedef struct rtp_fluid_params {
+  float restDensity;
+  float relaxCFM;
+  float timeStep;
+  uint32_t dim;
+  uint32_t isArtPressureEnabled;
+  float artPressureRadius;
+  float artPressureCoeff;
+  uint32_t artPressureExp;
+  uint32_t isVorticityConfEnabled;
+  float vorticityConfCoeff;
+  float xsphViscosityCoeff;
+} rtp_fluid_params;
+
+/* BoidsRuleKernelInputs, physics/ocl/Boids.hpp:14-20 == BoidsRuleParams, boids.cl:12-17. */
+typedef struct rtp_boids_params {
+  float velocityScale;
+  float alignmentScale;
+  float separationScale;
+  float cohesionScale;
+} rtp_boids_params;
+
+/* CloudKernelInputs, physics/ocl/Clouds.hpp:15-45 == CloudParams, clouds.cl:19-33
+ * (same field order, 52 bytes). */
+typedef struct rtp_cloud_params {
+  uint32_t dim;
+  float timeStep;
+  float restDensity;
+  float groundHeatCoeff;
+  float buoyancyCoeff;
+  float gravCoeff;
+  float adiabaticLapseRate;
+  float phaseTransitionRate;
+  float latentHeatCoeff;
+  uint32_t isTempSmoothingEnabled;
+  float relaxCFM;
+  float initVaporDensityCoeff;
+  float windCoeff;
+} rtp_cloud_params;
+
+/* Environment of the clouds model.  The reference hard-codes it in clouds.cl:72-89 and
+ * clouds.cl:951-952 for a 10x20x10 box: T_env(y) = 293 - 3.5 (y + W_y), ground heat
+ * source exp(-(y + W_y) / 3), wind profiles 1 - exp(-0.2 (y + W_y)) and
+ * 1 - exp(-0.3 (y + W_y)).  rtp_cloud_env_reference() returns exactly those values.
+ * `groundTemp` (optional, groundNx x groundNz floats, row-major in z) replaces the
+ * constant ground temperature by a field over (x, z), bilinearly sampled over
+ * [-W_x, W_x] x [-W_z, W_z]. */
+typedef struct rtp_cloud_env {
+  float groundTemp0;  /* 293 K: ground temperature when no field is given */
+  float lapseRate;    /* 3.5 K per box unit */
+  float heatDecay;    /* 3.0 box units */
+  float windDecayX;   /* 0.2 per box unit */
+  float windDecayZ;   /* 0.3 per box unit */
+  uint32_t groundNx;
+  uint32_t groundNz;
+} rtp_cloud_env;
+
+/* The -D constants the reference bakes into its JIT program (Fluids.cpp:104-119,
+ * Boids.cpp:103-113, Clouds.cpp:134-147), each round-tripped through the reference's
+ * 10-decimal FloatToStr (utils/Utils.cpp:24-28) exactly as the OpenCL compiler sees it. */
+typedef struct rtp_grid_constants {
+  float absWall[3];          /* ABS_WALL_X/Y/Z */
+  uint32_t gridRes[3];       /* GRID_RES_X/Y/Z */
+  float cellSize;            /* GRID_CELL_SIZE_XYZ */
+  uint32_t numCells;         /* GRID_NUM_CELLS */
+  uint32_t maxPartsInCell;   /* NUM_MAX_PARTS_IN_CELL */
+  float effectRadius;        /* EFFECT_RADIUS (fluids, clouds) */
+  float effectRadiusSquared; /* EFFECT_RADIUS_SQUARED (boids) */
+  float poly6Coeff;          /* POLY6_COEFF */
+  float spikyCoeff;          /* SPIKY_COEFF */
+  float maxVel;              /* MAX_VEL */
+  uint32_t keyBound;         /* 1 + largest cell key fillCellIDs can emit (grid.cl:33-35) */
+  uint32_t keyBits;          /* bits needed to sort keys < keyBound */
+} rtp_grid_constants;
+
+/* Buffers of a handle (headless replacement of the VBOs and named CL buffers,
+ * physics/ocl/Fluids.cpp:128-150).  float4 buffers hold xyzw with w = 0. */
+typedef enum rtp_buffer {
+  RTP_BUF_POS = 0,        /* float4 p_pos */
+  RTP_BUF_VEL = 1,        /* float4 p_vel */
+  RTP_BUF_PRED_POS = 2,   /* float4 p_predPos (after the last step) */
+  RTP_BUF_DENSITY = 3,    /* float  p_density (last Jacobi iteration) */
+  RTP_BUF_LAMBDA = 4,     /* float  p_constFactor (last Jacobi iteration) */
+  RTP_BUF_TEMP = 5,       /* float  p_temp (clouds) */
+  RTP_BUF_VAPOR = 6,      /* float  p_vaporDens (clouds) */
+  RTP_BUF_CLOUD = 7,      /* float  p_cloudDens (clouds) */
+  RTP_BUF_BUOYANCY = 8,   /* float  p_buoyancy (clouds) */
+  RTP_BUF_ID = 9,         /* uint   particle id carried through every sort (p_partID) */
+  RTP_BUF_CELL_ID = 10,   /* uint   p_cellID: sorted cell keys of the last step */
+  RTP_BUF_CELL_TABLE = 11,/* uint2  c_startEndPartID in the reference's inclusive format */
+  RTP_BUF_VORTICITY = 12, /* float4 p_vort */
+  RTP_BUF_ACC = 13        /* float4 p_acc (boids) */
+} rtp_buffer;
+
+/* Per-kernel device time, collected when profiling is enabled (the reference's
+ * Context::runKernel profiling, physics/ocl/Context.cpp:692-705). */
+typedef struct rtp_kernel_time {
+  char name[48];
+  uint64_t launches;
+  double total_ms;
+} rtp_kernel_time;
+
+/* Step metrics (new: the reference has no physics metrics).  Filled by rtp_get_metrics
+ * from the current state on the device. */
+typedef struct rtp_metrics {
+  double meanDensityError;  /* mean |rho_i / rho0 - 1| over active particles */
+  double maxDensityError;
+  double kineticEnergy;     /* 0.5 * sum |v|^2 (unit mass) */
+  double meanNeighbours;    /* mean neighbours within the effect radius */
+  uint32_t neighbourHist[64];
+} rtp_metrics;
+
+/* Library. */
+const char* rtp_last_error(void);
+int rtp_abi_version(void);
+/* Host-only: derives the JIT constants of a model from its parameters
+ * (Fluids::createProgram, Fluids.cpp:97-126; Boids.cpp:96-120; Clouds.cpp:127-160). */
+int rtp_get_constants(int model, const rtp_model_params* params, rtp_grid_constants* out);
+/* Host-only: the reference's default parameters (JSON defaults Fluids.cpp:52-74,
+ * Boids.cpp:41-73, Clouds.cpp:67-102). */
+int rtp_fluid_params_default(rtp_fluid_params* out);
+int rtp_boids_params_default(rtp_boids_params* out);
+int rtp_cloud_params_default(rtp_cloud_params* out);
+int rtp_cloud_env_reference(rtp_cloud_env* out);
+
+/* Model lifecycle: Physics::CreateModel (Model.cpp:10-24), ~Model, Model::reset
+ * (Fluids.cpp:196-216, Boids.cpp:228-275, Clouds.cpp:379-399), Model::update
+ * (Fluids.cpp:400-471, Boids.cpp:323-384, Clouds.cpp:503-627) called nsteps times. */
+int rtp_create(int model, const rtp_model_params* params, void** out_handle);
+int rtp_destroy(void* handle);
+int rtp_reset(void* handle);
+int rtp_update(void* handle, uint32_t nsteps);
+
+/* Parameter setters: OclModel::updateModelWithInputJson -> transferKernelInputsToGPU
+ * (OclModel.hpp:48-57; Fluids.cpp:218-271; Boids.cpp:177-226; Clouds.cpp:279-377). */
+int rtp_set_fluid_params(void* handle, const rtp_fluid_params* p);
+int rtp_get_fluid_params(void* handle, rtp_fluid_params* p);
+int rtp_set_jacobi_iterations(void* handle, uint32_t iters); /* "Nb Jacobi Iterations" */
+int rtp_set_boids_params(void* handle, const rtp_boids_params* p);
+int rtp_set_boids_time_step(void* handle, float dt);  /* Boids.cpp:334 hard-codes 0.1 */
+int rtp_set_cloud_params(void* handle, const rtp_cloud_params* p);
+int rtp_set_cloud_environment(void* handle, const rtp_cloud_env* env, const float* groundTemp);
+/* cld_initTemperature + cld_initVaporDensity over the current positions, cloud = 0
+ * (Clouds.cpp:495-498, clouds.cl:116-135); call after uploading positions. */
+int rtp_clouds_init(void* handle);
+
+/* Model setters (physics/Model.hpp:106-128). */
+int rtp_set_nb_particles(void* handle, uint64_t n);
+int rtp_get_nb_particles(void* handle, uint64_t* n);
+int rtp_set_boundary(void* handle, int boundary);
+int rtp_set_dimension(void* handle, uint32_t dim); /* triggers reset, Model.hpp:109-113 */
+int rtp_set_case(void* handle, int pcase);
+int rtp_pause(void* handle, int pause);
+
+/* Buffers (replaces the CL-GL VBO sharing, physics/ocl/Context.cpp:710-750 and
+ * loadBufferFromHost).  `count` is in elements of the buffer's type (float4, float,
+ * uint or uint2) and must be <= maxNbParticles (or numCells for the cell table). */
+int rtp_upload(void* handle, int buffer, const void* host, uint64_t count);
+int rtp_download(void* handle, int buffer, void* host, uint64_t count);
+int rtp_device_ptr(void* handle, int buffer, void** dptr);
+int rtp_stream(void* handle, void** stream);
+int rtp_synchronize(void* handle);
+
+/* Profiling (OclModel::isProfilingEnabled/enableProfiling, OclModel.hpp:28-38). */
+int rtp_enable_profiling(void* handle, int enable);
+int rtp_is_profiling_enabled(void* handle, int* enabled);
+int rtp_get_kernel_times(void* handle, rtp_kernel_time* out, uint32_t capacity, uint32_t* count);
+int rtp_reset_kernel_times(void* handle);
+/* Device-timed steps: runs `nsteps` updates, each bracketed by CUDA events on the
+ * handle's stream; when `flush_bytes` > 0 a buffer of that size is overwritten
+ * before every step (outside the timed interval) so every step starts with a cold L2. */
+int rtp_time_steps(void* handle, uint32_t nsteps, uint64_t flush_bytes, double* total_ms);
+
+/* Metrics (new). */
+int rtp_get_metrics(void* handle, rtp_metrics* out);
+
+/* Grid / sort operators on caller-owned device memory, ordered on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  They are the stand-alone forms of
+ * fillCellIDs (grid.cl:76-86), RadixSort::sort (physics/utils/RadixSort.cpp:122-189)
+ * and resetStartEndCell/fillStartCell/fillEndCell/adjustEndCell (grid.cl:91-152). */
+int rtp_fill_cell_ids(const rtp_grid_constants* c, const float* d_pos4, uint32_t n,
+                      uint32_t* d_keys, void* stream);
+/* Stable sort of n keys < 2^keyBits: keys_out = keys in ascending order, equal keys in
+ * input order; perm_out[i] = input index of keys_out[i].  `d_scratch` must hold
+ * rtp_radix_sort_scratch_bytes(n, keyBits) bytes. */
+int rtp_radix_sort_scratch_bytes(uint32_t n, uint32_t keyBits, size_t* bytes);
+int rtp_radix_sort(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits,
+                   uint32_t* d_keys_out, uint32_t* d_perm_out,
+                   void* d_scratch, size_t scratch_bytes, void* stream);
+/* Cell table from n sorted keys, in the reference's format: uint2 per cell,
+ * (start, end) inclusive, empty = (1, 0), capped at maxPartsInCell. */
+int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_keys,
+                         uint32_t n, uint32_t* d_table2, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTP_H */

@@ -1,0 +1,202 @@
+"""Python front end of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: this package is the checker.  tests/, __graft_entry__.smoke()
+and bench.py's CPU legs import it; the product package never does.  The C++ restatement
+of the reference kernels lives in oracle.cpp; see oracle.h for what each function follows.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from realtimeparticles_gb300 import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build(quiet=True):
+    """Compile liboracle.so with the Makefile next to this file."""
+    out = subprocess.run(["make", "-C", _HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        src = os.path.join(_HERE, "oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.or_derive_constants.argtypes = [C.c_int, C.POINTER(abi.ModelParams), C.POINTER(abi.GridConstants)]
+        L.or_fill_cell_ids.argtypes = [C.POINTER(abi.GridConstants), P, C.c_uint32, P]
+        L.or_stable_sort.argtypes = [P, C.c_uint32, P, P]
+        L.or_cell_table.argtypes = [C.POINTER(abi.GridConstants), P, C.c_uint32, P]
+        L.or_fluids_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.c_uint32,
+                                     C.c_uint32, P]
+        L.or_boids_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.BoidsParams), C.c_float,
+                                    C.c_int, C.c_uint32, P]
+        L.or_clouds_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
+                                     C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P, C.c_uint32,
+                                     C.c_uint32, P]
+        L.or_clouds_init.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.CloudParams),
+                                     C.POINTER(abi.CloudEnv), P, C.c_uint32, P]
+        L.or_fld_density.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P,
+                                     C.c_uint32, P]
+        L.or_fld_lambda.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P, P,
+                                    C.c_uint32, P]
+        L.or_fld_correction.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P, P,
+                                        C.c_uint32, P]
+        L.or_fluid_metrics.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P, P,
+                                       C.c_uint32, C.POINTER(abi.Metrics)]
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_get_threads.restype = C.c_int
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class _State(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "pos", "vel", "predPos", "totCorrPos", "acc", "vort", "density", "lambda_", "temp", "vapor",
+        "cloud", "buoyancy", "id", "cellId", "table")]
+
+
+_STATE_KEYS = {"pos": "pos", "vel": "vel", "predPos": "predPos", "totCorrPos": "totCorrPos",
+               "acc": "acc", "vort": "vort", "density": "density", "lambda": "lambda_", "temp": "temp",
+               "vapor": "vapor", "cloud": "cloud", "buoyancy": "buoyancy", "id": "id",
+               "cellId": "cellId", "table": "table"}
+
+
+def _state(d):
+    s = _State()
+    for k, f in _STATE_KEYS.items():
+        a = d.get(k)
+        if a is not None:
+            assert a.flags["C_CONTIGUOUS"], k
+            setattr(s, f, a.ctypes.data)
+    return s
+
+
+def set_threads(n):
+    lib().or_set_threads(int(n))
+
+
+def get_threads():
+    return lib().or_get_threads()
+
+
+def derive_constants(model, mp):
+    c = abi.GridConstants()
+    rc = lib().or_derive_constants(int(model), C.byref(mp), C.byref(c))
+    if rc != 0:
+        raise ValueError("or_derive_constants failed: %d" % rc)
+    return c
+
+
+def fill_cell_ids(c, pos):
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    n = pos.shape[0]
+    keys = np.empty(n, np.uint32)
+    lib().or_fill_cell_ids(C.byref(c), _p(pos), n, _p(keys))
+    return keys
+
+
+def stable_sort(keys):
+    keys = np.ascontiguousarray(keys, dtype=np.uint32)
+    n = keys.shape[0]
+    sk = np.empty(n, np.uint32)
+    perm = np.empty(n, np.uint32)
+    lib().or_stable_sort(_p(keys), n, _p(sk), _p(perm))
+    return sk, perm
+
+
+def cell_table(c, sorted_keys):
+    sorted_keys = np.ascontiguousarray(sorted_keys, dtype=np.uint32)
+    t = np.empty((c.numCells, 2), np.uint32)
+    lib().or_cell_table(C.byref(c), _p(sorted_keys), sorted_keys.shape[0], _p(t))
+    return t
+
+
+def new_state(n, c=None, model=abi.FLUIDS):
+    """Zeroed state arrays for n particles (float4 arrays are (n, 4))."""
+    f4 = lambda: np.zeros((n, 4), np.float32)
+    f1 = lambda: np.zeros(n, np.float32)
+    d = {"pos": f4(), "vel": f4(), "predPos": f4(), "density": f1(), "lambda": f1(),
+         "vort": f4(), "id": np.arange(n, dtype=np.uint32), "cellId": np.zeros(n, np.uint32)}
+    if model == abi.BOIDS:
+        d["acc"] = f4()
+    if model == abi.CLOUDS:
+        d.update(totCorrPos=f4(), temp=f1(), vapor=f1(), cloud=f1(), buoyancy=f1())
+    if c is not None:
+        d["table"] = np.zeros((c.numCells, 2), np.uint32)
+    return d
+
+
+def fluids_step(c, fp, iters, st):
+    n = st["pos"].shape[0]
+    s = _state(st)
+    rc = lib().or_fluids_step(C.byref(c), C.byref(fp), int(iters), n, C.byref(s))
+    if rc != 0:
+        raise ValueError("or_fluids_step failed: %d" % rc)
+
+
+def boids_step(c, bp, dt, boundary, st):
+    n = st["pos"].shape[0]
+    s = _state(st)
+    rc = lib().or_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), n, C.byref(s))
+    if rc != 0:
+        raise ValueError("or_boids_step failed: %d" % rc)
+
+
+def clouds_init(c, cp, env, ground, st):
+    n = st["pos"].shape[0]
+    s = _state(st)
+    g = None if ground is None else np.ascontiguousarray(ground, dtype=np.float32)
+    lib().or_clouds_init(C.byref(c), C.byref(cp), C.byref(env), _p(g), n, C.byref(s))
+
+
+def clouds_step(c, fp, cp, env, ground, iters, st):
+    n = st["pos"].shape[0]
+    s = _state(st)
+    g = None if ground is None else np.ascontiguousarray(ground, dtype=np.float32)
+    rc = lib().or_clouds_step(C.byref(c), C.byref(fp), C.byref(cp), C.byref(env), _p(g), int(iters), n,
+                              C.byref(s))
+    if rc != 0:
+        raise ValueError("or_clouds_step failed: %d" % rc)
+
+
+def fld_density(c, fp, pred, table):
+    n = pred.shape[0]
+    out = np.empty(n, np.float32)
+    lib().or_fld_density(C.byref(c), C.byref(fp), _p(pred), _p(table), n, _p(out))
+    return out
+
+
+def fld_lambda(c, fp, pred, density, table):
+    n = pred.shape[0]
+    out = np.empty(n, np.float32)
+    lib().or_fld_lambda(C.byref(c), C.byref(fp), _p(pred), _p(density), _p(table), n, _p(out))
+    return out
+
+
+def fld_correction(c, fp, pred, lam, table):
+    n = pred.shape[0]
+    out = np.empty((n, 4), np.float32)
+    lib().or_fld_correction(C.byref(c), C.byref(fp), _p(pred), _p(lam), _p(table), n, _p(out))
+    return out
+
+
+def fluid_metrics(c, fp, pred, vel, table):
+    m = abi.Metrics()
+    lib().or_fluid_metrics(C.byref(c), C.byref(fp), _p(pred), _p(vel), _p(table), pred.shape[0], C.byref(m))
+    return m

@@ -1,0 +1,867 @@
+// oracle.cpp - CPU restatement of the RealTimeParticles simulation step.
+//
+// TEST INFRASTRUCTURE ONLY (the checker): loaded by tests/, __graft_entry__.smoke() and
+// bench.py's CPU legs, never by the product.  Each function follows one reference kernel
+// (physics/ocl/kernels/*.cl) or host sequence (physics/ocl/*.cpp) in the same order of
+// operations, so that float results agree with the reference's kernels compiled for a CPU.
+// Build: oracle/Makefile (-ffp-contract=off, OpenMP over particles).
+//
+// OpenCL builtins are evaluated with standard C++ math:
+//   fast_length(v)   = sqrt(dot(v, v))                   (dot over all four lanes)
+//   fast_normalize(v), normalize(v) = v / sqrt(dot(v, v)), and v itself when dot(v, v) == 0
+//   pow(x, k) for the integer-valued exponents used here (2, 3, artPressureExp) = repeated
+//                      multiplication, which keeps the sign of a negative base as pow must.
+//   step(e, x) = x < e ? 0 : 1;  clamp(x, a, b) = fmin(fmax(x, a), b)
+//   double literals in saturationVaporDensity (clouds.cl:98) are evaluated in double.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct f4 {
+  float x, y, z, w;
+};
+
+inline f4 mk(float x, float y, float z, float w) { return f4{x, y, z, w}; }
+inline f4 splat(float v) { return f4{v, v, v, v}; }
+inline f4 operator+(f4 a, f4 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline f4 operator-(f4 a, f4 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+inline f4 operator*(f4 a, float s) { return mk(a.x * s, a.y * s, a.z * s, a.w * s); }
+inline f4 operator*(float s, f4 a) { return mk(s * a.x, s * a.y, s * a.z, s * a.w); }
+inline f4 operator/(f4 a, float s) { return mk(a.x / s, a.y / s, a.z / s, a.w / s); }
+inline float dot(f4 a, f4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+inline float flen(f4 a) { return std::sqrt(dot(a, a)); }
+inline f4 fnormalize(f4 a) {
+  const float d = dot(a, a);
+  if (d == 0.0f) return a;
+  return a / std::sqrt(d);
+}
+// OpenCL cross() on float4: w = 0.
+inline f4 cross(f4 a, f4 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x, 0.0f);
+}
+inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
+inline f4 clamp4(f4 v, f4 lo, f4 hi) {
+  return mk(clampf(v.x, lo.x, hi.x), clampf(v.y, lo.y, hi.y), clampf(v.z, lo.z, hi.z),
+            clampf(v.w, lo.w, hi.w));
+}
+inline f4 clamp4s(f4 v, float lo, float hi) {
+  return mk(clampf(v.x, lo, hi), clampf(v.y, lo, hi), clampf(v.z, lo, hi), clampf(v.w, lo, hi));
+}
+inline float stepf(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
+inline float powi(float x, uint32_t k) {
+  if (k == 0) return 1.0f;
+  float r = x;
+  for (uint32_t i = 1; i < k; ++i) r = r * x;
+  return r;
+}
+
+inline f4 ld4(const float* a, size_t i) { return mk(a[4 * i], a[4 * i + 1], a[4 * i + 2], a[4 * i + 3]); }
+inline void st4(float* a, size_t i, f4 v) {
+  a[4 * i] = v.x;
+  a[4 * i + 1] = v.y;
+  a[4 * i + 2] = v.z;
+  a[4 * i + 3] = v.w;
+}
+
+constexpr float FLOAT_EPS = 0.00000001f;    // define.cl:6
+constexpr float ABS_GRAVITY_ACC_Y = 9.81f;  // define.cl:8
+constexpr float PI_F = 3.1415927f;          // utils/Math.hpp:69
+
+// Utils::FloatToStr (utils/Utils.cpp:24-28) prints a float with 10 fixed decimals; the
+// OpenCL compiler parses that literal back to a float.
+float round_trip(float v) {
+  char buf[128];
+  std::snprintf(buf, sizeof buf, "%.10f", (double)v);
+  return std::strtof(buf, nullptr);
+}
+
+struct Grid {
+  float W[3];
+  int R[3];
+  float cell;
+  uint32_t nc;
+  uint32_t cap;
+  explicit Grid(const rtp_grid_constants* c) {
+    for (int a = 0; a < 3; ++a) {
+      W[a] = c->absWall[a];
+      R[a] = (int)c->gridRes[a];
+    }
+    cell = c->cellSize;
+    nc = c->numCells;
+    cap = c->maxPartsInCell;
+  }
+  // getCell3DIndexFromPos, grid.cl:14-24.
+  inline void cell3(f4 p, uint32_t out[3]) const {
+    const float v[3] = {p.x, p.y, p.z};
+    for (int a = 0; a < 3; ++a) {
+      const float q = clampf(v[a], -W[a], W[a]) + W[a];
+      out[a] = (uint32_t)std::floor(q / cell);
+    }
+  }
+  // getCell1DIndexFromPos, grid.cl:29-38.
+  inline uint32_t cell1(f4 p) const {
+    uint32_t c[3];
+    cell3(p, c);
+    return c[0] * (uint32_t)R[2] * (uint32_t)R[1] + c[1] * (uint32_t)R[2] + c[2];
+  }
+};
+
+// Neighbour loop of the fluids kernels (fluids.cl:101-123): 27 cells wrapped modulo the
+// grid resolution, then every e in the cell's inclusive range.
+template <class F>
+inline void fluid_neighbours(const Grid& g, const uint32_t* table, f4 pos, F&& f) {
+  uint32_t c3[3];
+  g.cell3(pos, c3);
+  const int cx = (int)c3[0], cy = (int)c3[1], cz = (int)c3[2];
+  for (int iX = -1; iX <= 1; ++iX)
+    for (int iY = -1; iY <= 1; ++iY)
+      for (int iZ = -1; iZ <= 1; ++iZ) {
+        const int nx = (cx + iX + g.R[0]) % g.R[0];
+        const int ny = (cy + iY + g.R[1]) % g.R[1];
+        const int nz = (cz + iZ + g.R[2]) % g.R[2];
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= g.R[0] || ny >= g.R[1] || nz >= g.R[2]) continue;
+        const uint32_t c1 = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2] + (uint32_t)nz;
+        const uint32_t s = table[2 * c1], e = table[2 * c1 + 1];
+        for (uint32_t k = s; k <= e; ++k) f(k);
+      }
+}
+
+// Neighbour loop of the clouds kernels (clouds.cl:326-356): x and z periodic with an image
+// shift of 2W * sign, y walls (out-of-range cells skipped).
+template <class F>
+inline void cloud_neighbours(const Grid& g, const uint32_t* table, f4 pos, F&& f) {
+  uint32_t c3[3];
+  g.cell3(pos, c3);
+  const int cx = (int)c3[0], cy = (int)c3[1], cz = (int)c3[2];
+  for (int iX = -1; iX <= 1; ++iX)
+    for (int iY = -1; iY <= 1; ++iY)
+      for (int iZ = -1; iZ <= 1; ++iZ) {
+        f4 sign = splat(0.0f);
+        const int nx = (cx + iX + g.R[0]) % g.R[0];
+        const int ny = (cy + iY + g.R[1]) % g.R[1];
+        const int nz = (cz + iZ + g.R[2]) % g.R[2];
+        if ((cx + iX) >= g.R[0]) sign.x = 2.0f;
+        else if ((cx + iX) < 0) sign.x = -2.0f;
+        if (((cy + iY) >= g.R[1]) || ((cy + iY) < 0)) continue;
+        if ((cz + iZ) >= g.R[2]) sign.z = 2.0f;
+        else if ((cz + iZ) < 0) sign.z = -2.0f;
+        const uint32_t c1 = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2] + (uint32_t)nz;
+        const uint32_t s = table[2 * c1], e = table[2 * c1 + 1];
+        const f4 shift = mk(g.W[0] * sign.x, g.W[1] * sign.y, g.W[2] * sign.z, 0.0f * sign.w);
+        for (uint32_t k = s; k <= e; ++k) f(k, shift);
+      }
+}
+
+// Neighbour loop of the boids kernel (boids.cl:78-113): no wrap, out-of-range cells skipped.
+template <class F>
+inline void boid_neighbours(const Grid& g, const uint32_t* table, f4 pos, F&& f) {
+  uint32_t c3[3];
+  g.cell3(pos, c3);
+  for (int iX = -1; iX <= 1; ++iX)
+    for (int iY = -1; iY <= 1; ++iY)
+      for (int iZ = -1; iZ <= 1; ++iZ) {
+        const int nx = (int)c3[0] + iX, ny = (int)c3[1] + iY, nz = (int)c3[2] + iZ;
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= g.R[0] || ny >= g.R[1] || nz >= g.R[2]) continue;
+        const uint32_t c1 = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2] + (uint32_t)nz;
+        const uint32_t s = table[2 * c1], e = table[2 * c1 + 1];
+        for (uint32_t k = s; k <= e; ++k) f(k);
+      }
+}
+
+struct Sph {
+  float h, poly6c, spikyc;
+  explicit Sph(const rtp_grid_constants* c) : h(c->effectRadius), poly6c(c->poly6Coeff), spikyc(c->spikyCoeff) {}
+  // poly6 / poly6L, sph.cl:10-19.
+  inline float poly6L(float L) const { return (1.0f - stepf(h, L)) * poly6c * powi(h * h - L * L, 3); }
+  inline float poly6(f4 v) const { return poly6L(flen(v)); }
+  // gradSpiky, sph.cl:26-34.
+  inline f4 grad(f4 v) const {
+    const float L = flen(v);
+    if (L <= FLOAT_EPS) return splat(0.0f);
+    return v * (1.0f - stepf(h, L)) * spikyc * -3.0f * powi(h - L, 2) / L;
+  }
+  // artPressure, fluids.cl:51-57 (== clouds.cl:105-111).
+  inline float artPressure(f4 v, const rtp_fluid_params* p) const {
+    if (p->isArtPressureEnabled == 0) return 0.0f;
+    return -p->artPressureCoeff * powi(poly6(v) / poly6L(p->artPressureRadius * h), p->artPressureExp);
+  }
+};
+
+#define OR_PARALLEL_FOR _Pragma("omp parallel for schedule(static)")
+
+void sort_and_table(const rtp_grid_constants* c, uint32_t n, std::vector<uint32_t>& keys,
+                    std::vector<uint32_t>& perm, uint32_t* sorted_keys_out, uint32_t* table) {
+  std::vector<uint32_t> sk(n);
+  perm.resize(n);
+  or_stable_sort(keys.data(), n, sk.data(), perm.data());
+  or_cell_table(c, sk.data(), n, table);
+  if (sorted_keys_out) std::memcpy(sorted_keys_out, sk.data(), sizeof(uint32_t) * n);
+  keys.swap(sk);
+}
+
+void gather4(float* a, const std::vector<uint32_t>& perm, uint32_t n) {
+  if (!a) return;
+  std::vector<float> t(a, a + 4 * (size_t)n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) st4(a, i, ld4(t.data(), perm[i]));
+}
+template <class T>
+void gather1(T* a, const std::vector<uint32_t>& perm, uint32_t n) {
+  if (!a) return;
+  std::vector<T> t(a, a + n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) a[i] = t[perm[i]];
+}
+
+}  // namespace
+
+extern "C" {
+
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+  (void)n;
+#endif
+}
+
+int or_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int or_derive_constants(int model, const rtp_model_params* p, rtp_grid_constants* c) {
+  if (!p || !c) return RTP_ERR_INVALID_ARGUMENT;
+  std::memset(c, 0, sizeof *c);
+  for (int a = 0; a < 3; ++a) {
+    if (p->gridRes[a] == 0 || !(p->boxSize[a] > 0.0f)) return RTP_ERR_INVALID_ARGUMENT;
+    c->gridRes[a] = p->gridRes[a];
+    c->absWall[a] = round_trip(p->boxSize[a] / 2.0f);  // Fluids.cpp:108-110
+  }
+  const float bx = p->boxSize[0];
+  const float rx = (float)p->gridRes[0];
+  c->cellSize = round_trip(bx / rx);  // Fluids.cpp:114
+  c->numCells = p->gridRes[0] * p->gridRes[1] * p->gridRes[2];
+  const float effectRadius = bx / rx;  // Fluids.cpp:104
+  c->effectRadius = round_trip(effectRadius);
+  c->effectRadiusSquared =
+      round_trip(1.0f * bx * bx / (float)(p->gridRes[0] * p->gridRes[0]));  // Boids.cpp:104
+  c->poly6Coeff = round_trip(315.0f / (64.0f * PI_F * std::pow(effectRadius, 9.f)));  // :117
+  c->spikyCoeff = round_trip(15.0f / (PI_F * std::pow(effectRadius, 6.f)));           // :118
+  c->maxVel = round_trip(30.0f);                                                      // :119
+  uint32_t cap = p->maxNbPartsInCell;
+  if (cap == 0) cap = (model == RTP_MODEL_BOIDS) ? 3000u : 100u;  // Boids.cpp:78, Fluids.cpp:79
+  c->maxPartsInCell = cap;
+  // Largest key: every axis at +W (grid.cl:33-35 aliases index == GRID_RES).
+  Grid g(c);
+  const f4 top = mk(c->absWall[0], c->absWall[1], c->absWall[2], 0.0f);
+  c->keyBound = g.cell1(top) + 1u;
+  uint32_t bits = 0;
+  while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)c->keyBound) ++bits;
+  c->keyBits = bits;
+  return RTP_OK;
+}
+
+void or_fill_cell_ids(const rtp_grid_constants* c, const float* pos4, uint32_t n, uint32_t* keys) {
+  const Grid g(c);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) keys[i] = g.cell1(ld4(pos4, i));
+}
+
+void or_stable_sort(const uint32_t* keys, uint32_t n, uint32_t* keys_out, uint32_t* perm) {
+  std::vector<uint32_t> idx(n);
+  for (uint32_t i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
+  for (uint32_t i = 0; i < n; ++i) {
+    perm[i] = idx[i];
+    keys_out[i] = keys[idx[i]];
+  }
+}
+
+void or_cell_table(const rtp_grid_constants* c, const uint32_t* k, uint32_t n, uint32_t* t) {
+  const uint32_t nc = c->numCells;
+  // resetStartEndCell, grid.cl:91-96.
+  for (uint32_t i = 0; i < nc; ++i) {
+    t[2 * i] = 1;
+    t[2 * i + 1] = 0;
+  }
+  // fillStartCell, grid.cl:101-116: ID 0 never starts a cell.
+  for (uint32_t i = 1; i < n; ++i)
+    if (k[i] < nc && k[i] != k[i - 1]) t[2 * k[i]] = i;
+  // fillEndCell, grid.cl:121-138: index n holds an inactive sentinel key.
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t right = (i + 1 < n) ? k[i + 1] : 0xFFFFFFFFu;
+    if (k[i] < nc && k[i] != right) t[2 * k[i] + 1] = i;
+  }
+  // adjustEndCell, grid.cl:143-152.
+  for (uint32_t i = 0; i < nc; ++i) {
+    const uint32_t s = t[2 * i], e = t[2 * i + 1];
+    if (e > s) t[2 * i + 1] = s + std::min(e - s, c->maxPartsInCell);
+  }
+}
+
+void or_fld_density(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* pred,
+                    const uint32_t* table, uint32_t n, float* density) {
+  (void)p;
+  const Grid g(c);
+  const Sph k(c);
+  // fld_computeDensity, fluids.cl:80-126.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 pos = ld4(pred, i);
+    float rho = 0.0f;
+    fluid_neighbours(g, table, pos, [&](uint32_t e) { rho += k.poly6(pos - ld4(pred, e)); });
+    density[i] = rho;
+  }
+}
+
+void or_fld_lambda(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* pred,
+                   const float* density, const uint32_t* table, uint32_t n, float* lambda) {
+  const Grid g(c);
+  const Sph k(c);
+  // fld_computeConstraintFactor, fluids.cl:131-193.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 pos = ld4(pred, i);
+    const float densityC = density[i] / p->restDensity - 1.0f;
+    f4 sumGradCi = splat(0.0f);
+    float sumSqGradC = 0.0f;
+    fluid_neighbours(g, table, pos, [&](uint32_t e) {
+      const f4 grad = k.grad(pos - ld4(pred, e));
+      sumGradCi = sumGradCi + grad;
+      sumSqGradC += dot(grad, grad);
+    });
+    sumSqGradC += dot(sumGradCi, sumGradCi);
+    sumSqGradC /= p->restDensity * p->restDensity;
+    lambda[i] = -densityC / (sumSqGradC + p->relaxCFM);
+  }
+}
+
+void or_fld_correction(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* pred,
+                       const float* lambda, const uint32_t* table, uint32_t n, float* corr) {
+  const Grid g(c);
+  const Sph k(c);
+  // fld_computeConstraintCorrection, fluids.cl:198-247.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 pos = ld4(pred, i);
+    const float lambdaI = lambda[i];
+    f4 acc = splat(0.0f);
+    fluid_neighbours(g, table, pos, [&](uint32_t e) {
+      const f4 vec = pos - ld4(pred, e);
+      acc = acc + (lambdaI + lambda[e] + k.artPressure(vec, p)) * k.grad(vec);
+    });
+    st4(corr, i, acc / p->restDensity);
+  }
+}
+
+int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters,
+                   uint32_t n, or_state* s) {
+  if (!c || !p || !s || !s->pos || !s->vel || !s->predPos) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const float dt = p->timeStep;
+  float* pos = s->pos;
+  float* vel = s->vel;
+  float* pred = s->predPos;
+
+  // fld_predictPosition, fluids.cl:62-74 (Fluids.cpp:412).
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 gdt = mk(0.0f * dt, -ABS_GRAVITY_ACC_Y * dt, 0.0f * dt, 0.0f * dt);
+    const f4 newVel = ld4(vel, i) + gdt;
+    st4(pred, i, ld4(pos, i) + newVel * dt);
+  }
+  // fillCellIDs(predPos) (Fluids.cpp:415), sort of {pos, col, vel, predPos} (:417; col is
+  // render-only), cell table (:419-424).
+  std::vector<uint32_t> keys(n), perm;
+  or_fill_cell_ids(c, pred, n, keys.data());
+  std::vector<uint32_t> table(2 * (size_t)c->numCells);
+  sort_and_table(c, n, keys, perm, s->cellId, table.data());
+  gather4(pos, perm, n);
+  gather4(vel, perm, n);
+  gather4(pred, perm, n);
+  gather1(s->id, perm, n);
+  if (s->table) std::memcpy(s->table, table.data(), sizeof(uint32_t) * table.size());
+
+  std::vector<float> density(n), lambda(n), corr(4 * (size_t)n);
+  const f4 lo = mk(-g.W[0] + 0.01f, -g.W[1] + 0.01f, -g.W[2] + 0.01f, 0.0f);
+  const f4 hi = mk(g.W[0] - 0.1f, g.W[1] - 0.1f, g.W[2] - 0.1f, 0.0f);
+  // Jacobi loop, Fluids.cpp:427-439.
+  for (uint32_t it = 0; it < iters; ++it) {
+    // fld_applyBoundaryCondition, fluids.cl:435-439.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, clamp4(ld4(pred, i), lo, hi));
+    or_fld_density(c, p, pred, table.data(), n, density.data());
+    or_fld_lambda(c, p, pred, density.data(), table.data(), n, lambda.data());
+    or_fld_correction(c, p, pred, lambda.data(), table.data(), n, corr.data());
+    // fld_correctPosition, fluids.cl:252-258.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, ld4(pred, i) + ld4(corr.data(), i));
+  }
+  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
+  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+
+  // fld_updateVel, fluids.cl:263-273 (Fluids.cpp:442).
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i)
+    st4(vel, i, clamp4s((ld4(pred, i) - ld4(pos, i)) / (dt + FLOAT_EPS), -c->maxVel, c->maxVel));
+
+  if (p->isVorticityConfEnabled) {  // Fluids.cpp:444-454
+    std::vector<float> vort(4 * (size_t)n), velIn(4 * (size_t)n);
+    // fld_computeVorticity, fluids.cl:278-324.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), v = ld4(vel, i);
+      f4 w = splat(0.0f);
+      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
+        w = w + cross(ld4(vel, e) - v, k.grad(x - ld4(pred, e)));
+      });
+      st4(vort.data(), i, w);
+    }
+    // fld_applyVorticityConfinement, fluids.cl:329-377 (writes only vel[ID]).
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), w = ld4(vort.data(), i);
+      f4 eta = splat(0.0f);
+      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
+        eta = eta + flen(ld4(vort.data(), e)) * k.grad(x - ld4(pred, e));
+      });
+      st4(vel, i, ld4(vel, i) + p->vorticityConfCoeff * cross(fnormalize(eta), w) * dt);
+    }
+    // copyBuffer(p_vel, p_velInViscosity), Fluids.cpp:451.
+    std::memcpy(velIn.data(), vel, sizeof(float) * 4 * n);
+    // fld_applyXsphViscosityCorrection, fluids.cl:383-430.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), v = ld4(velIn.data(), i);
+      f4 visc = splat(0.0f);
+      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
+        visc = visc + (ld4(velIn.data(), e) - v) * k.poly6(x - ld4(pred, e));
+      });
+      st4(vel, i, v + p->xsphViscosityCoeff * visc);
+    }
+    if (s->vort) std::memcpy(s->vort, vort.data(), sizeof(float) * 4 * n);
+  }
+  // fld_updatePosition, fluids.cl:444-450.
+  std::memcpy(pos, pred, sizeof(float) * 4 * n);
+  return RTP_OK;
+}
+
+void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* pred,
+                      const float* vel, const uint32_t* table, uint32_t n, rtp_metrics* m) {
+  std::memset(m, 0, sizeof *m);
+  if (n == 0) return;
+  const Grid g(c);
+  const Sph k(c);
+  std::vector<float> rho(n);
+  std::vector<uint32_t> nb(n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 x = ld4(pred, i);
+    float r = 0.0f;
+    uint32_t cnt = 0;
+    fluid_neighbours(g, table, x, [&](uint32_t e) {
+      const f4 v = x - ld4(pred, e);
+      r += k.poly6(v);
+      if ((int64_t)e != i && flen(v) < k.h) ++cnt;
+    });
+    rho[i] = r;
+    nb[i] = cnt;
+  }
+  double sum = 0.0, mx = 0.0, ke = 0.0, nsum = 0.0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double err = std::fabs((double)rho[i] / (double)p->restDensity - 1.0);
+    sum += err;
+    mx = std::max(mx, err);
+    const f4 v = ld4(vel, i);
+    ke += 0.5 * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+    nsum += nb[i];
+    m->neighbourHist[std::min<uint32_t>(nb[i], 63)]++;
+  }
+  m->meanDensityError = sum / n;
+  m->maxDensityError = mx;
+  m->kineticEnergy = ke;
+  m->meanNeighbours = nsum / n;
+}
+
+int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary,
+                  uint32_t n, or_state* s) {
+  if (!c || !p || !s || !s->pos || !s->vel) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  float* pos = s->pos;
+  float* vel = s->vel;
+  // fillCellIDs(pos), Boids.cpp:335; sort {pos, col, vel, acc} (:337); table (:339-344).
+  std::vector<uint32_t> keys(n), perm;
+  or_fill_cell_ids(c, pos, n, keys.data());
+  std::vector<uint32_t> table(2 * (size_t)c->numCells);
+  sort_and_table(c, n, keys, perm, s->cellId, table.data());
+  gather4(pos, perm, n);
+  gather4(vel, perm, n);
+  gather1(s->id, perm, n);
+  if (s->table) std::memcpy(s->table, table.data(), sizeof(uint32_t) * table.size());
+
+  std::vector<float> acc(4 * (size_t)n);
+  const float R2 = c->effectRadiusSquared;
+  // bd_applyBoidsRulesWithGrid3D, boids.cl:46-132.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 x = ld4(pos, i);
+    int count = 0;
+    f4 newAcc = splat(0.0f), avgPos = splat(0.0f), avgVel = splat(0.0f), repulse = splat(0.0f);
+    boid_neighbours(g, table.data(), x, [&](uint32_t e) {
+      const f4 posN = ld4(pos, e);
+      const f4 vec = x - posN;
+      const float sq = dot(vec, vec);
+      if (sq < R2 && sq > FLOAT_EPS) {
+        avgPos = avgPos + posN;
+        avgVel = avgVel + fnormalize(ld4(vel, e));
+        repulse = repulse + vec / sq;
+        ++count;
+      }
+    });
+    if (count != 0) {
+      avgPos = avgPos / (float)count;
+      avgPos = avgPos - x;
+      avgPos = fnormalize(avgPos) * p->velocityScale;
+      avgVel = fnormalize(avgVel) * p->velocityScale;
+      repulse = fnormalize(repulse) * p->velocityScale;
+      newAcc = avgVel * p->alignmentScale + repulse * p->separationScale + avgPos * p->cohesionScale;
+    }
+    st4(acc.data(), i, newAcc);
+  }
+  // bd_updateVel, boids.cl:246-259 (maxVelocity = velocityScale, Boids.cpp:217).
+  const float vmax = p->velocityScale;
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 nv = ld4(vel, i) + ld4(acc.data(), i) * dt;
+    const float norm = clampf(flen(nv), 0.2f * vmax, vmax);
+    st4(vel, i, fnormalize(nv) * norm);
+  }
+  const f4 lo = mk(-g.W[0], -g.W[1], -g.W[2], 0.0f), hi = mk(g.W[0], g.W[1], g.W[2], 0.0f);
+  if (boundary == RTP_BOUNDARY_CYCLIC_WALL) {
+    // bd_updatePosAndApplyPeriodicBC, boids.cl:289-315.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 np = ld4(pos, i) + ld4(vel, i) * dt;
+      f4 cp = clamp4(np, lo, hi);
+      if (!(cp.x == np.x)) cp.x *= -1.0f;
+      if (!(cp.y == np.y)) cp.y *= -1.0f;
+      if (!(cp.z == np.z)) cp.z *= -1.0f;
+      st4(pos, i, cp);
+    }
+  } else {
+    // bd_updatePosAndApplyWallBC, boids.cl:264-284.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 np = ld4(pos, i) + ld4(vel, i) * dt;
+      const f4 cp = clamp4(np, lo, hi);
+      st4(pos, i, cp);
+      if (!(cp.x == np.x && cp.y == np.y && cp.z == np.z)) st4(vel, i, ld4(vel, i) * -0.5f);
+    }
+  }
+  if (s->acc) std::memcpy(s->acc, acc.data(), sizeof(float) * 4 * n);
+  return RTP_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Clouds (clouds.cl, Clouds.cpp:503-610).
+namespace {
+
+struct CloudEnv {
+  float W[3];
+  float T0, lapse, heatDecay, windX, windZ;
+  const float* ground;
+  uint32_t nx, nz;
+  CloudEnv(const rtp_grid_constants* c, const rtp_cloud_env* e, const float* g) {
+    for (int a = 0; a < 3; ++a) W[a] = c->absWall[a];
+    T0 = e->groundTemp0;
+    lapse = e->lapseRate;
+    heatDecay = e->heatDecay;
+    windX = e->windDecayX;
+    windZ = e->windDecayZ;
+    ground = (g && e->groundNx >= 2 && e->groundNz >= 2) ? g : nullptr;
+    nx = e->groundNx;
+    nz = e->groundNz;
+  }
+  // Ground temperature at (x, z): bilinear in a nx x nz table spanning the box floor.
+  inline float groundTemp(float x, float z) const {
+    if (!ground) return T0;
+    const float u = clampf((x + W[0]) / (2.0f * W[0]), 0.0f, 1.0f) * (float)(nx - 1);
+    const float v = clampf((z + W[2]) / (2.0f * W[2]), 0.0f, 1.0f) * (float)(nz - 1);
+    const uint32_t i0 = std::min((uint32_t)std::floor(u), nx - 2);
+    const uint32_t k0 = std::min((uint32_t)std::floor(v), nz - 2);
+    const float fu = u - (float)i0, fv = v - (float)k0;
+    const float a = ground[i0 * nz + k0], b = ground[i0 * nz + k0 + 1];
+    const float cc = ground[(i0 + 1) * nz + k0], d = ground[(i0 + 1) * nz + k0 + 1];
+    const float ab = a + (b - a) * fv;
+    const float cd = cc + (d - cc) * fv;
+    return ab + (cd - ab) * fu;
+  }
+  // environmentTemp, clouds.cl:80-89.
+  inline float envTemp(f4 p) const { return -lapse * (p.y + W[1]) + groundTemp(p.x, p.z); }
+  // externalHeatSource, clouds.cl:72-75.
+  inline float heatSource(float alt) const { return clampf(std::exp(-(alt + W[1]) / heatDecay), 0.0f, 1.0f); }
+};
+
+// saturationVaporDensity, clouds.cl:94-99 (double literals -> double arithmetic).
+inline float qsat(float T) { return (float)(217 * std::exp(19.5 - 4303.4 / ((double)T - 29.5)) / (double)T); }
+
+// cld_applyMixedBoundaryConditions, clouds.cl:279-299.
+inline f4 mixed_bc(const Grid& g, f4 np) {
+  const f4 cp = clamp4(np, mk(-g.W[0], -g.W[1], -g.W[2], 0.0f), mk(g.W[0], g.W[1], g.W[2], 0.0f));
+  f4 r = np;
+  if (std::fabs(np.x) > g.W[0]) r.x = np.x - 2 * cp.x;
+  if (std::fabs(np.y) > g.W[1]) r.y = cp.y;
+  if (std::fabs(np.z) > g.W[2]) r.z = np.z - 2 * cp.z;
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+void or_clouds_init(const rtp_grid_constants* c, const rtp_cloud_params* cp, const rtp_cloud_env* env,
+                    const float* ground, uint32_t n, or_state* s) {
+  const CloudEnv E(c, env, ground);
+  for (uint32_t i = 0; i < n; ++i) {
+    const f4 p = ld4(s->pos, i);
+    s->temp[i] = E.envTemp(p);                                  // cld_initTemperature
+    s->vapor[i] = cp->initVaporDensityCoeff * qsat(s->temp[i]);  // cld_initVaporDensity
+    s->cloud[i] = 0.0f;                                          // Clouds.cpp:487-488
+    if (s->buoyancy) s->buoyancy[i] = 0.0f;
+  }
+}
+
+int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                   const rtp_cloud_env* env, const float* ground, uint32_t iters, uint32_t n,
+                   or_state* s) {
+  if (!c || !fp || !cp || !env || !s || !s->pos || !s->vel || !s->predPos || !s->totCorrPos ||
+      !s->temp || !s->vapor || !s->cloud || !s->buoyancy)
+    return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const CloudEnv E(c, env, ground);
+  float* pos = s->pos;
+  float* vel = s->vel;
+  float* pred = s->predPos;
+  float* tot = s->totCorrPos;
+  float* temp = s->temp;
+  float* vapor = s->vapor;
+  float* cloud = s->cloud;
+  float* buoy = s->buoyancy;
+  const float dt = cp->timeStep;
+  const float fdt = fp->timeStep;
+
+  // Thermodynamics, Clouds.cpp:516-529.
+  std::vector<float> tempIn(temp, temp + n), cloudGen(n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 p = ld4(pos, i);
+    // cld_heatFromGround, clouds.cl:159-168.
+    temp[i] = std::fmin(tempIn[i] + E.heatSource(p.y) * cp->groundHeatCoeff * dt, 313.0f);
+    // cld_computeBuoyancy, clouds.cl:173-184.
+    const float envT = E.envTemp(p);
+    buoy[i] = cp->buoyancyCoeff * (temp[i] - envT) / envT - cp->gravCoeff * ABS_GRAVITY_ACC_Y * cloud[i];
+    // cld_applyAdiabaticCooling, clouds.cl:189-198.
+    tempIn[i] = std::fmax(temp[i] - cp->adiabaticLapseRate * ld4(vel, i).y * dt, 223.0f);
+    // cld_generateCloud, clouds.cl:207-221.
+    cloudGen[i] = cp->phaseTransitionRate * (vapor[i] - qsat(tempIn[i]));
+    // cld_applyPhaseTransition, clouds.cl:226-238 (inputs are copies, Clouds.cpp:525-526).
+    const float cIn = cloud[i], vIn = vapor[i];
+    cloud[i] = std::fmax(cIn + cloudGen[i] * dt, 0.0f);
+    vapor[i] = std::fmax(vIn - cloudGen[i] * dt, 0.0f);
+    // cld_applyLatentHeat, clouds.cl:243-252.
+    temp[i] = tempIn[i] + std::fmax(cp->latentHeatCoeff * cloudGen[i] * dt, 0.0f);
+  }
+  // cld_predictPosition, clouds.cl:257-273, then the mixed BC (Clouds.cpp:534-538).
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 predVel = ld4(vel, i) + mk(0.0f, buoy[i], 0.0f, 0.0f) * dt;
+    st4(tot, i, predVel * dt);
+    st4(pred, i, mixed_bc(g, ld4(pos, i) + predVel * dt));
+  }
+  // fillCellIDs + sort {pos, col, vel, predPos, totCorrPos}, {temp, buoyancy, vapor,
+  // cloud, partID} (Clouds.cpp:541-543), table (:545-550).
+  std::vector<uint32_t> keys(n), perm;
+  or_fill_cell_ids(c, pred, n, keys.data());
+  std::vector<uint32_t> table(2 * (size_t)c->numCells);
+  sort_and_table(c, n, keys, perm, s->cellId, table.data());
+  gather4(pos, perm, n);
+  gather4(vel, perm, n);
+  gather4(pred, perm, n);
+  gather4(tot, perm, n);
+  gather1(temp, perm, n);
+  gather1(buoy, perm, n);
+  gather1(vapor, perm, n);
+  gather1(cloud, perm, n);
+  gather1(s->id, perm, n);
+  if (s->table) std::memcpy(s->table, table.data(), sizeof(uint32_t) * table.size());
+  const uint32_t* T = table.data();
+
+  if (cp->isTempSmoothingEnabled) {  // Clouds.cpp:554-567, on p_pos
+    std::vector<float> lap(n), lamT(n);
+    // cld_computeLaplacianTemp, clouds.cl:508-569.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pos, i);
+      const float Ti = temp[i];
+      float l = 0.0f;
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        const f4 vec = x - ld4(pos, e) - sh;
+        l += (Ti - temp[e]) * dot(vec, k.grad(vec)) / (dot(vec, vec) + FLOAT_EPS);
+      });
+      lap[i] = l / cp->restDensity;
+    }
+    // cld_computeConstraintFactorTemp, clouds.cl:575-648.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pos, i);
+      float sumG = 0.0f, sumSq = 0.0f;
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        const f4 vec = x - ld4(pos, e) - sh;
+        const f4 gr = k.grad(vec);
+        const float d = dot(vec, gr) / (dot(vec, vec) * cp->restDensity + FLOAT_EPS);
+        sumG += d;
+        sumSq += d * d;
+      });
+      sumSq += sumG * sumG;
+      lamT[i] = -lap[i] / (sumSq + cp->relaxCFM);
+    }
+    // cld_computeConstraintCorrectionTemp, clouds.cl:654-722, cld_correctTemperature :931-937.
+    std::vector<float> corrT(n);
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pos, i);
+      const float li = lamT[i];
+      float cr = 0.0f;
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        const f4 vec = x - ld4(pos, e) - sh;
+        const f4 gr = k.grad(vec);
+        const float d = dot(vec, gr) / (dot(vec, vec) * cp->restDensity + FLOAT_EPS);
+        cr += (li + lamT[e]) * d;
+      });
+      corrT[i] = cr;
+    }
+    for (uint32_t i = 0; i < n; ++i) temp[i] += 0.3f * corrT[i];
+  }
+
+  std::vector<float> density(n), lambda(n), corr(4 * (size_t)n);
+  for (uint32_t it = 0; it < iters; ++it) {  // Clouds.cpp:570-587
+    // cld_computeDensity, clouds.cl:305-360.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i);
+      float rho = 0.0f;
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) { rho += k.poly6(x - ld4(pred, e) - sh); });
+      density[i] = rho;
+    }
+    // cld_computeConstraintFactor, clouds.cl:365-436.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i);
+      const float densityC = density[i] / fp->restDensity - 1.0f;
+      f4 sg = splat(0.0f);
+      float sq = 0.0f;
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        const f4 gr = k.grad(x - ld4(pred, e) - sh);
+        sg = sg + gr;
+        sq += dot(gr, gr);
+      });
+      sq += dot(sg, sg);
+      sq /= fp->restDensity * fp->restDensity;
+      lambda[i] = -densityC / (sq + fp->relaxCFM);
+    }
+    // cld_computeConstraintCorrection, clouds.cl:441-502.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i);
+      const float li = lambda[i];
+      f4 a = splat(0.0f);
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        const f4 vec = x - ld4(pred, e) - sh;
+        a = a + (li + lambda[e] + k.artPressure(vec, fp)) * k.grad(vec);
+      });
+      st4(corr.data(), i, a / fp->restDensity);
+    }
+    // cld_correctPosition on predPos and totCorrPos, then the BC (Clouds.cpp:579-586).
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 cr = ld4(corr.data(), i);
+      st4(pred, i, ld4(pred, i) + cr);
+      st4(tot, i, ld4(tot, i) + cr);
+      st4(pred, i, mixed_bc(g, ld4(pred, i)));
+    }
+  }
+  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
+  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+
+  // cld_updateVel, clouds.cl:958-966.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i)
+    st4(vel, i, clamp4s(ld4(tot, i) / (fdt + FLOAT_EPS), -c->maxVel, c->maxVel));
+
+  if (fp->isVorticityConfEnabled) {  // Clouds.cpp:592-602
+    std::vector<float> vort(4 * (size_t)n), velIn(4 * (size_t)n);
+    // cld_computeVorticity, clouds.cl:727-785.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), v = ld4(vel, i);
+      f4 w = splat(0.0f);
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        w = w + cross(ld4(vel, e) - v, k.grad(x - ld4(pred, e) - sh));
+      });
+      st4(vort.data(), i, w);
+    }
+    // cld_applyVorticityConfinement, clouds.cl:790-850.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), w = ld4(vort.data(), i);
+      f4 eta = splat(0.0f);
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        eta = eta + flen(ld4(vort.data(), e)) * k.grad(x - ld4(pred, e) - sh);
+      });
+      st4(vel, i, ld4(vel, i) + fp->vorticityConfCoeff * cross(fnormalize(eta), w) * fdt);
+    }
+    std::memcpy(velIn.data(), vel, sizeof(float) * 4 * n);
+    // cld_applyXsphViscosityCorrection, clouds.cl:856-915.
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 x = ld4(pred, i), v = ld4(velIn.data(), i);
+      f4 visc = splat(0.0f);
+      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+        visc = visc + (ld4(velIn.data(), e) - v) * k.poly6(x - ld4(pred, e) - sh);
+      });
+      st4(vel, i, v + fp->xsphViscosityCoeff * visc);
+    }
+    if (s->vort) std::memcpy(s->vort, vort.data(), sizeof(float) * 4 * n);
+  }
+  // cld_updatePosition, clouds.cl:942-953.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    f4 p = ld4(pred, i);
+    const float alt = p.y + g.W[1];
+    p.x += (1 - std::exp(-alt * E.windX)) * cp->windCoeff * cp->timeStep * (float)(cp->dim - 2);
+    p.z += (1 - std::exp(-alt * E.windZ)) * 0.7f * cp->windCoeff * cp->timeStep;
+    st4(pos, i, p);
+  }
+  return RTP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+/*
+ * oracle.h - CPU restatement of the RealTimeParticles simulation step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA library is compared with: only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs load it.
+ * The product (realtimeparticles_gb300) never links, loads or calls anything here.
+ *
+ * Every function restates one reference kernel (or host sequence) in the same operation
+ * order, citing the file:line it follows (paths relative to the reference project).
+ * It is compiled with -ffp-contract=off so the float arithmetic is the same on x86-64
+ * and aarch64.  Parity is pinned by comparing it bit-for-bit with the reference's own
+ * kernel sources compiled for the CPU (oracle/ref/, outputs in oracle/_ref/), and by the
+ * golden fixtures under tests/golden/ that were produced from those reference kernels.
+ */
+#ifndef RTP_ORACLE_H
+#define RTP_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/rtp.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Number of OpenMP threads used by the oracle (0 = all). */
+void or_set_threads(int n);
+int or_get_threads(void);
+
+/* JIT constants, Fluids.cpp:104-119 / Boids.cpp:103-113 / Clouds.cpp:134-147. */
+int or_derive_constants(int model, const rtp_model_params* p, rtp_grid_constants* c);
+
+/* grid.cl:76-86 (fillCellIDs) over n float4 positions. */
+void or_fill_cell_ids(const rtp_grid_constants* c, const float* pos4, uint32_t n, uint32_t* keys);
+/* The contract of RadixSort::sort (RadixSort.cpp:122-189): stable ascending sort. */
+void or_stable_sort(const uint32_t* keys, uint32_t n, uint32_t* keys_out, uint32_t* perm);
+/* grid.cl:91-152: resetStartEndCell, fillStartCell, fillEndCell, adjustEndCell. */
+void or_cell_table(const rtp_grid_constants* c, const uint32_t* sorted_keys, uint32_t n, uint32_t* table2);
+
+/* State arrays of one model, all of length n (float4 arrays hold 4*n floats).
+ * Unused members may be NULL. */
+typedef struct or_state {
+  float* pos;
+  float* vel;
+  float* predPos;
+  float* totCorrPos;
+  float* acc;
+  float* vort;
+  float* density;
+  float* lambda;
+  float* temp;
+  float* vapor;
+  float* cloud;
+  float* buoyancy;
+  uint32_t* id;
+  uint32_t* cellId;   /* sorted keys of the step */
+  uint32_t* table;    /* 2 * numCells */
+} or_state;
+
+/* One Fluids::update (Fluids.cpp:400-457 without the render-only lines 459-468). */
+int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters,
+                   uint32_t n, or_state* s);
+/* One Boids::update (Boids.cpp:323-377, target rule off, dt a parameter). */
+int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt,
+                  int boundary, uint32_t n, or_state* s);
+/* One Clouds::update (Clouds.cpp:503-610). `ground` may be NULL (constant groundTemp0). */
+int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp,
+                   const rtp_cloud_params* cp, const rtp_cloud_env* env, const float* ground,
+                   uint32_t iters, uint32_t n, or_state* s);
+/* cld_initTemperature + cld_initVaporDensity (clouds.cl:116-135), cloud = 0. */
+void or_clouds_init(const rtp_grid_constants* c, const rtp_cloud_params* cp,
+                    const rtp_cloud_env* env, const float* ground, uint32_t n, or_state* s);
+
+/* Single kernels on a sorted state with a built table, for per-kernel parity. */
+void or_fld_density(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* predPos,
+                    const uint32_t* table, uint32_t n, float* density);
+void or_fld_lambda(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* predPos,
+                   const float* density, const uint32_t* table, uint32_t n, float* lambda);
+void or_fld_correction(const rtp_grid_constants* c, const rtp_fluid_params* p,
+                       const float* predPos, const float* lambda, const uint32_t* table,
+                       uint32_t n, float* corr);
+/* Mean |rho/rho0 - 1|, max, kinetic energy and neighbour statistics of a fluid state
+ * (uses the sorted state and its table, like the sweeps). */
+void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* predPos,
+                      const float* vel, const uint32_t* table, uint32_t n, rtp_metrics* m);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,136 @@
+// boids.cu - 3D boids step (GB300, sm_103a).
+//
+// Replaces kernels/boids.cl driven by Boids::update (physics/ocl/Boids.cpp:323-377):
+//   k_boids_keys          fillCellIDs(pos) + sort-tile histogram
+//   sort passes           RadixSort::sort of {pos, vel} (+ ids); acc is recomputed each step
+//   cell table            start/end (cap 3000, Boids.cpp:78)
+//   k_boids_rules_update  bd_applyBoidsRulesWithGrid3D + bd_updateVel + the boundary
+//                         condition (bd_updatePosAndApplyPeriodicBC / ...WallBC), reading
+//                         the sorted copies and writing the canonical pos/vel buffers.
+#include "boids.cuh"
+
+namespace rtp {
+
+__global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, const float4* __restrict__ pos, uint32_t n,
+                                                             uint32_t* __restrict__ keys, int bits0,
+                                                             uint32_t* __restrict__ hist0) {
+  __shared__ uint32_t s_hist[kMaxBins];
+  TileHistogram th;
+  th.init(s_hist, bits0);
+  const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll 2
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) {
+      const uint32_t key = cell_key(g, ld4(pos + i));
+      keys[i] = key;
+      th.add(key);
+    }
+  }
+  th.store(hist0);
+}
+
+__device__ __forceinline__ float4 fnorm(float4 a) {
+  const float d = dot4(a, a);
+  if (d == 0.0f) return a;
+  return a * rsqrtf(d);
+}
+
+template <bool PERIODIC>
+__global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, const float4* __restrict__ posS,
+                                                            const float4* __restrict__ velS,
+                                                            const uint2* __restrict__ table, uint32_t n,
+                                                            const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
+                                                            float4* __restrict__ vel, float4* __restrict__ acc,
+                                                            uint32_t* __restrict__ ids) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = ld4(posS + i);
+  int cx, cy, cz;
+  cell3(g, xi, cx, cy, cz);
+  int count = 0;
+  float4 sp = f4(0.f, 0.f, 0.f, 0.f), sv = sp, sr = sp;
+  // bd_applyBoidsRulesWithGrid3D (boids.cl:78-113): 27 cells, no wrap.
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int nx = cx + dx;
+    if (nx < 0 || nx >= g.R[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int ny = cy + dy;
+      if (ny < 0 || ny >= g.R[1]) continue;
+      const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int nz = cz + dz;
+        if (nz < 0 || nz >= g.R[2]) continue;
+        uint32_t j0, j1;
+        cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
+        for (uint32_t j = j0; j < j1; ++j) {
+          const float4 xj = ld4(posS + j);
+          const float4 v = xi - xj;
+          const float sq = dot4(v, v);
+          if (sq < g.boidsR2 && sq > kFloatEps) {
+            sp = sp + xj;
+            sv = sv + fnorm(ld4(velS + j));
+            sr = sr + v * (1.0f / sq);
+            ++count;
+          }
+        }
+      }
+    }
+  }
+  float4 a = f4(0.f, 0.f, 0.f, 0.f);
+  if (count != 0) {
+    float4 coh = sp * (1.0f / (float)count) - xi;
+    coh = fnorm(coh) * p.velocityScale;
+    const float4 ali = fnorm(sv) * p.velocityScale;
+    const float4 sep = fnorm(sr) * p.velocityScale;
+    a = ali * p.alignmentScale + sep * p.separationScale + coh * p.cohesionScale;
+  }
+  acc[i] = a;
+  // bd_updateVel (boids.cl:246-259).
+  const float4 nv = ld4(velS + i) + a * p.dt;
+  const float norm = fminf(fmaxf(sqrtf(dot4(nv, nv)), 0.2f * p.maxVelocity), p.maxVelocity);
+  float4 v = fnorm(nv) * norm;
+  const float4 np = xi + v * p.dt;
+  const float4 lo = f4(-g.W[0], -g.W[1], -g.W[2], 0.0f), hi = f4(g.W[0], g.W[1], g.W[2], 0.0f);
+  float4 cp = clamp4(np, lo, hi);
+  if (PERIODIC) {
+    // bd_updatePosAndApplyPeriodicBC (boids.cl:289-315).
+    if (!(cp.x == np.x)) cp.x *= -1.0f;
+    if (!(cp.y == np.y)) cp.y *= -1.0f;
+    if (!(cp.z == np.z)) cp.z *= -1.0f;
+  } else {
+    // bd_updatePosAndApplyWallBC (boids.cl:264-284).
+    if (!(cp.x == np.x && cp.y == np.y && cp.z == np.z)) v = v * -0.5f;
+  }
+  pos[i] = cp;
+  vel[i] = v;
+  if (ids) ids[i] = __ldg(idsS + i);
+}
+
+static int check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
+}
+
+int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
+                  Launcher& L) {
+  L.begin("bd_keys");
+  k_boids_keys<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, pos, n, keys, plan.bits[0], hist0);
+  L.end("bd_keys");
+  return check("k_boids_keys");
+}
+
+int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, const float4* posS, const float4* velS,
+                       const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, float4* acc,
+                       uint32_t* ids, Launcher& L) {
+  const uint32_t b = (n + 127) / 128;
+  L.begin("bd_rules_update");
+  if (periodic)
+    k_boids_rules_update<true><<<b, 128, 0, L.stream>>>(g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+  else
+    k_boids_rules_update<false><<<b, 128, 0, L.stream>>>(g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+  L.end("bd_rules_update");
+  return check("k_boids_rules_update");
+}
+
+}  // namespace rtp

@@ -1,0 +1,438 @@
+// clouds.cu - clouds step: PBF with mixed boundaries + thermodynamics (GB300, sm_103a).
+//
+// Replaces kernels/clouds.cl driven by Clouds::update (physics/ocl/Clouds.cpp:503-610):
+//   k_cloud_thermo_predict  cld_heatFromGround, cld_computeBuoyancy, cld_applyAdiabaticCooling,
+//                           cld_generateCloud, cld_applyPhaseTransition, cld_applyLatentHeat
+//                           (the reference's 6 kernels + 3 buffer copies), cld_predictPosition,
+//                           cld_applyMixedBoundaryConditions, fillCellIDs, sort histogram
+//   sort passes             {pos, vel, predPos, totCorrPos} + {temp, buoyancy, vapor, cloud, id}
+//   k_cloud_temp_lambda     cld_computeLaplacianTemp + cld_computeConstraintFactorTemp (one sweep)
+//   k_cloud_temp_correct    cld_computeConstraintCorrectionTemp + cld_correctTemperature
+//   I x k_cloud_lambda      cld_computeDensity + cld_computeConstraintFactor
+//   I x k_cloud_deltap      cld_computeConstraintCorrection + cld_correctPosition (predPos and
+//                           totCorrPos) + the mixed boundary; the last adds cld_updateVel
+//   vorticity, confinement, XSPH + cld_updatePosition (wind drift), state written back.
+// Neighbour sweeps follow clouds.cl:326-356: x and z periodic with image shifts of
+// 2W * sign, y walls.
+#include "clouds.cuh"
+
+namespace rtp {
+
+template <class F>
+__device__ __forceinline__ void for_each_cloud_neighbour(const GridK& g, const uint2* __restrict__ table, float4 xi,
+                                                         F&& f) {
+  int cx, cy, cz;
+  cell3(g, xi, cx, cy, cz);
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int ux = cx + dx;
+    const int nx = (ux + g.R[0]) % g.R[0];
+    const float shx = ux >= g.R[0] ? 2.0f * g.W[0] : (ux < 0 ? -2.0f * g.W[0] : 0.0f);
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int ny = cy + dy;
+      if (ny >= g.R[1] || ny < 0) continue;
+      const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int uz = cz + dz;
+        const int nz = (uz + g.R[2]) % g.R[2];
+        const float shz = uz >= g.R[2] ? 2.0f * g.W[2] : (uz < 0 ? -2.0f * g.W[2] : 0.0f);
+        uint32_t j0, j1;
+        cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
+        for (uint32_t j = j0; j < j1; ++j) f(j, shx, shz);
+      }
+    }
+  }
+}
+
+// Ground temperature: bilinear in the groundNx x groundNz table over the box floor.
+__device__ __forceinline__ float ground_temp(const CloudK& c, const GridK& g, float x, float z) {
+  if (!c.ground) return c.T0;
+  const float u = fminf(fmaxf((x + g.W[0]) / (2.0f * g.W[0]), 0.0f), 1.0f) * (float)(c.nx - 1);
+  const float v = fminf(fmaxf((z + g.W[2]) / (2.0f * g.W[2]), 0.0f), 1.0f) * (float)(c.nz - 1);
+  const uint32_t i0 = min((uint32_t)floorf(u), c.nx - 2), k0 = min((uint32_t)floorf(v), c.nz - 2);
+  const float fu = u - (float)i0, fv = v - (float)k0;
+  const float a = __ldg(c.ground + i0 * c.nz + k0), b = __ldg(c.ground + i0 * c.nz + k0 + 1);
+  const float cc = __ldg(c.ground + (i0 + 1) * c.nz + k0), d = __ldg(c.ground + (i0 + 1) * c.nz + k0 + 1);
+  const float ab = a + (b - a) * fv, cd = cc + (d - cc) * fv;
+  return ab + (cd - ab) * fu;
+}
+// environmentTemp (clouds.cl:80-89).
+__device__ __forceinline__ float env_temp(const CloudK& c, const GridK& g, float4 p) {
+  return -c.lapse * (p.y + g.W[1]) + ground_temp(c, g, p.x, p.z);
+}
+// saturationVaporDensity (clouds.cl:94-99): double literals, evaluated in double.
+__device__ __forceinline__ float qsat(float T) { return (float)(217.0 * exp(19.5 - 4303.4 / ((double)T - 29.5)) / (double)T); }
+
+// cld_applyMixedBoundaryConditions (clouds.cl:279-299).
+__device__ __forceinline__ float4 mixed_bc(const GridK& g, float4 np) {
+  float4 r = np;
+  if (fabsf(np.x) > g.W[0]) r.x = np.x - 2.0f * fminf(fmaxf(np.x, -g.W[0]), g.W[0]);
+  if (fabsf(np.y) > g.W[1]) r.y = fminf(fmaxf(np.y, -g.W[1]), g.W[1]);
+  if (fabsf(np.z) > g.W[2]) r.z = np.z - 2.0f * fminf(fmaxf(np.z, -g.W[2]), g.W[2]);
+  return r;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_cloud_thermo_predict(
+    GridK g, CloudK c, const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
+    float* __restrict__ temp, float* __restrict__ vapor, float* __restrict__ cloud, float* __restrict__ buoy,
+    float4* __restrict__ pred, float4* __restrict__ tot, uint32_t* __restrict__ keys, int bits0,
+    uint32_t* __restrict__ hist0) {
+  __shared__ uint32_t s_hist[kMaxBins];
+  TileHistogram th;
+  th.init(s_hist, bits0);
+  const float dt = c.dt;
+  const uint32_t base = blockIdx.x * kSortTile;
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+    if (i >= n) continue;
+    const float4 p = ld4(pos + i), v = ld4(vel + i);
+    const float tIn = temp[i];
+    // cld_heatFromGround (clouds.cl:159-168).
+    const float heat = fminf(fmaxf(expf(-(p.y + g.W[1]) / c.heatDecay), 0.0f), 1.0f);
+    const float t1 = fminf(tIn + heat * c.groundHeat * dt, 313.0f);
+    // cld_computeBuoyancy (clouds.cl:173-184).
+    const float envT = env_temp(c, g, p);
+    const float b = c.buoyancy * (t1 - envT) / envT - c.gravCoeff * kAbsGravityY * cloud[i];
+    // cld_applyAdiabaticCooling (clouds.cl:189-198).
+    const float t2 = fmaxf(t1 - c.adiabatic * v.y * dt, 223.0f);
+    // cld_generateCloud (clouds.cl:207-221), cld_applyPhaseTransition (:226-238).
+    const float gen = c.phaseRate * (vapor[i] - qsat(t2));
+    cloud[i] = fmaxf(cloud[i] + gen * dt, 0.0f);
+    vapor[i] = fmaxf(vapor[i] - gen * dt, 0.0f);
+    // cld_applyLatentHeat (clouds.cl:243-252).
+    temp[i] = t2 + fmaxf(c.latent * gen * dt, 0.0f);
+    buoy[i] = b;
+    // cld_predictPosition (clouds.cl:257-273) + mixed boundary (Clouds.cpp:537-538).
+    const float4 pv = f4(v.x, v.y + b * dt, v.z, v.w);
+    tot[i] = pv * dt;
+    const float4 pp = mixed_bc(g, p + pv * dt);
+    pred[i] = pp;
+    const uint32_t key = cell_key(g, pp);
+    keys[i] = key;
+    th.add(key);
+  }
+  th.store(hist0);
+}
+
+// cld_computeLaplacianTemp + cld_computeConstraintFactorTemp, on p_pos (Clouds.cpp:253-255).
+__global__ void __launch_bounds__(128) k_cloud_temp_lambda(GridK g, CloudK c, const float4* __restrict__ pos,
+                                                           const float* __restrict__ temp,
+                                                           const uint2* __restrict__ table, uint32_t n,
+                                                           float* __restrict__ lamT) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pos + i);
+  const float ti = __ldg(temp + i);
+  float lap = 0.0f, sg = 0.0f, ssq = 0.0f;
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pos + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      const float vg = r2 * s;  // dot(vec, gradSpiky(vec))
+      lap += (ti - __ldg(temp + j)) * vg / (r2 + kFloatEps);
+      const float d = vg / (r2 * c.cloudRho0 + kFloatEps);
+      sg += d;
+      ssq += d * d;
+    }
+  });
+  lap /= c.cloudRho0;
+  ssq += sg * sg;
+  lamT[i] = -lap / (ssq + c.cloudRelax);
+}
+
+// cld_computeConstraintCorrectionTemp + cld_correctTemperature (in place: the sweep reads
+// only lamT and positions of the neighbours).
+__global__ void __launch_bounds__(128) k_cloud_temp_correct(GridK g, CloudK c, const float4* __restrict__ pos,
+                                                            const float* __restrict__ lamT,
+                                                            const uint2* __restrict__ table, uint32_t n,
+                                                            float* __restrict__ temp) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pos + i);
+  const float li = __ldg(lamT + i);
+  float corr = 0.0f;
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pos + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      const float d = r2 * s / (r2 * c.cloudRho0 + kFloatEps);
+      corr += (li + __ldg(lamT + j)) * d;
+    }
+  });
+  temp[i] += 0.3f * corr;
+}
+
+// cld_computeDensity + cld_computeConstraintFactor.
+__global__ void __launch_bounds__(128) k_cloud_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                      const uint2* __restrict__ table, uint32_t n,
+                                                      float* __restrict__ lambda, float* __restrict__ density) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i);
+  float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      rho += k.w(r2);
+      float r;
+      const float s = k.gs(r2, r);
+      const float a = vx * s, b = vy * s, cc = vz * s;
+      sgx += a;
+      sgy += b;
+      sgz += cc;
+      ssq += a * a + b * b + cc * cc;
+    }
+  });
+  const float C = rho / p.rho0 - 1.0f;
+  ssq += sgx * sgx + sgy * sgy + sgz * sgz;
+  ssq *= p.invRho0Sq;
+  lambda[i] = -C / (ssq + p.relaxCFM);
+  density[i] = rho;
+}
+
+// cld_computeConstraintCorrection, cld_correctPosition x2 and the mixed boundary
+// (Clouds.cpp:577-586); LAST adds cld_updateVel (clouds.cl:958-966).
+template <bool LAST>
+__global__ void __launch_bounds__(128) k_cloud_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                      const float* __restrict__ lambda, const uint2* __restrict__ table,
+                                                      uint32_t n, float4* __restrict__ predOut, float4* __restrict__ tot,
+                                                      float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i);
+  const float li = __ldg(lambda + i);
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      float sc = 0.0f;
+      if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
+      const float f = (li + __ldg(lambda + j) + sc) * s;
+      ax += vx * f;
+      ay += vy * f;
+      az += vz * f;
+    }
+  });
+  const float4 dp = f4(ax * p.invRho0, ay * p.invRho0, az * p.invRho0, 0.0f);
+  predOut[i] = mixed_bc(g, xi + dp);
+  const float4 t = tot[i] + dp;
+  tot[i] = t;
+  if (LAST) {
+    const float d = p.dt + kFloatEps;
+    velS[i] = clamp4s(f4(__fdiv_rn(t.x, d), __fdiv_rn(t.y, d), __fdiv_rn(t.z, d), __fdiv_rn(t.w, d)), -g.maxVel,
+                      g.maxVel);
+  }
+}
+
+__global__ void k_cloud_update_vel(GridK g, FluidK p, const float4* __restrict__ tot, uint32_t n,
+                                   float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 t = ld4(tot + i);
+  const float d = p.dt + kFloatEps;
+  velS[i] = clamp4s(f4(__fdiv_rn(t.x, d), __fdiv_rn(t.y, d), __fdiv_rn(t.z, d), __fdiv_rn(t.w, d)), -g.maxVel, g.maxVel);
+}
+
+// cld_computeVorticity (clouds.cl:727-785).
+__global__ void __launch_bounds__(128) k_cloud_vorticity(GridK g, const float4* __restrict__ pred,
+                                                         const float4* __restrict__ velS, const uint2* __restrict__ table,
+                                                         uint32_t n, float4* __restrict__ vort) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  float4 w = f4(0.f, 0.f, 0.f, 0.f);
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      w = w + cross4(ld4(velS + j) - vi, f4(vx * s, vy * s, vz * s, 0.0f));
+    }
+  });
+  vort[i] = w;
+}
+
+// cld_applyVorticityConfinement (clouds.cl:790-850).
+__global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                       const float4* __restrict__ vort, const uint2* __restrict__ table,
+                                                       uint32_t n, float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), wi = ld4(vort + i);
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      const float4 wj = ld4(vort + j);
+      const float f = sqrtf(dot4(wj, wj)) * s;
+      ex += vx * f;
+      ey += vy * f;
+      ez += vz * f;
+    }
+  });
+  const float4 c = cross4(normalize0(f4(ex, ey, ez, 0.0f)), wi);
+  const float s = p.vortCoeff * p.dt;
+  float4 v = velS[i];
+  v.x += c.x * s;
+  v.y += c.y * s;
+  v.z += c.z * s;
+  velS[i] = v;
+}
+
+// cld_applyXsphViscosityCorrection (clouds.cl:856-915) + cld_updatePosition (:942-953);
+// writes the canonical state (pos, vel, temp, vapor, cloud, buoyancy, ids).
+__global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
+                                                     const float4* __restrict__ velS, const uint2* __restrict__ table,
+                                                     uint32_t n, CloudState s) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  float4 out = vi;
+  if (p.vorticity) {
+    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+    for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(pred + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        const float wv = k.w(r2);
+        const float4 vj = ld4(velS + j);
+        ax += (vj.x - vi.x) * wv;
+        ay += (vj.y - vi.y) * wv;
+        az += (vj.z - vi.z) * wv;
+        aw += (vj.w - vi.w) * wv;
+      }
+    });
+    out = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
+  }
+  s.vel[i] = out;
+  float4 x = xi;
+  const float alt = xi.y + g.W[1];
+  x.x += (1.0f - expf(-alt * c.windX)) * c.wind * c.dt * (float)(c.dim - 2u);
+  x.z += (1.0f - expf(-alt * c.windZ)) * 0.7f * c.wind * c.dt;
+  s.pos[i] = x;
+  s.temp[i] = __ldg(s.tempS + i);
+  s.vapor[i] = __ldg(s.vaporS + i);
+  s.cloud[i] = __ldg(s.cloudS + i);
+  s.buoy[i] = __ldg(s.buoyS + i);
+  if (s.ids) s.ids[i] = __ldg(s.idsS + i);
+}
+
+// cld_initTemperature + cld_initVaporDensity (clouds.cl:116-135); cloud = 0.
+__global__ void k_cloud_init(GridK g, CloudK c, const float4* __restrict__ pos, uint32_t n, float* __restrict__ temp,
+                             float* __restrict__ vapor, float* __restrict__ cloud, float* __restrict__ buoy) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float t = env_temp(c, g, ld4(pos + i));
+  temp[i] = t;
+  vapor[i] = c.initVapor * qsat(t);
+  cloud[i] = 0.0f;
+  buoy[i] = 0.0f;
+}
+
+static int check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
+}
+static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+
+int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const float4* vel, uint32_t n, float* temp,
+                  float* vapor, float* cloud, float* buoy, float4* pred, float4* tot, uint32_t* keys,
+                  const SortPlan& plan, uint32_t* hist0, Launcher& L) {
+  L.begin("cld_thermo_predict");
+  k_cloud_thermo_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, c, pos, vel, n, temp, vapor, cloud, buoy, pred,
+                                                                    tot, keys, plan.bits[0], hist0);
+  L.end("cld_thermo_predict");
+  return check("k_cloud_thermo_predict");
+}
+
+int cloud_temperature(const GridK& g, const CloudK& c, const float4* posS, float* tempS, float* lamT, const uint2* table,
+                      uint32_t n, Launcher& L) {
+  L.begin("cld_temp_lambda");
+  k_cloud_temp_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, c, posS, tempS, table, n, lamT);
+  L.end("cld_temp_lambda");
+  int rc = check("k_cloud_temp_lambda");
+  if (rc) return rc;
+  L.begin("cld_temp_correct");
+  k_cloud_temp_correct<<<blocks(n, 128), 128, 0, L.stream>>>(g, c, posS, lamT, table, n, tempS);
+  L.end("cld_temp_correct");
+  return check("k_cloud_temp_correct");
+}
+
+int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, float4* totS,
+                    const uint2* table, uint32_t n, float* lambda, float* density, bool last, float4* velS, Launcher& L) {
+  L.begin("cld_lambda");
+  k_cloud_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, table, n, lambda, density);
+  L.end("cld_lambda");
+  int rc = check("k_cloud_lambda");
+  if (rc) return rc;
+  L.begin(last ? "cld_deltap_vel" : "cld_deltap");
+  if (last)
+    k_cloud_deltap<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS);
+  else
+    k_cloud_deltap<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS);
+  L.end(last ? "cld_deltap_vel" : "cld_deltap");
+  return check("k_cloud_deltap");
+}
+
+int cloud_update_vel(const GridK& g, const FluidK& p, const float4* totS, uint32_t n, float4* velS, Launcher& L) {
+  L.begin("cld_updateVel");
+  k_cloud_update_vel<<<blocks(n, 256), 256, 0, L.stream>>>(g, p, totS, n, velS);
+  L.end("cld_updateVel");
+  return check("k_cloud_update_vel");
+}
+
+int cloud_post(const GridK& g, const FluidK& p, const CloudK& c, const float4* pred, float4* velS, float4* vort,
+               const uint2* table, uint32_t n, const CloudState& s, Launcher& L) {
+  if (p.vorticity) {
+    L.begin("cld_vorticity");
+    k_cloud_vorticity<<<blocks(n, 128), 128, 0, L.stream>>>(g, pred, velS, table, n, vort);
+    L.end("cld_vorticity");
+    int rc = check("k_cloud_vorticity");
+    if (rc) return rc;
+    L.begin("cld_confine");
+    k_cloud_confine<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS);
+    L.end("cld_confine");
+    rc = check("k_cloud_confine");
+    if (rc) return rc;
+  }
+  L.begin("cld_xsph_final");
+  k_cloud_final<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, c, pred, velS, table, n, s);
+  L.end("cld_xsph_final");
+  return check("k_cloud_final");
+}
+
+int cloud_init(const GridK& g, const CloudK& c, const float4* pos, uint32_t n, float* temp, float* vapor, float* cloud,
+               float* buoy, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  L.begin("cld_init");
+  k_cloud_init<<<blocks(n, 256), 256, 0, L.stream>>>(g, c, pos, n, temp, vapor, cloud, buoy);
+  L.end("cld_init");
+  return check("k_cloud_init");
+}
+
+}  // namespace rtp

@@ -1,0 +1,377 @@
+// fluids.cu - position-based fluids step (GB300, sm_103a).
+//
+// Replaces kernels/fluids.cl driven by Fluids::update (physics/ocl/Fluids.cpp:400-457).
+// Per substep (I Jacobi iterations, vorticity on):
+//   k_fluid_predict       fld_predictPosition + fillCellIDs + sort-tile histogram
+//   sort passes           RadixSort::sort of {pos, vel, predPos} (+ particle ids)
+//   cell table            resetStartEndCell / fillStartCell / fillEndCell (+ cap on read)
+//   I x k_fluid_lambda    fld_applyBoundaryCondition (clamp on load) + fld_computeDensity
+//                         + fld_computeConstraintFactor in one neighbour sweep
+//   I x k_fluid_deltap    fld_computeConstraintCorrection + fld_correctPosition into a
+//                         second buffer (Jacobi); the last one also does fld_updateVel
+//   k_fluid_vorticity     fld_computeVorticity
+//   k_fluid_confine       fld_applyVorticityConfinement (in place: reads only vort of others)
+//   k_fluid_xsph_final    fld_applyXsphViscosityCorrection + fld_updatePosition, writing
+//                         the state back to the canonical pos/vel buffers
+// Neighbour sweeps visit the reference's 27 cells, wrapped modulo the grid resolution
+// (fluids.cl:101-123), in the same order.
+#include "fluids.cuh"
+
+namespace rtp {
+
+template <class F>
+__device__ __forceinline__ void for_each_fluid_neighbour(const GridK& g, const uint2* __restrict__ table, float4 xi,
+                                                         F&& f) {
+  int cx, cy, cz;
+  cell3(g, xi, cx, cy, cz);
+  int xs[3], ys[3], zs[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xs[d] = (cx + d - 1 + g.R[0]) % g.R[0];
+    ys[d] = (cy + d - 1 + g.R[1]) % g.R[1];
+    zs[d] = (cz + d - 1 + g.R[2]) % g.R[2];
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      const uint32_t row = ((uint32_t)xs[a] * g.R[1] + (uint32_t)ys[b]) * g.R[2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        uint32_t j0, j1;
+        cell_range(table, row + (uint32_t)zs[c], g.cap, j0, j1);
+        for (uint32_t j = j0; j < j1; ++j) f(j);
+      }
+    }
+}
+
+__device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
+
+// fld_predictPosition (fluids.cl:62-74) + fillCellIDs (grid.cl:76-86) + digit-0 histogram.
+// Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
+__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK p, const float4* __restrict__ pos,
+                                                                const float4* __restrict__ vel, uint32_t n,
+                                                                float4* __restrict__ pred, uint32_t* __restrict__ keys,
+                                                                int bits0, uint32_t* __restrict__ hist0) {
+  __shared__ uint32_t s_hist[kMaxBins];
+  TileHistogram th;
+  th.init(s_hist, bits0);
+  const float dt = p.dt;
+  const float gx = __fmul_rn(0.0f, dt), gy = __fmul_rn(-kAbsGravityY, dt);
+  const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll 2
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) {
+      const float4 x = ld4(pos + i), v = ld4(vel + i);
+      const float4 nv = f4(__fadd_rn(v.x, gx), __fadd_rn(v.y, gy), __fadd_rn(v.z, gx), __fadd_rn(v.w, gx));
+      const float4 pp = f4(__fadd_rn(x.x, __fmul_rn(nv.x, dt)), __fadd_rn(x.y, __fmul_rn(nv.y, dt)),
+                           __fadd_rn(x.z, __fmul_rn(nv.z, dt)), __fadd_rn(x.w, __fmul_rn(nv.w, dt)));
+      pred[i] = pp;
+      const uint32_t key = cell_key(g, pp);
+      keys[i] = key;
+      th.add(key);
+    }
+  }
+  th.store(hist0);
+}
+
+// fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor.
+__global__ void __launch_bounds__(128) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                      const uint2* __restrict__ table, uint32_t n,
+                                                      float* __restrict__ lambda, float* __restrict__ density) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = bc_clamp(p, ld4(pred + i));
+  float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
+  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+    const float4 xj = bc_clamp(p, ld4(pred + j));
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      rho += k.w(r2);
+      float r;
+      const float s = k.gs(r2, r);
+      const float gxx = vx * s, gyy = vy * s, gzz = vz * s;
+      sgx += gxx;
+      sgy += gyy;
+      sgz += gzz;
+      ssq += gxx * gxx + gyy * gyy + gzz * gzz;
+    }
+  });
+  const float C = rho / p.rho0 - 1.0f;
+  ssq += sgx * sgx + sgy * sgy + sgz * sgz;
+  ssq *= p.invRho0Sq;
+  lambda[i] = -C / (ssq + p.relaxCFM);
+  density[i] = rho;
+}
+
+// fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
+// LAST adds fld_updateVel (fluids.cl:263-273).
+template <bool LAST>
+__global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                      const float* __restrict__ lambda, const uint2* __restrict__ table,
+                                                      uint32_t n, float4* __restrict__ predOut,
+                                                      const float4* __restrict__ posS, float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = bc_clamp(p, ld4(pred + i));
+  const float li = __ldg(lambda + i);
+  float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+    const float4 xj = bc_clamp(p, ld4(pred + j));
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      float sc = 0.0f;
+      if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
+      const float f = (li + __ldg(lambda + j) + sc) * s;
+      cx += vx * f;
+      cy += vy * f;
+      cz += vz * f;
+    }
+  });
+  const float4 out = f4(xi.x + cx * p.invRho0, xi.y + cy * p.invRho0, xi.z + cz * p.invRho0, xi.w);
+  predOut[i] = out;
+  if (LAST) {
+    const float4 x0 = ld4(posS + i);
+    const float d = p.dt + kFloatEps;
+    velS[i] = clamp4s(f4(__fdiv_rn(out.x - x0.x, d), __fdiv_rn(out.y - x0.y, d), __fdiv_rn(out.z - x0.z, d),
+                         __fdiv_rn(out.w - x0.w, d)),
+                      -g.maxVel, g.maxVel);
+  }
+}
+
+// fld_updateVel alone (only used when the solver runs zero iterations).
+__global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ posS,
+                                   uint32_t n, float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = ld4(pred + i), b = ld4(posS + i);
+  const float d = p.dt + kFloatEps;
+  velS[i] = clamp4s(f4(__fdiv_rn(a.x - b.x, d), __fdiv_rn(a.y - b.y, d), __fdiv_rn(a.z - b.z, d), __fdiv_rn(a.w - b.w, d)),
+                    -g.maxVel, g.maxVel);
+}
+
+// fld_computeVorticity (fluids.cl:278-324).
+__global__ void __launch_bounds__(128) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
+                                                         const float4* __restrict__ velS, const uint2* __restrict__ table,
+                                                         uint32_t n, float4* __restrict__ vort) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
+  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      const float4 dv = ld4(velS + j) - vi;
+      const float4 gr = f4(vx * s, vy * s, vz * s, 0.0f);
+      w = w + cross4(dv, gr);
+    }
+  });
+  vort[i] = w;
+}
+
+// fld_applyVorticityConfinement (fluids.cl:329-377).
+__global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                       const float4* __restrict__ vort, const uint2* __restrict__ table,
+                                                       uint32_t n, float4* __restrict__ velS) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), wi = ld4(vort + i);
+  float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      float r;
+      const float s = k.gs(r2, r);
+      const float4 wj = ld4(vort + j);
+      const float f = sqrtf(dot4(wj, wj)) * s;
+      ex += vx * f;
+      ey += vy * f;
+      ez += vz * f;
+    }
+  });
+  const float4 nrm = normalize0(f4(ex, ey, ez, 0.0f));
+  const float4 c = cross4(nrm, wi);
+  const float s = p.vortCoeff * p.dt;
+  float4 v = velS[i];
+  v.x += c.x * s;
+  v.y += c.y * s;
+  v.z += c.z * s;
+  velS[i] = v;
+}
+
+// fld_applyXsphViscosityCorrection (fluids.cl:383-430) + fld_updatePosition (:444-450),
+// writing the canonical state buffers.
+__global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                          const float4* __restrict__ velS,
+                                                          const uint2* __restrict__ table, uint32_t n,
+                                                          const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
+                                                          float4* __restrict__ vel, uint32_t* __restrict__ ids) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Sph k(g);
+  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  float ax = 0.0f, ay = 0.0f, az = 0.0f, aw = 0.0f;
+  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+    const float4 xj = ld4(pred + j);
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      const float wv = k.w(r2);
+      const float4 vj = ld4(velS + j);
+      ax += (vj.x - vi.x) * wv;
+      ay += (vj.y - vi.y) * wv;
+      az += (vj.z - vi.z) * wv;
+      aw += (vj.w - vi.w) * wv;
+    }
+  });
+  vel[i] = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
+  pos[i] = xi;
+  if (ids) ids[i] = __ldg(idsS + i);
+}
+
+// fld_updatePosition alone (vorticity confinement disabled: Fluids.cpp:444 skips XSPH too).
+__global__ void k_fluid_final(const float4* __restrict__ pred, const float4* __restrict__ velS, uint32_t n,
+                              const uint32_t* __restrict__ idsS, float4* __restrict__ pos, float4* __restrict__ vel,
+                              uint32_t* __restrict__ ids) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  pos[i] = ld4(pred + i);
+  vel[i] = ld4(velS + i);
+  if (ids) ids[i] = __ldg(idsS + i);
+}
+
+// Step metrics: density (as fld_computeDensity) at the current positions with the step's
+// table, neighbour counts, kinetic energy.
+__global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const float4* __restrict__ pos,
+                                                       const float4* __restrict__ vel, const uint2* __restrict__ table,
+                                                       uint32_t n, double* __restrict__ acc, uint32_t* __restrict__ hist) {
+  // acc: [0] sum |rho/rho0 - 1|, [1] kinetic energy, [2] neighbour count; hist[64] = max error bits.
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  double err = 0.0, ke = 0.0, nb = 0.0;
+  float mx = 0.0f;
+  if (i < n) {
+    const Sph k(g);
+    const float4 xi = ld4(pos + i);
+    float rho = 0.0f;
+    uint32_t cnt = 0;
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+      const float4 xj = ld4(pos + j);
+      const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        rho += k.w(r2);
+        if (j != i) ++cnt;
+      }
+    });
+    const float e = fabsf(rho / p.rho0 - 1.0f);
+    err = e;
+    mx = e;
+    const float4 v = ld4(vel + i);
+    ke = 0.5 * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+    nb = cnt;
+    atomicAdd(hist + min(cnt, 63u), 1u);
+  }
+  // Warp reduction, one atomic per warp.
+  for (int o = 16; o > 0; o >>= 1) {
+    err += __shfl_down_sync(0xffffffffu, err, o);
+    ke += __shfl_down_sync(0xffffffffu, ke, o);
+    nb += __shfl_down_sync(0xffffffffu, nb, o);
+    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(acc + 0, err);
+    atomicAdd(acc + 1, ke);
+    atomicAdd(acc + 2, nb);
+    atomicMax(hist + 64, __float_as_uint(mx));  // mx >= 0: uint order == float order
+  }
+}
+
+static int check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
+}
+
+static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+
+int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
+                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, Launcher& L) {
+  L.begin("fld_predict");
+  k_fluid_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0);
+  L.end("fld_predict");
+  return check("k_fluid_predict");
+}
+
+int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table, uint32_t n,
+                    float* lambda, float* density, bool last, const float4* posS, float4* velS, Launcher& L) {
+  L.begin("fld_lambda");
+  k_fluid_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, table, n, lambda, density);
+  L.end("fld_lambda");
+  int rc = check("k_fluid_lambda");
+  if (rc) return rc;
+  if (last) {
+    L.begin("fld_deltap_vel");
+    k_fluid_deltap<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS);
+    L.end("fld_deltap_vel");
+  } else {
+    L.begin("fld_deltap");
+    k_fluid_deltap<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS);
+    L.end("fld_deltap");
+  }
+  return check("k_fluid_deltap");
+}
+
+int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const float4* posS, uint32_t n, float4* velS,
+                     Launcher& L) {
+  L.begin("fld_updateVel");
+  k_fluid_update_vel<<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
+  L.end("fld_updateVel");
+  return check("k_fluid_update_vel");
+}
+
+int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
+               uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, Launcher& L) {
+  if (p.vorticity) {
+    L.begin("fld_vorticity");
+    k_fluid_vorticity<<<blocks(n, 128), 128, 0, L.stream>>>(g, pred, velS, table, n, vort);
+    L.end("fld_vorticity");
+    int rc = check("k_fluid_vorticity");
+    if (rc) return rc;
+    L.begin("fld_confine");
+    k_fluid_confine<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS);
+    L.end("fld_confine");
+    rc = check("k_fluid_confine");
+    if (rc) return rc;
+    L.begin("fld_xsph_final");
+    k_fluid_xsph_final<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS, pos, vel, ids);
+    L.end("fld_xsph_final");
+    return check("k_fluid_xsph_final");
+  }
+  L.begin("fld_final");
+  k_fluid_final<<<blocks(n, 256), 256, 0, L.stream>>>(pred, velS, n, idsS, pos, vel, ids);
+  L.end("fld_final");
+  return check("k_fluid_final");
+}
+
+int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, const uint2* table, uint32_t n,
+                  double* acc, uint32_t* hist, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  L.begin("fld_metrics");
+  k_fluid_metrics<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
+  L.end("fld_metrics");
+  return check("k_fluid_metrics");
+}
+
+}  // namespace rtp

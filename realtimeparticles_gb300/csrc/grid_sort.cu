@@ -1,0 +1,380 @@
+// grid_sort.cu - uniform grid and stable radix sort (GB300, sm_103a).
+//
+// Replaces grid.cl (cell ids, start/end table) and RadixSort (physics/utils/RadixSort.cpp,
+// kernels/radixSort.cl).  The reference sorts all maxNb keys in 4 passes of 8 bits with
+// 512 work-items that each scan N/512 keys serially; here each pass is a tile-parallel
+// reduce-then-scan LSD pass:
+//   * digit histogram per 2048-key tile (pass 0: fused into the kernel that computes the
+//     keys; pass p > 0: accumulated by pass p-1's scatter with warp-aggregated atomics),
+//   * per-digit exclusive scan over tiles (k_sort_scan),
+//   * stable rank inside the tile with __match_any_sync (warp w owns a contiguous chunk,
+//     items processed in index order) and scatter; the last pass gathers the payloads
+//     (pos, vel, ...) directly, so no permutation array round trip is needed.
+// Only ceil(keyBits / 9) passes run: cell keys need 17 bits on a 40^3 grid.
+#include <algorithm>
+#include <cstring>
+
+#include "rtp_internal.hpp"
+
+namespace rtp {
+
+SortPlan make_sort_plan(uint32_t n, uint32_t keyBits) {
+  SortPlan p;
+  p.n = n;
+  p.keyBits = std::max<uint32_t>(1u, std::min<uint32_t>(keyBits, 32u));
+  p.passes = (int)((p.keyBits + kMaxRadixBits - 1) / kMaxRadixBits);
+  const int per = (int)((p.keyBits + p.passes - 1) / p.passes);
+  int shift = 0;
+  for (int i = 0; i < p.passes; ++i) {
+    p.shift[i] = shift;
+    p.bits[i] = std::min(per, (int)p.keyBits - shift);
+    shift += p.bits[i];
+  }
+  p.tiles = (n + kSortTile - 1) / kSortTile;
+  if (p.tiles == 0) p.tiles = 1;
+  return p;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t sort_scratch_bytes(const SortPlan& p) {
+  const size_t nk = align256(sizeof(uint32_t) * (size_t)std::max<uint32_t>(p.n, 1));
+  const size_t h = align256(sizeof(uint32_t) * (size_t)p.passes * p.tiles * kMaxBins);
+  const size_t t = align256(sizeof(uint32_t) * (size_t)p.passes * kMaxBins);
+  return 4 * nk + h + t;
+}
+
+void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s) {
+  char* b = (char*)base;
+  const size_t nk = align256(sizeof(uint32_t) * (size_t)std::max<uint32_t>(p.n, 1));
+  s.keysA = (uint32_t*)b;
+  b += nk;
+  s.keysB = (uint32_t*)b;
+  b += nk;
+  s.idxA = (uint32_t*)b;
+  b += nk;
+  s.idxB = (uint32_t*)b;
+  b += nk;
+  s.hist = (uint32_t*)b;
+  b += align256(sizeof(uint32_t) * (size_t)p.passes * p.tiles * kMaxBins);
+  s.totals = (uint32_t*)b;
+}
+
+// fillCellIDs (grid.cl:76-86).
+__global__ void k_fill_cell_ids(GridK g, const float4* __restrict__ pos, uint32_t n, uint32_t* __restrict__ keys) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keys[i] = cell_key(g, ld4(pos + i));
+}
+
+// Digit-0 histogram per tile of externally supplied keys.
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist0(const uint32_t* __restrict__ keys, uint32_t n, int bits,
+                                                             uint32_t* __restrict__ hist0) {
+  __shared__ uint32_t s_hist[kMaxBins];
+  TileHistogram th;
+  th.init(s_hist, bits);
+  const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t e = base + k * kSortThreads + threadIdx.x;
+    if (e < n) th.add(__ldg(keys + e));
+  }
+  th.store(hist0);
+}
+
+// In-place exclusive scan over tiles of each digit's column; totals[d] = column sum.
+// Block = 8 warps, lane = digit within a group of 32, warp = contiguous range of tiles.
+__global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, uint32_t tiles, int bins,
+                                                   uint32_t* __restrict__ totals) {
+  __shared__ uint32_t s_part[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + lane;
+  const uint32_t chunk = (tiles + 7) / 8;
+  const uint32_t t0 = min(tiles, warp * chunk), t1 = min(tiles, t0 + chunk);
+  uint32_t sum = 0;
+  if (d < bins)
+    for (uint32_t t = t0; t < t1; ++t) sum += hist[(size_t)t * kMaxBins + d];
+  s_part[warp][lane] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      const uint32_t v = s_part[w][lane];
+      s_part[w][lane] = run;
+      run += v;
+    }
+    if (d < bins) totals[d] = run;
+  }
+  __syncthreads();
+  if (d < bins) {
+    uint32_t run = s_part[warp][lane];
+    for (uint32_t t = t0; t < t1; ++t) {
+      const size_t at = (size_t)t * kMaxBins + d;
+      const uint32_t v = hist[at];
+      hist[at] = run;
+      run += v;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// One LSD pass over a tile of kSortTile keys.  hist holds, for this pass, the exclusive
+// prefix over tiles per digit (k_sort_scan); totals the per-digit totals.
+template <bool LAST>
+__global__ void __launch_bounds__(kSortThreads) k_sort_pass(
+    const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ idx_in, uint32_t n, int shift, int bits,
+    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, uint32_t* __restrict__ keys_out,
+    uint32_t* __restrict__ idx_out, uint32_t* __restrict__ hist_next, int next_shift, int next_bits, GatherList g) {
+  __shared__ uint32_t s_base[kMaxBins];
+  __shared__ uint32_t s_wc[kSortWarps][kMaxBins];
+  __shared__ uint32_t s_wsum[kSortWarps];
+  const int bins = 1 << bits;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t tile = blockIdx.x;
+
+  // Exclusive scan of the digit totals (2 digits per thread) + this tile's prefix.
+  {
+    const int d0 = 2 * tid, d1 = 2 * tid + 1;
+    const uint32_t v0 = d0 < bins ? __ldg(totals + d0) : 0u;
+    const uint32_t v1 = d1 < bins ? __ldg(totals + d1) : 0u;
+    uint32_t x = v0 + v1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) wpre += (w < warp) ? s_wsum[w] : 0u;
+    const uint32_t excl = wpre + x - (v0 + v1);
+    const uint32_t* tp = hist + (size_t)tile * kMaxBins;
+    if (d0 < bins) s_base[d0] = excl + __ldg(tp + d0);
+    if (d1 < bins) s_base[d1] = excl + v0 + __ldg(tp + d1);
+  }
+  for (int i = tid; i < kSortWarps * bins; i += kSortThreads) s_wc[i / bins][i % bins] = 0;
+  __syncthreads();
+
+  // Stable rank within the warp's contiguous chunk, items in index order.
+  const uint32_t wbase = tile * kSortTile + warp * (32 * kSortItems);
+  const uint32_t ltmask = lanemask_lt();
+  uint32_t key[kSortItems], dig[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t e = wbase + k * 32 + lane;
+    const bool valid = e < n;
+    key[k] = valid ? __ldg(keys_in + e) : 0u;
+    dig[k] = valid ? ((key[k] >> shift) & (uint32_t)(bins - 1)) : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xffffffffu, dig[k]);
+    uint32_t old = 0;
+    if (valid) old = s_wc[warp][dig[k]];
+    __syncwarp();
+    if (valid && (peers & ltmask) == 0) s_wc[warp][dig[k]] = old + __popc(peers);
+    __syncwarp();
+    rank[k] = old + __popc(peers & ltmask);
+  }
+  __syncthreads();
+  for (int d = tid; d < bins; d += kSortThreads) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t t = s_wc[w][d];
+      s_wc[w][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+
+  const uint32_t nmask = (1u << next_bits) - 1u;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t e = wbase + k * 32 + lane;
+    const bool valid = e < n;
+    uint32_t pos = 0;
+    if (valid) {
+      const uint32_t d = dig[k];
+      pos = s_base[d] + s_wc[warp][d] + rank[k];
+      keys_out[pos] = key[k];
+      const uint32_t src = idx_in ? __ldg(idx_in + e) : e;
+      if (!LAST) {
+        idx_out[pos] = src;
+      } else {
+        for (int b = 0; b < g.n4; ++b) g.dst4[b][pos] = __ldg(g.src4[b] + src);
+        for (int b = 0; b < g.n1; ++b) g.dst1[b][pos] = __ldg(g.src1[b] + src);
+        if (g.perm) g.perm[pos] = src;
+      }
+    }
+    if (!LAST) {
+      // Next pass's tile histogram, aggregated over lanes hitting the same (tile, digit).
+      const uint32_t slot = valid ? (pos / kSortTile) * kMaxBins + ((key[k] >> next_shift) & nmask) : 0xFFFFFFFFu;
+      const uint32_t peers = __match_any_sync(0xffffffffu, slot);
+      if (valid && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
+    }
+  }
+}
+
+// Cell table fill (grid.cl:91-138) in the [begin, endExcl) encoding; the table was zeroed.
+__global__ void k_cell_table_fill(const uint32_t* __restrict__ sk, uint32_t n, uint32_t nc, uint2* __restrict__ table) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = __ldg(sk + i);
+  if (k >= nc) return;
+  uint32_t* t = reinterpret_cast<uint32_t*>(table + k);
+  if (i == 0) t[0] = 1u;  // fillStartCell skips ID 0: the reset value start = 1 stays
+  else if (__ldg(sk + i - 1) != k) t[0] = i;
+  const uint32_t right = (i + 1 < n) ? __ldg(sk + i + 1) : 0xFFFFFFFFu;
+  if (right != k) t[1] = i + 1;
+}
+
+// Internal encoding -> reference format (start, end inclusive, capped; empty = (1, 0)).
+// In place is allowed: each thread reads and writes only its own cell.
+__global__ void k_cell_table_ref(const uint2* table, uint32_t nc, uint32_t cap, uint2* out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const uint2 se = table[c];
+  const uint32_t cnt = se.y > se.x ? min(se.y - se.x, cap + 1u) : 0u;
+  out[c] = cnt ? make_uint2(se.x, se.x + cnt - 1u) : make_uint2(1u, 0u);
+}
+
+static int check_launch(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return RTP_OK;
+}
+
+int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  L.begin("fillCellIDs");
+  k_fill_cell_ids<<<(n + 255) / 256, 256, 0, L.stream>>>(g, pos, n, keys);
+  L.end("fillCellIDs");
+  return check_launch("k_fill_cell_ids");
+}
+
+int launch_sort_histogram(const SortPlan& p, const uint32_t* keys, const SortScratch& s, Launcher& L) {
+  L.begin("sort_hist0");
+  k_sort_hist0<<<p.tiles, kSortThreads, 0, L.stream>>>(keys, p.n, p.bits[0], s.hist);
+  L.end("sort_hist0");
+  return check_launch("k_sort_hist0");
+}
+
+int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L) {
+  if (p.passes <= 1) return RTP_OK;
+  const size_t per = (size_t)p.tiles * kMaxBins;
+  RTP_CUDA(cudaMemsetAsync(s.hist + per, 0, sizeof(uint32_t) * per * (p.passes - 1), L.stream));
+  return RTP_OK;
+}
+
+int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* keys_out, const SortScratch& s,
+                       const GatherList& g, Launcher& L) {
+  if (p.n == 0) return RTP_OK;
+  const size_t per = (size_t)p.tiles * kMaxBins;
+  const uint32_t* kin = keys_in;
+  const uint32_t* iin = nullptr;
+  for (int pass = 0; pass < p.passes; ++pass) {
+    const bool last = pass == p.passes - 1;
+    uint32_t* hist = s.hist + per * pass;
+    uint32_t* totals = s.totals + (size_t)kMaxBins * pass;
+    const int bins = 1 << p.bits[pass];
+    L.begin("sort_scan");
+    k_sort_scan<<<(bins + 31) / 32, 256, 0, L.stream>>>(hist, p.tiles, bins, totals);
+    L.end("sort_scan");
+    int rc = check_launch("k_sort_scan");
+    if (rc) return rc;
+    uint32_t* kout = last ? keys_out : ((pass % 2 == 0) ? s.keysB : s.keysA);
+    uint32_t* iout = last ? nullptr : ((pass % 2 == 0) ? s.idxB : s.idxA);
+    if (!last && kout == kin) kout = (kout == s.keysA) ? s.keysB : s.keysA;
+    if (last) {
+      L.begin("sort_pass_gather");
+      k_sort_pass<true><<<p.tiles, kSortThreads, 0, L.stream>>>(kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+                                                                totals, kout, nullptr, nullptr, 0, 1, g);
+      L.end("sort_pass_gather");
+    } else {
+      L.begin("sort_pass");
+      k_sort_pass<false><<<p.tiles, kSortThreads, 0, L.stream>>>(kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+                                                                 totals, kout, iout, hist + per, p.shift[pass + 1],
+                                                                 p.bits[pass + 1], g);
+      L.end("sort_pass");
+    }
+    rc = check_launch("k_sort_pass");
+    if (rc) return rc;
+    kin = kout;
+    iin = iout;
+  }
+  return RTP_OK;
+}
+
+int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L) {
+  RTP_CUDA(cudaMemsetAsync(table, 0, sizeof(uint2) * g.nc, L.stream));
+  if (n == 0) return RTP_OK;
+  L.begin("cellTable");
+  k_cell_table_fill<<<(n + 255) / 256, 256, 0, L.stream>>>(sorted_keys, n, g.nc, table);
+  L.end("cellTable");
+  return check_launch("k_cell_table_fill");
+}
+
+int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L) {
+  L.begin("cellTableRef");
+  k_cell_table_ref<<<(g.nc + 255) / 256, 256, 0, L.stream>>>(table, g.nc, g.cap, out);
+  L.end("cellTableRef");
+  return check_launch("k_cell_table_ref");
+}
+
+}  // namespace rtp
+
+using namespace rtp;
+
+extern "C" {
+
+int rtp_fill_cell_ids(const rtp_grid_constants* c, const float* d_pos4, uint32_t n, uint32_t* d_keys, void* stream) {
+  if (!c || (n && (!d_pos4 || !d_keys))) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_fill_cell_ids: null argument");
+  Launcher L;
+  L.stream = (cudaStream_t)stream;
+  return launch_fill_cell_ids(make_gridk(*c), reinterpret_cast<const float4*>(d_pos4), n, d_keys, L);
+}
+
+int rtp_radix_sort_scratch_bytes(uint32_t n, uint32_t keyBits, size_t* bytes) {
+  if (!bytes || keyBits > 32) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort_scratch_bytes: bad argument");
+  *bytes = sort_scratch_bytes(make_sort_plan(n, keyBits));
+  return RTP_OK;
+}
+
+int rtp_radix_sort(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint32_t* d_keys_out, uint32_t* d_perm_out,
+                   void* d_scratch, size_t scratch_bytes, void* stream) {
+  if (keyBits > 32) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort: keyBits > 32");
+  if (n == 0) return RTP_OK;
+  if (!d_keys_in || !d_keys_out || !d_scratch) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort: null pointer");
+  const SortPlan p = make_sort_plan(n, keyBits);
+  if (scratch_bytes < sort_scratch_bytes(p)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort: scratch too small");
+  if ((reinterpret_cast<uintptr_t>(d_scratch) & 255u) != 0)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort: scratch must be 256-byte aligned");
+  SortScratch s;
+  sort_scratch_carve(p, d_scratch, s);
+  Launcher L;
+  L.stream = (cudaStream_t)stream;
+  int rc = launch_sort_clear(p, s, L);
+  if (rc) return rc;
+  rc = launch_sort_histogram(p, d_keys_in, s, L);
+  if (rc) return rc;
+  GatherList g;
+  g.perm = d_perm_out;
+  return launch_sort_passes(p, d_keys_in, d_keys_out, s, g, L);
+}
+
+int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_keys, uint32_t n, uint32_t* d_table2,
+                         void* stream) {
+  if (!c || !d_table2 || (n && !d_sorted_keys)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_build_cell_table: null argument");
+  const GridK g = make_gridk(*c);
+  Launcher L;
+  L.stream = (cudaStream_t)stream;
+  uint2* t = reinterpret_cast<uint2*>(d_table2);
+  const int rc = launch_cell_table(g, d_sorted_keys, n, t, L);
+  return rc ? rc : launch_cell_table_to_reference(g, t, t, L);
+}
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+// rtp_internal.hpp - host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/rtp.h"
+#include "rtp_common.cuh"
+
+namespace rtp {
+
+// Thread-local error message (rtp_last_error).
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define RTP_CUDA(call)                                    \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return ::rtp::cuda_fail(_e, #call); \
+  } while (0)
+
+// Kernel launch bookkeeping: names each launch so the profiler can attribute time.
+struct Launcher {
+  cudaStream_t stream = nullptr;
+  bool profiling = false;
+  void* owner = nullptr;  // Handle* when profiling
+  int begin(const char* name);
+  int end(const char* name);
+};
+
+// ---- Radix sort ---------------------------------------------------------------------
+struct SortPlan {
+  uint32_t n = 0;
+  uint32_t keyBits = 0;
+  int passes = 0;
+  int bits[4] = {0, 0, 0, 0};
+  int shift[4] = {0, 0, 0, 0};
+  uint32_t tiles = 0;
+};
+SortPlan make_sort_plan(uint32_t n, uint32_t keyBits);
+// Scratch layout for a plan: keys ping-pong, index ping-pong, histograms, totals.
+struct SortScratch {
+  uint32_t* keysA = nullptr;
+  uint32_t* keysB = nullptr;
+  uint32_t* idxA = nullptr;
+  uint32_t* idxB = nullptr;
+  uint32_t* hist = nullptr;    // passes x tiles x kMaxBins
+  uint32_t* totals = nullptr;  // passes x kMaxBins
+};
+size_t sort_scratch_bytes(const SortPlan& p);
+void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s);
+
+// Values carried by the last sort pass: dst[pos] = src[perm[pos]].
+struct GatherList {
+  static constexpr int kMax4 = 6;
+  static constexpr int kMax1 = 6;
+  const float4* src4[kMax4];
+  float4* dst4[kMax4];
+  const uint32_t* src1[kMax1];
+  uint32_t* dst1[kMax1];
+  int n4 = 0;
+  int n1 = 0;
+  uint32_t* perm = nullptr;  // optional: write the permutation
+};
+
+// Histogram of digit 0 of `keys` per tile (used when keys come from outside a model step).
+int launch_sort_histogram(const SortPlan& p, const uint32_t* keys, const SortScratch& s, Launcher& L);
+// Passes 0..passes-1: keys (already histogrammed for pass 0) -> sorted keys in keys_out,
+// values gathered by `g` in the last pass.  keys_in may alias s.keysA.
+int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* keys_out, const SortScratch& s,
+                       const GatherList& g, Launcher& L);
+// Zero the histogram area (the first pass reads it after the producer kernel filled it).
+int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L);
+
+// Cell table in the internal [begin, endExcl) encoding from sorted keys.
+int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L);
+// Internal encoding -> the reference's inclusive (start, end) with (1, 0) for empty cells.
+int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L);
+int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L);
+
+}  // namespace rtp

@@ -1,0 +1,1103 @@
+// runtime.cu - model handles, step pipelines, CUDA-graph executor and the C ABI.
+//
+// Replaces the OpenCL runtime role of CL::Context (physics/ocl/Context.cpp: buffer
+// registry, runKernel, profiling) and the host update() sequences of the three models.
+// One handle = one model on one CUDA stream.  A step is recorded once into a CUDA graph
+// and replayed; the graph is re-recorded whenever a parameter, the particle count or the
+// boundary changes.  When profiling is on, every kernel of the graph is bracketed by
+// captured event-record nodes, so per-kernel device times come from the replays
+// themselves (Context::runKernel's event profiling, Context.cpp:692-705).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "boids.cuh"
+#include "clouds.cuh"
+#include "fluids.cuh"
+#include "rtp_internal.hpp"
+
+namespace rtp {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return RTP_ERR_NO_DEVICE;
+  if (e == cudaErrorMemoryAllocation) return RTP_ERR_OUT_OF_MEMORY;
+  return RTP_ERR_CUDA;
+}
+
+constexpr float PI_F = 3.1415927f;  // utils/Math.hpp:69
+
+// Utils::FloatToStr (utils/Utils.cpp:24-28) + the OpenCL compiler's parse of the literal.
+static float round_trip(float v) {
+  char buf[128];
+  std::snprintf(buf, sizeof buf, "%.10f", (double)v);
+  return std::strtof(buf, nullptr);
+}
+
+static int derive_constants(int model, const rtp_model_params* p, rtp_grid_constants* c) {
+  if (!p || !c) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  std::memset(c, 0, sizeof *c);
+  for (int a = 0; a < 3; ++a) {
+    if (p->gridRes[a] == 0 || !(p->boxSize[a] > 0.0f)) return fail(RTP_ERR_INVALID_ARGUMENT, "empty box or grid");
+    c->gridRes[a] = p->gridRes[a];
+    c->absWall[a] = round_trip(p->boxSize[a] / 2.0f);  // Fluids.cpp:108-110
+  }
+  const float bx = p->boxSize[0];
+  const float rx = (float)p->gridRes[0];
+  c->cellSize = round_trip(bx / rx);  // Fluids.cpp:114
+  const uint64_t nc = (uint64_t)p->gridRes[0] * p->gridRes[1] * p->gridRes[2];
+  if (nc > (1ull << 30)) return fail(RTP_ERR_INVALID_ARGUMENT, "grid too large");
+  c->numCells = (uint32_t)nc;
+  const float effectRadius = bx / rx;  // Fluids.cpp:104
+  c->effectRadius = round_trip(effectRadius);
+  c->effectRadiusSquared = round_trip(1.0f * bx * bx / (float)(p->gridRes[0] * p->gridRes[0]));  // Boids.cpp:104
+  c->poly6Coeff = round_trip(315.0f / (64.0f * PI_F * std::pow(effectRadius, 9.f)));             // Fluids.cpp:117
+  c->spikyCoeff = round_trip(15.0f / (PI_F * std::pow(effectRadius, 6.f)));                      // Fluids.cpp:118
+  c->maxVel = round_trip(30.0f);                                                                 // Fluids.cpp:119
+  uint32_t cap = p->maxNbPartsInCell;
+  if (cap == 0) cap = (model == RTP_MODEL_BOIDS) ? 3000u : 100u;  // Boids.cpp:78, Fluids.cpp:79
+  c->maxPartsInCell = cap;
+  // Largest key: every axis at +W (index == GRID_RES aliases, grid.cl:33-35).
+  uint32_t top[3];
+  for (int a = 0; a < 3; ++a) {
+    const float q = std::fmin(std::fmax(c->absWall[a], -c->absWall[a]), c->absWall[a]) + c->absWall[a];
+    top[a] = (uint32_t)std::floor(q / c->cellSize);
+  }
+  const uint64_t kb = (uint64_t)top[0] * c->gridRes[2] * c->gridRes[1] + (uint64_t)top[1] * c->gridRes[2] + top[2] + 1;
+  if (kb > 0xFFFFFFFFull) return fail(RTP_ERR_INVALID_ARGUMENT, "key range exceeds 32 bits");
+  c->keyBound = (uint32_t)kb;
+  uint32_t bits = 0;
+  while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)c->keyBound) ++bits;
+  c->keyBits = bits;
+  return RTP_OK;
+}
+
+FluidK make_fluidk(const rtp_grid_constants& c, const rtp_fluid_params& p) {
+  FluidK k;
+  k.rho0 = p.restDensity;
+  k.invRho0 = 1.0f / p.restDensity;
+  k.invRho0Sq = 1.0f / (p.restDensity * p.restDensity);
+  k.relaxCFM = p.relaxCFM;
+  k.dt = p.timeStep;
+  k.lo = make_float4(-c.absWall[0] + 0.01f, -c.absWall[1] + 0.01f, -c.absWall[2] + 0.01f, 0.0f);
+  k.hi = make_float4(c.absWall[0] - 0.1f, c.absWall[1] - 0.1f, c.absWall[2] - 0.1f, 0.0f);
+  k.artPressure = p.isArtPressureEnabled ? 1 : 0;
+  k.apCoeff = p.artPressureCoeff;
+  // poly6L(artPressureRadius * h, h), sph.cl:16-19.
+  const float h = c.effectRadius;
+  const float L = p.artPressureRadius * h;
+  const float q = h * h - L * L;
+  const float wq = (L < h ? 1.0f : 0.0f) * c.poly6Coeff * (q * q * q);
+  k.apInvWq = wq != 0.0f ? 1.0f / wq : 0.0f;
+  k.apExp = p.artPressureExp;
+  k.vorticity = p.isVorticityConfEnabled ? 1 : 0;
+  k.vortCoeff = p.vorticityConfCoeff;
+  k.xsph = p.xsphViscosityCoeff;
+  return k;
+}
+
+// ---------------------------------------------------------------------------------------
+struct TimedSlot {
+  std::string name;
+  int ev;  // index of the start event; end = ev + 1
+};
+
+struct KernelStat {
+  uint64_t launches = 0;
+  double ms = 0.0;
+};
+
+struct Handle {
+  int model = 0;
+  rtp_model_params mp{};
+  rtp_grid_constants gc{};
+  GridK g{};
+  rtp_fluid_params fp{};
+  uint32_t iters = 2;
+  rtp_boids_params bp{};
+  float boidsDt = 0.1f;
+  rtp_cloud_params cp{};
+  rtp_cloud_env env{};
+  float* ground = nullptr;
+  int boundary = RTP_BOUNDARY_BOUNCING_WALL;
+  bool paused = false;
+  uint64_t maxN = 0, curN = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // Canonical state (the Model's buffers) and the sorted working copies.
+  float4 *pos = nullptr, *vel = nullptr, *posS = nullptr, *velS = nullptr;
+  float4 *predTmp = nullptr, *predA = nullptr, *predB = nullptr, *predFinal = nullptr;
+  float4 *vort = nullptr, *acc = nullptr, *totCorr = nullptr, *totCorrS = nullptr;
+  float *lambda = nullptr, *density = nullptr;
+  float *temp = nullptr, *vapor = nullptr, *cloud = nullptr, *buoy = nullptr;
+  float *tempS = nullptr, *vaporS = nullptr, *cloudS = nullptr, *buoyS = nullptr;
+  float *lapT = nullptr, *lamT = nullptr;
+  uint32_t *ids = nullptr, *idsS = nullptr, *cellId = nullptr;
+  uint2* table = nullptr;
+  uint2* tableRef = nullptr;
+  void* sortMem = nullptr;
+  SortScratch ss{};
+  double* mAcc = nullptr;
+  uint32_t* mHist = nullptr;
+  std::vector<void*> allocs;
+
+  // Graph executor.
+  cudaGraphExec_t graph = nullptr;
+  bool graphValid = false;
+  bool graphProfiled = false;
+
+  // Profiling.
+  bool profiling = false;
+  std::vector<cudaEvent_t> events;
+  std::vector<TimedSlot> slots;
+  std::map<std::string, KernelStat> stats;
+
+  // Timing.
+  void* flush = nullptr;
+  size_t flushBytes = 0;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+
+  bool hasStep = false;  // a step ran since the last upload (cell table / keys valid)
+};
+
+int Launcher::begin(const char* name) {
+  if (!profiling || !owner) return RTP_OK;
+  Handle* h = (Handle*)owner;
+  const int ev = (int)h->slots.size() * 2;
+  while ((int)h->events.size() < ev + 2) {
+    cudaEvent_t e;
+    RTP_CUDA(cudaEventCreate(&e));
+    h->events.push_back(e);
+  }
+  h->slots.push_back({name, ev});
+  RTP_CUDA(cudaEventRecord(h->events[ev], stream));
+  return RTP_OK;
+}
+
+int Launcher::end(const char* name) {
+  (void)name;
+  if (!profiling || !owner) return RTP_OK;
+  Handle* h = (Handle*)owner;
+  RTP_CUDA(cudaEventRecord(h->events[h->slots.back().ev + 1], stream));
+  return RTP_OK;
+}
+
+template <class T>
+static int dalloc(Handle* h, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  RTP_CUDA(cudaMalloc((void**)p, sizeof(T) * count));
+  RTP_CUDA(cudaMemset(*p, 0, sizeof(T) * count));
+  h->allocs.push_back((void*)*p);
+  return RTP_OK;
+}
+
+#define RTP_TRY(x)           \
+  do {                       \
+    int _rc = (x);           \
+    if (_rc) return _rc;     \
+  } while (0)
+
+static int alloc_buffers(Handle* h) {
+  const size_t M = h->maxN;
+  RTP_TRY(dalloc(h, &h->pos, M));
+  RTP_TRY(dalloc(h, &h->vel, M));
+  RTP_TRY(dalloc(h, &h->posS, M));
+  RTP_TRY(dalloc(h, &h->velS, M));
+  RTP_TRY(dalloc(h, &h->ids, M));
+  RTP_TRY(dalloc(h, &h->idsS, M));
+  RTP_TRY(dalloc(h, &h->cellId, M));
+  RTP_TRY(dalloc(h, &h->table, h->gc.numCells));
+  RTP_TRY(dalloc(h, &h->tableRef, h->gc.numCells));
+  RTP_TRY(dalloc(h, &h->mAcc, 4));
+  RTP_TRY(dalloc(h, &h->mHist, 80));
+  if (h->model == RTP_MODEL_BOIDS) {
+    RTP_TRY(dalloc(h, &h->acc, M));
+  } else {
+    RTP_TRY(dalloc(h, &h->predTmp, M));
+    RTP_TRY(dalloc(h, &h->predA, M));
+    RTP_TRY(dalloc(h, &h->predB, M));
+    RTP_TRY(dalloc(h, &h->vort, M));
+    RTP_TRY(dalloc(h, &h->lambda, M));
+    RTP_TRY(dalloc(h, &h->density, M));
+    h->predFinal = h->predA;
+  }
+  if (h->model == RTP_MODEL_CLOUDS) {
+    RTP_TRY(dalloc(h, &h->totCorr, M));
+    RTP_TRY(dalloc(h, &h->totCorrS, M));
+    RTP_TRY(dalloc(h, &h->temp, M));
+    RTP_TRY(dalloc(h, &h->vapor, M));
+    RTP_TRY(dalloc(h, &h->cloud, M));
+    RTP_TRY(dalloc(h, &h->buoy, M));
+    RTP_TRY(dalloc(h, &h->tempS, M));
+    RTP_TRY(dalloc(h, &h->vaporS, M));
+    RTP_TRY(dalloc(h, &h->cloudS, M));
+    RTP_TRY(dalloc(h, &h->buoyS, M));
+    RTP_TRY(dalloc(h, &h->lapT, M));
+    RTP_TRY(dalloc(h, &h->lamT, M));
+  }
+  const SortPlan full = make_sort_plan((uint32_t)M, h->gc.keyBits);
+  const size_t sb = sort_scratch_bytes(full);
+  RTP_CUDA(cudaMalloc(&h->sortMem, sb));
+  h->allocs.push_back(h->sortMem);
+  sort_scratch_carve(full, h->sortMem, h->ss);
+  // Identity ids.
+  std::vector<uint32_t> id(M);
+  for (size_t i = 0; i < M; ++i) id[i] = (uint32_t)i;
+  RTP_CUDA(cudaMemcpy(h->ids, id.data(), sizeof(uint32_t) * M, cudaMemcpyHostToDevice));
+  return RTP_OK;
+}
+
+static void free_handle(Handle* h) {
+  if (!h) return;
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->ground) cudaFree(h->ground);
+  if (h->flush) cudaFree(h->flush);
+  for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+  if (h->t0) cudaEventDestroy(h->t0);
+  if (h->t1) cudaEventDestroy(h->t1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+static void invalidate(Handle* h) { h->graphValid = false; }
+
+// ---- one model step (the update() sequences) ------------------------------------------
+static int record_fluids_step(Handle* h, Launcher& L) {
+  const uint32_t n = (uint32_t)h->curN;
+  if (n == 0) return RTP_OK;
+  const GridK& g = h->g;
+  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
+  RTP_TRY(launch_sort_clear(plan, h->ss, L));
+  // Fluids.cpp:412-417: predict, cell ids, sort {pos, vel, predPos} (+ ids).
+  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, L));
+  GatherList gl;
+  gl.src4[0] = h->pos;
+  gl.dst4[0] = h->posS;
+  gl.src4[1] = h->vel;
+  gl.dst4[1] = h->velS;
+  gl.src4[2] = h->predTmp;
+  gl.dst4[2] = h->predA;
+  gl.n4 = 3;
+  gl.src1[0] = h->ids;
+  gl.dst1[0] = h->idsS;
+  gl.n1 = 1;
+  RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
+  // Fluids.cpp:419-424.
+  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  // Fluids.cpp:427-442.
+  float4* cur = h->predA;
+  float4* nxt = h->predB;
+  for (uint32_t it = 0; it < h->iters; ++it) {
+    RTP_TRY(fluid_iteration(g, fk, cur, nxt, h->table, n, h->lambda, h->density, it + 1 == h->iters, h->posS, h->velS, L));
+    std::swap(cur, nxt);
+  }
+  if (h->iters == 0) RTP_TRY(fluid_update_vel(g, fk, cur, h->posS, n, h->velS, L));
+  h->predFinal = cur;
+  // Fluids.cpp:444-457.
+  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, L);
+}
+
+static int record_boids_step(Handle* h, Launcher& L) {
+  const uint32_t n = (uint32_t)h->curN;
+  if (n == 0) return RTP_OK;
+  const GridK& g = h->g;
+  const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
+  RTP_TRY(launch_sort_clear(plan, h->ss, L));
+  // Boids.cpp:335-344.
+  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L));
+  GatherList gl;
+  gl.src4[0] = h->pos;
+  gl.dst4[0] = h->posS;
+  gl.src4[1] = h->vel;
+  gl.dst4[1] = h->velS;
+  gl.n4 = 2;
+  gl.src1[0] = h->ids;
+  gl.dst1[0] = h->idsS;
+  gl.n1 = 1;
+  RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
+  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  // Boids.cpp:346-373.
+  BoidsK bk;
+  bk.velocityScale = h->bp.velocityScale;
+  bk.alignmentScale = h->bp.alignmentScale;
+  bk.separationScale = h->bp.separationScale;
+  bk.cohesionScale = h->bp.cohesionScale;
+  bk.dt = h->boidsDt;
+  bk.maxVelocity = h->bp.velocityScale;
+  return boids_rules_update(g, bk, h->boundary == RTP_BOUNDARY_CYCLIC_WALL, h->posS, h->velS, h->table, n, h->idsS,
+                            h->pos, h->vel, h->acc, h->ids, L);
+}
+
+static CloudK make_cloudk(const Handle* h) {
+  CloudK c;
+  c.dim = h->cp.dim;
+  c.dt = h->cp.timeStep;
+  c.cloudRho0 = h->cp.restDensity;
+  c.cloudRelax = h->cp.relaxCFM;
+  c.groundHeat = h->cp.groundHeatCoeff;
+  c.buoyancy = h->cp.buoyancyCoeff;
+  c.gravCoeff = h->cp.gravCoeff;
+  c.adiabatic = h->cp.adiabaticLapseRate;
+  c.phaseRate = h->cp.phaseTransitionRate;
+  c.latent = h->cp.latentHeatCoeff;
+  c.initVapor = h->cp.initVaporDensityCoeff;
+  c.wind = h->cp.windCoeff;
+  c.smoothing = h->cp.isTempSmoothingEnabled ? 1 : 0;
+  c.T0 = h->env.groundTemp0;
+  c.lapse = h->env.lapseRate;
+  c.heatDecay = h->env.heatDecay;
+  c.windX = h->env.windDecayX;
+  c.windZ = h->env.windDecayZ;
+  c.ground = h->ground;
+  c.nx = h->ground ? h->env.groundNx : 0u;
+  c.nz = h->ground ? h->env.groundNz : 0u;
+  return c;
+}
+
+// Clouds::update (Clouds.cpp:503-610).
+int record_clouds_step(Handle* h, Launcher& L) {
+  const uint32_t n = (uint32_t)h->curN;
+  if (n == 0) return RTP_OK;
+  const GridK& g = h->g;
+  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const CloudK ck = make_cloudk(h);
+  const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
+  RTP_TRY(launch_sort_clear(plan, h->ss, L));
+  // Clouds.cpp:516-541: thermodynamics, predict, mixed boundary, cell ids.
+  RTP_TRY(cloud_presort(g, ck, h->pos, h->vel, n, h->temp, h->vapor, h->cloud, h->buoy, h->predTmp, h->totCorr,
+                        h->ss.keysA, plan, h->ss.hist, L));
+  // Clouds.cpp:543.
+  GatherList gl;
+  gl.src4[0] = h->pos;
+  gl.dst4[0] = h->posS;
+  gl.src4[1] = h->vel;
+  gl.dst4[1] = h->velS;
+  gl.src4[2] = h->predTmp;
+  gl.dst4[2] = h->predA;
+  gl.src4[3] = h->totCorr;
+  gl.dst4[3] = h->totCorrS;
+  gl.n4 = 4;
+  gl.src1[0] = reinterpret_cast<const uint32_t*>(h->temp);
+  gl.dst1[0] = reinterpret_cast<uint32_t*>(h->tempS);
+  gl.src1[1] = reinterpret_cast<const uint32_t*>(h->buoy);
+  gl.dst1[1] = reinterpret_cast<uint32_t*>(h->buoyS);
+  gl.src1[2] = reinterpret_cast<const uint32_t*>(h->vapor);
+  gl.dst1[2] = reinterpret_cast<uint32_t*>(h->vaporS);
+  gl.src1[3] = reinterpret_cast<const uint32_t*>(h->cloud);
+  gl.dst1[3] = reinterpret_cast<uint32_t*>(h->cloudS);
+  gl.src1[4] = h->ids;
+  gl.dst1[4] = h->idsS;
+  gl.n1 = 5;
+  RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
+  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  // Clouds.cpp:554-567.
+  if (ck.smoothing) RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, L));
+  // Clouds.cpp:570-590.
+  float4* cur = h->predA;
+  float4* nxt = h->predB;
+  for (uint32_t it = 0; it < h->iters; ++it) {
+    RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == h->iters,
+                            h->velS, L));
+    std::swap(cur, nxt);
+  }
+  if (h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
+  h->predFinal = cur;
+  // Clouds.cpp:592-605.
+  CloudState s;
+  s.pos = h->pos;
+  s.vel = h->vel;
+  s.temp = h->temp;
+  s.vapor = h->vapor;
+  s.cloud = h->cloud;
+  s.buoy = h->buoy;
+  s.tempS = h->tempS;
+  s.vaporS = h->vaporS;
+  s.cloudS = h->cloudS;
+  s.buoyS = h->buoyS;
+  s.ids = h->ids;
+  s.idsS = h->idsS;
+  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, L);
+}
+
+// ---- Model::reset: reference defaults + the case's initial particles ------------------
+struct V3 {
+  float x, y, z;
+};
+
+// Geometry::GenerateBoxGrid, uniform (utils/Geometry.cpp:190-219).
+static void box_grid(std::vector<V3>& out, const int res[3], V3 s, V3 e) {
+  const V3 sp = {(e.x - s.x) / res[0], (e.y - s.y) / res[1], (e.z - s.z) / res[2]};
+  for (int ix = 0; ix < res[0]; ++ix)
+    for (int iy = 0; iy < res[1]; ++iy)
+      for (int iz = 0; iz < res[2]; ++iz) out.push_back({s.x + ix * sp.x, s.y + iy * sp.y, s.z + iz * sp.z});
+}
+
+// Geometry::GenerateBoxGrid, random (utils/Geometry.cpp:220-230), seeded instead of rand().
+static void box_random(std::vector<V3>& out, int count, V3 s, V3 e, uint64_t seed) {
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto next = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return (float)((st >> 40) & 0xFFFFFF) / (float)0xFFFFFF;
+  };
+  const V3 v = {e.x - s.x, e.y - s.y, e.z - s.z};
+  for (int i = 0; i < count; ++i) {
+    const float a = next(), b = next(), c = next();
+    out.push_back({a * v.x + s.x, b * v.y + s.y, c * v.z + s.z});
+  }
+}
+
+// Geometry::GenerateSphereGrid (utils/Geometry.cpp:236-263).
+static void sphere_grid(std::vector<V3>& out, const int res[3], V3 s, V3 e) {
+  const V3 v = {e.x - s.x, e.y - s.y, e.z - s.z};
+  const V3 c = {s.x + v.x / 2.0f, s.y + v.y / 2.0f, s.z + v.z / 2.0f};
+  const float radius = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z) / 2.0f;
+  const float dphi = PI_F / res[0], dth = 2.0f * PI_F / res[1], dr = radius / res[2];
+  for (int ip = 0; ip < res[0]; ++ip)
+    for (int it = 0; it < res[1]; ++it)
+      for (int ir = 0; ir < res[2]; ++ir) {
+        const float r = (ir + 1) * dr;
+        out.push_back({c.x + r * std::cos(it * dth) * std::sin(ip * dphi), c.y + r * std::sin(it * dth) * std::sin(ip * dphi),
+                       c.z + r * std::cos(ip * dphi)});
+      }
+}
+
+// Utils::ALL_NB_PARTICLES subdiv3D (utils/Parameters.hpp:89-98).
+static bool subdiv3(uint64_t n, int out[3]) {
+  static const struct {
+    uint64_t n;
+    int s[3];
+  } T[] = {{512, {8, 8, 8}},       {1024, {16, 8, 8}},     {4096, {16, 16, 16}}, {8192, {32, 16, 16}},
+           {16384, {32, 32, 16}},  {32768, {32, 32, 32}}, {65536, {64, 32, 32}}, {131072, {64, 64, 32}}};
+  for (const auto& e : T)
+    if (e.n == n) {
+      out[0] = e.s[0];
+      out[1] = e.s[1];
+      out[2] = e.s[2];
+      return true;
+    }
+  return false;
+}
+
+static int init_case(Handle* h) {
+  const float bx = h->mp.boxSize[0], by = h->mp.boxSize[1], bz = h->mp.boxSize[2];
+  std::vector<V3> verts;
+  int res[3];
+  uint64_t n = 0;
+  const int pc = h->mp.pCase;
+  if (h->model == RTP_MODEL_FLUIDS) {
+    if (pc == RTP_CASE_FLUIDS_DAM) {  // Fluids.cpp:341-346
+      n = 131072;
+      subdiv3(n, res);
+      box_grid(verts, res, {bx / -2.0f, by / -2.0f, bz / -2.0f}, {bx / 2.0f, 0.0f, 0.0f});
+    } else if (pc == RTP_CASE_FLUIDS_BOMB) {  // :347-352
+      n = 65536;
+      subdiv3(n, res);
+      sphere_grid(verts, res, {bx / -6.0f, by / -6.0f, bz / -6.0f}, {bx / 6.0f, by / 6.0f, bz / 6.0f});
+    } else if (pc == RTP_CASE_FLUIDS_DROP) {  // :353-380
+      n = 4096;
+      subdiv3(n, res);
+      box_grid(verts, res, {bx / -10.0f, 2.0f * by / 10.0f, bz / -10.0f}, {bx / 10.0f, 4.0f * by / 10.0f, bz / 10.0f});
+      const int bottom[3] = {64, 16, 64};
+      box_grid(verts, bottom, {bx / -2.0f, by / -2.0f, bz / -2.0f}, {bx / 2.0f, by / -2.55f, bz / 2.0f});
+      n += 65536;
+    } else {
+      return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a fluids case");
+    }
+  } else if (h->model == RTP_MODEL_BOIDS) {  // Boids.cpp:235-257, 300-308
+    if (pc == RTP_CASE_BOIDS_SMALL) n = 512;
+    else if (pc == RTP_CASE_BOIDS_MEDIUM) n = 16384;
+    else if (pc == RTP_CASE_BOIDS_LARGE) n = 65536;
+    else if (pc == RTP_CASE_BOIDS_XLARGE) n = 131072;
+    else return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a boids case");
+    subdiv3(n, res);
+    sphere_grid(verts, res, {bx / -6.0f, by / -6.0f, bz / -6.0f}, {bx / 6.0f, by / 6.0f, bz / 6.0f});
+  } else {  // Clouds.cpp:451-471
+    n = 65536;
+    if (pc == RTP_CASE_CLOUDS_CUMULUS)
+      box_random(verts, (int)n, {bx / -2.0f, by / -2.0f, bz / -2.0f}, {bx / 2.0f, by / -4.0f, bz / 2.0f}, 1);
+    else if (pc == RTP_CASE_CLOUDS_HOMOGENEOUS)
+      box_random(verts, (int)n, {bx / -2.0f, by / -2.0f, bz / -2.0f}, {bx / 2.0f, by / 2.0f, bz / 2.0f}, 1);
+    else
+      return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a clouds case");
+  }
+  if (n > h->maxN) return fail(RTP_ERR_CAPACITY, "rtp_reset: the case needs more than maxNbParticles");
+  const float inf = INFINITY;
+  std::vector<float4> pos(h->maxN, make_float4(inf, inf, inf, 0.0f)), vel(h->maxN, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (size_t i = 0; i < verts.size() && i < n; ++i) pos[i] = make_float4(verts[i].x, verts[i].y, verts[i].z, 0.0f);
+  if (h->model == RTP_MODEL_BOIDS) vel = pos;  // Boids.cpp:317-318: vel initialised from the position buffer
+  std::vector<uint32_t> id(h->maxN);
+  for (size_t i = 0; i < id.size(); ++i) id[i] = (uint32_t)i;
+  RTP_CUDA(cudaMemcpyAsync(h->pos, pos.data(), sizeof(float4) * h->maxN, cudaMemcpyHostToDevice, h->stream));
+  RTP_CUDA(cudaMemcpyAsync(h->vel, vel.data(), sizeof(float4) * h->maxN, cudaMemcpyHostToDevice, h->stream));
+  RTP_CUDA(cudaMemcpyAsync(h->ids, id.data(), sizeof(uint32_t) * h->maxN, cudaMemcpyHostToDevice, h->stream));
+  h->curN = n;
+  if (h->model == RTP_MODEL_CLOUDS) {
+    Launcher L;
+    L.stream = h->stream;
+    RTP_TRY(cloud_init(h->g, make_cloudk(h), h->pos, (uint32_t)h->maxN, h->temp, h->vapor, h->cloud, h->buoy, L));
+  }
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasStep = false;
+  return RTP_OK;
+}
+
+static int record_step(Handle* h, Launcher& L) {
+  switch (h->model) {
+    case RTP_MODEL_FLUIDS:
+      return record_fluids_step(h, L);
+    case RTP_MODEL_BOIDS:
+      return record_boids_step(h, L);
+    case RTP_MODEL_CLOUDS:
+      return record_clouds_step(h, L);
+  }
+  return fail(RTP_ERR_STATE, "unknown model");
+}
+
+static int build_graph(Handle* h) {
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  h->slots.clear();
+  Launcher L;
+  L.stream = h->stream;
+  L.profiling = h->profiling;
+  L.owner = h;
+  RTP_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = record_step(h, L);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(h->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+  const cudaError_t ei = cudaGraphInstantiate(&h->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate");
+  h->graphValid = true;
+  h->graphProfiled = h->profiling;
+  return RTP_OK;
+}
+
+static int collect_profile(Handle* h) {
+  if (!h->graphProfiled || h->slots.empty()) return RTP_OK;
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  for (const TimedSlot& s : h->slots) {
+    float ms = 0.0f;
+    RTP_CUDA(cudaEventElapsedTime(&ms, h->events[s.ev], h->events[s.ev + 1]));
+    KernelStat& k = h->stats[s.name];
+    k.launches += 1;
+    k.ms += ms;
+  }
+  return RTP_OK;
+}
+
+static int run_steps(Handle* h, uint32_t nsteps) {
+  if (h->paused || nsteps == 0 || h->curN == 0) return RTP_OK;
+  if (!h->graphValid || h->graphProfiled != h->profiling) RTP_TRY(build_graph(h));
+  for (uint32_t s = 0; s < nsteps; ++s) {
+    RTP_CUDA(cudaGraphLaunch(h->graph, h->stream));
+    if (h->graphProfiled) RTP_TRY(collect_profile(h));
+  }
+  h->hasStep = true;
+  return RTP_OK;
+}
+
+static Handle* H(void* p) { return reinterpret_cast<Handle*>(p); }
+
+}  // namespace rtp
+
+using namespace rtp;
+
+#define RTP_GUARD_BEGIN try {
+#define RTP_GUARD_END                                              \
+  }                                                                \
+  catch (const std::bad_alloc&) {                                  \
+    return fail(RTP_ERR_OUT_OF_MEMORY, "host allocation failed");  \
+  }                                                                \
+  catch (...) {                                                    \
+    return fail(RTP_ERR_STATE, "unexpected C++ exception");        \
+  }
+
+extern "C" {
+
+const char* rtp_last_error(void) { return g_last_error.c_str(); }
+int rtp_abi_version(void) { return RTP_ABI_VERSION; }
+
+int rtp_get_constants(int model, const rtp_model_params* params, rtp_grid_constants* out) {
+  RTP_GUARD_BEGIN
+  if (model < RTP_MODEL_BOIDS || model > RTP_MODEL_CLOUDS) return fail(RTP_ERR_INVALID_ARGUMENT, "unknown model");
+  return derive_constants(model, params, out);
+  RTP_GUARD_END
+}
+
+// JSON defaults: Fluids.cpp:52-74.
+int rtp_fluid_params_default(rtp_fluid_params* p) {
+  if (!p) return fail(RTP_ERR_INVALID_ARGUMENT, "null");
+  p->restDensity = 450.0f;
+  p->relaxCFM = 600.0f;
+  p->timeStep = 0.010f;
+  p->dim = 3;
+  p->isArtPressureEnabled = 1;
+  p->artPressureRadius = 0.006f;
+  p->artPressureCoeff = 0.001f;
+  p->artPressureExp = 4;
+  p->isVorticityConfEnabled = 1;
+  p->vorticityConfCoeff = 0.0004f;
+  p->xsphViscosityCoeff = 0.0001f;
+  return RTP_OK;
+}
+
+// JSON defaults: Boids.cpp:41-73 (all rules enabled).
+int rtp_boids_params_default(rtp_boids_params* p) {
+  if (!p) return fail(RTP_ERR_INVALID_ARGUMENT, "null");
+  p->velocityScale = 0.5f;
+  p->alignmentScale = 1.6f;
+  p->separationScale = 1.6f;
+  p->cohesionScale = 1.45f;
+  return RTP_OK;
+}
+
+// JSON defaults: Clouds.cpp:67-102 (shared fluid values copied as in :307-311).
+int rtp_cloud_params_default(rtp_cloud_params* p) {
+  if (!p) return fail(RTP_ERR_INVALID_ARGUMENT, "null");
+  p->dim = 3;
+  p->timeStep = 0.010f;
+  p->restDensity = 450.0f;
+  p->groundHeatCoeff = 10.0f;
+  p->buoyancyCoeff = 0.10f;
+  p->gravCoeff = 0.0005f;
+  p->adiabaticLapseRate = 5.0f;
+  p->phaseTransitionRate = 0.3485f;
+  p->latentHeatCoeff = 0.07f;
+  p->isTempSmoothingEnabled = 1;
+  p->relaxCFM = 600.0f;
+  p->initVaporDensityCoeff = 0.75f;
+  p->windCoeff = 1.0f;
+  return RTP_OK;
+}
+
+// Constants of clouds.cl:72-89 and :951-952.
+int rtp_cloud_env_reference(rtp_cloud_env* e) {
+  if (!e) return fail(RTP_ERR_INVALID_ARGUMENT, "null");
+  e->groundTemp0 = 293.0f;
+  e->lapseRate = 3.5f;
+  e->heatDecay = 3.0f;
+  e->windDecayX = 0.2f;
+  e->windDecayZ = 0.3f;
+  e->groundNx = 0;
+  e->groundNz = 0;
+  return RTP_OK;
+}
+
+int rtp_create(int model, const rtp_model_params* params, void** out_handle) {
+  RTP_GUARD_BEGIN
+  if (!params || !out_handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: null argument");
+  *out_handle = nullptr;
+  if (model < RTP_MODEL_BOIDS || model > RTP_MODEL_CLOUDS) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: unknown model");
+  if (params->maxNbParticles == 0 || params->maxNbParticles > 0x7FFFFFFFull)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: maxNbParticles must be in [1, 2^31)");
+  if (params->currNbParticles > params->maxNbParticles)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: currNbParticles > maxNbParticles");
+  if (params->dimension != 3 && params->dimension != 2)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: dimension must be 2 or 3");
+  if (params->dimension == 2) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_create: 2D models are not built yet");
+  int ndev = 0;
+  const cudaError_t de = cudaGetDeviceCount(&ndev);
+  if (de != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(RTP_ERR_NO_DEVICE, "rtp_create: no CUDA device");
+  }
+  Handle* h = new Handle();
+  h->model = model;
+  h->mp = *params;
+  h->maxN = params->maxNbParticles;
+  h->curN = params->currNbParticles;
+  int rc = derive_constants(model, params, &h->gc);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  h->g = make_gridk(h->gc);
+  rtp_fluid_params_default(&h->fp);
+  rtp_boids_params_default(&h->bp);
+  rtp_cloud_params_default(&h->cp);
+  rtp_cloud_env_reference(&h->env);
+  h->iters = (model == RTP_MODEL_CLOUDS) ? 1u : 2u;  // Clouds.cpp:111, Fluids.cpp:81
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  rc = alloc_buffers(h);
+  if (!rc) {
+    e = cudaEventCreate(&h->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->t1);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
+  }
+  if (rc) {
+    free_handle(h);
+    return rc;
+  }
+  *out_handle = h;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_destroy(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return RTP_OK;
+  Handle* h = H(handle);
+  cudaStreamSynchronize(h->stream);
+  free_handle(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_update(void* handle, uint32_t nsteps) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_update: null handle");
+  return run_steps(H(handle), nsteps);
+  RTP_GUARD_END
+}
+
+int rtp_reset(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: null handle");
+  Handle* h = H(handle);
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  rtp_fluid_params_default(&h->fp);
+  rtp_boids_params_default(&h->bp);
+  rtp_cloud_params_default(&h->cp);
+  h->iters = (h->model == RTP_MODEL_CLOUDS) ? 1u : 2u;
+  h->boidsDt = 0.1f;
+  invalidate(h);
+  return init_case(h);
+  RTP_GUARD_END
+}
+
+int rtp_clouds_init(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_clouds_init: null handle");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_CLOUDS) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_clouds_init: not a clouds model");
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(cloud_init(h->g, make_cloudk(h), h->pos, (uint32_t)h->curN, h->temp, h->vapor, h->cloud, h->buoy, L));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_set_fluid_params(void* handle, const rtp_fluid_params* p) {
+  if (!handle || !p) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_fluid_params: null argument");
+  if (!(p->restDensity > 0.0f) || !(p->timeStep > 0.0f))
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_fluid_params: restDensity and timeStep must be > 0");
+  H(handle)->fp = *p;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_get_fluid_params(void* handle, rtp_fluid_params* p) {
+  if (!handle || !p) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_get_fluid_params: null argument");
+  *p = H(handle)->fp;
+  return RTP_OK;
+}
+
+int rtp_set_jacobi_iterations(void* handle, uint32_t iters) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  if (iters > 64) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_jacobi_iterations: at most 64");
+  H(handle)->iters = iters;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_set_boids_params(void* handle, const rtp_boids_params* p) {
+  if (!handle || !p) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_boids_params: null argument");
+  H(handle)->bp = *p;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_set_boids_time_step(void* handle, float dt) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  H(handle)->boidsDt = dt;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_set_cloud_params(void* handle, const rtp_cloud_params* p) {
+  if (!handle || !p) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_cloud_params: null argument");
+  H(handle)->cp = *p;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_set_cloud_environment(void* handle, const rtp_cloud_env* env, const float* groundTemp) {
+  RTP_GUARD_BEGIN
+  if (!handle || !env) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_cloud_environment: null argument");
+  Handle* h = H(handle);
+  const bool field = groundTemp && env->groundNx >= 2 && env->groundNz >= 2;
+  if (h->ground) {
+    RTP_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(h->ground);
+    h->ground = nullptr;
+  }
+  h->env = *env;
+  if (field) {
+    const size_t cnt = (size_t)env->groundNx * env->groundNz;
+    RTP_CUDA(cudaMalloc((void**)&h->ground, sizeof(float) * cnt));
+    RTP_CUDA(cudaMemcpy(h->ground, groundTemp, sizeof(float) * cnt, cudaMemcpyHostToDevice));
+  } else {
+    h->env.groundNx = h->env.groundNz = 0;
+  }
+  invalidate(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_set_nb_particles(void* handle, uint64_t n) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  if (n > H(handle)->maxN) return fail(RTP_ERR_CAPACITY, "rtp_set_nb_particles: n > maxNbParticles");
+  H(handle)->curN = n;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_get_nb_particles(void* handle, uint64_t* n) {
+  if (!handle || !n) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  *n = H(handle)->curN;
+  return RTP_OK;
+}
+
+int rtp_set_boundary(void* handle, int boundary) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  if (boundary != RTP_BOUNDARY_BOUNCING_WALL && boundary != RTP_BOUNDARY_CYCLIC_WALL)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_boundary: unknown boundary");
+  H(handle)->boundary = boundary;
+  invalidate(H(handle));
+  return RTP_OK;
+}
+
+int rtp_set_dimension(void* handle, uint32_t dim) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  if (dim == 3) {
+    H(handle)->mp.dimension = 3;
+    return rtp_reset(handle);
+  }
+  if (dim == 2) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_dimension: 2D models are not built yet");
+  return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_dimension: dimension must be 2 or 3");
+}
+
+int rtp_set_case(void* handle, int pcase) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  H(handle)->mp.pCase = pcase;
+  return RTP_OK;
+}
+
+int rtp_pause(void* handle, int pause) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  H(handle)->paused = pause != 0;
+  return RTP_OK;
+}
+
+static int buffer_info(Handle* h, int buf, void** dptr, size_t* elem, uint64_t* cap) {
+  *cap = h->maxN;
+  switch (buf) {
+    case RTP_BUF_POS: *dptr = h->pos; *elem = 16; break;
+    case RTP_BUF_VEL: *dptr = h->vel; *elem = 16; break;
+    case RTP_BUF_PRED_POS: *dptr = h->predFinal; *elem = 16; break;
+    case RTP_BUF_DENSITY: *dptr = h->density; *elem = 4; break;
+    case RTP_BUF_LAMBDA: *dptr = h->lambda; *elem = 4; break;
+    case RTP_BUF_TEMP: *dptr = h->temp; *elem = 4; break;
+    case RTP_BUF_VAPOR: *dptr = h->vapor; *elem = 4; break;
+    case RTP_BUF_CLOUD: *dptr = h->cloud; *elem = 4; break;
+    case RTP_BUF_BUOYANCY: *dptr = h->buoy; *elem = 4; break;
+    case RTP_BUF_ID: *dptr = h->ids; *elem = 4; break;
+    case RTP_BUF_CELL_ID: *dptr = h->cellId; *elem = 4; break;
+    case RTP_BUF_CELL_TABLE: *dptr = h->tableRef; *elem = 8; *cap = h->gc.numCells; break;
+    case RTP_BUF_VORTICITY: *dptr = h->vort; *elem = 16; break;
+    case RTP_BUF_ACC: *dptr = h->acc; *elem = 16; break;
+    default: return fail(RTP_ERR_INVALID_ARGUMENT, "unknown buffer");
+  }
+  if (!*dptr) return fail(RTP_ERR_INVALID_ARGUMENT, "buffer not used by this model");
+  return RTP_OK;
+}
+
+int rtp_upload(void* handle, int buffer, const void* host, uint64_t count) {
+  RTP_GUARD_BEGIN
+  if (!handle || (count && !host)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_upload: null argument");
+  Handle* h = H(handle);
+  void* d;
+  size_t elem;
+  uint64_t cap;
+  RTP_TRY(buffer_info(h, buffer, &d, &elem, &cap));
+  if (buffer == RTP_BUF_CELL_TABLE || buffer == RTP_BUF_CELL_ID)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_upload: derived buffer is read-only");
+  if (count > cap) return fail(RTP_ERR_CAPACITY, "rtp_upload: count exceeds capacity");
+  RTP_CUDA(cudaMemcpyAsync(d, host, elem * count, cudaMemcpyHostToDevice, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_download(void* handle, int buffer, void* host, uint64_t count) {
+  RTP_GUARD_BEGIN
+  if (!handle || (count && !host)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_download: null argument");
+  Handle* h = H(handle);
+  void* d;
+  size_t elem;
+  uint64_t cap;
+  RTP_TRY(buffer_info(h, buffer, &d, &elem, &cap));
+  if (count > cap) return fail(RTP_ERR_CAPACITY, "rtp_download: count exceeds capacity");
+  if (buffer == RTP_BUF_CELL_TABLE) {
+    Launcher L;
+    L.stream = h->stream;
+    RTP_TRY(launch_cell_table_to_reference(h->g, h->table, h->tableRef, L));
+  }
+  RTP_CUDA(cudaMemcpyAsync(host, d, elem * count, cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_device_ptr(void* handle, int buffer, void** dptr) {
+  if (!handle || !dptr) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_device_ptr: null argument");
+  size_t elem;
+  uint64_t cap;
+  return buffer_info(H(handle), buffer, dptr, &elem, &cap);
+}
+
+int rtp_stream(void* handle, void** stream) {
+  if (!handle || !stream) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  *stream = (void*)H(handle)->stream;
+  return RTP_OK;
+}
+
+int rtp_synchronize(void* handle) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  RTP_CUDA(cudaStreamSynchronize(H(handle)->stream));
+  return RTP_OK;
+}
+
+int rtp_enable_profiling(void* handle, int enable) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  H(handle)->profiling = enable != 0;
+  return RTP_OK;
+}
+
+int rtp_is_profiling_enabled(void* handle, int* enabled) {
+  if (!handle || !enabled) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  *enabled = H(handle)->profiling ? 1 : 0;
+  return RTP_OK;
+}
+
+int rtp_get_kernel_times(void* handle, rtp_kernel_time* out, uint32_t capacity, uint32_t* count) {
+  RTP_GUARD_BEGIN
+  if (!handle || !count) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  uint32_t i = 0;
+  for (const auto& kv : h->stats) {
+    if (out && i < capacity) {
+      std::memset(out[i].name, 0, sizeof out[i].name);
+      std::strncpy(out[i].name, kv.first.c_str(), sizeof(out[i].name) - 1);
+      out[i].launches = kv.second.launches;
+      out[i].total_ms = kv.second.ms;
+    }
+    ++i;
+  }
+  *count = i;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_reset_kernel_times(void* handle) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  H(handle)->stats.clear();
+  return RTP_OK;
+}
+
+int rtp_time_steps(void* handle, uint32_t nsteps, uint64_t flush_bytes, double* total_ms) {
+  RTP_GUARD_BEGIN
+  if (!handle || !total_ms) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  *total_ms = 0.0;
+  if (h->curN == 0 || nsteps == 0) return RTP_OK;
+  if (flush_bytes && flush_bytes != h->flushBytes) {
+    if (h->flush) cudaFree(h->flush);
+    h->flush = nullptr;
+    h->flushBytes = 0;
+    RTP_CUDA(cudaMalloc(&h->flush, flush_bytes));
+    h->flushBytes = flush_bytes;
+  }
+  if (!h->graphValid || h->graphProfiled != h->profiling) RTP_TRY(build_graph(h));
+  for (uint32_t s = 0; s < nsteps; ++s) {
+    if (flush_bytes) RTP_CUDA(cudaMemsetAsync(h->flush, (int)(s & 0xff), flush_bytes, h->stream));
+    RTP_CUDA(cudaEventRecord(h->t0, h->stream));
+    RTP_CUDA(cudaGraphLaunch(h->graph, h->stream));
+    RTP_CUDA(cudaEventRecord(h->t1, h->stream));
+    RTP_CUDA(cudaEventSynchronize(h->t1));
+    float ms = 0.0f;
+    RTP_CUDA(cudaEventElapsedTime(&ms, h->t0, h->t1));
+    *total_ms += ms;
+    if (h->graphProfiled) RTP_TRY(collect_profile(h));
+  }
+  h->hasStep = true;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_get_metrics(void* handle, rtp_metrics* out) {
+  RTP_GUARD_BEGIN
+  if (!handle || !out) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  std::memset(out, 0, sizeof *out);
+  if (h->model == RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_get_metrics: fluids and clouds only");
+  if (!h->hasStep) return fail(RTP_ERR_STATE, "rtp_get_metrics: run a step first (the cell table is built by update)");
+  const uint32_t n = (uint32_t)h->curN;
+  if (n == 0) return RTP_OK;
+  RTP_CUDA(cudaMemsetAsync(h->mAcc, 0, sizeof(double) * 4, h->stream));
+  RTP_CUDA(cudaMemsetAsync(h->mHist, 0, sizeof(uint32_t) * 80, h->stream));
+  Launcher L;
+  L.stream = h->stream;
+  rtp_fluid_params fp = h->fp;
+  if (h->model == RTP_MODEL_CLOUDS) fp.restDensity = h->fp.restDensity;
+  RTP_TRY(fluid_metrics(h->g, make_fluidk(h->gc, fp), h->predFinal, h->vel, h->table, n, h->mAcc, h->mHist, L));
+  double acc[4];
+  uint32_t hist[80];
+  RTP_CUDA(cudaMemcpyAsync(acc, h->mAcc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaMemcpyAsync(hist, h->mHist, sizeof hist, cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  out->meanDensityError = acc[0] / n;
+  float mx;
+  std::memcpy(&mx, &hist[64], sizeof mx);
+  out->maxDensityError = mx;
+  out->kineticEnergy = acc[1];
+  out->meanNeighbours = acc[2] / n;
+  for (int i = 0; i < 64; ++i) out->neighbourHist[i] = hist[i];
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+}  // extern "C"

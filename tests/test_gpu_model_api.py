@@ -1,0 +1,91 @@
+"""Model API behaviour on the GPU: reset cases, setters, JSON inputs, errors, buffers,
+profiling (physics/Model.hpp:81-216, physics/ocl/OclModel.hpp)."""
+import numpy as np
+import pytest
+
+from realtimeparticles_gb300 import RtpError, abi, model, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_params(mtype, case, box=(10.0, 10.0, 10.0), res=(30, 30, 30)):
+    # ParticleSystemApp::initPhysicsEngine (app/ParticleSystemApp.cpp:275-318).
+    return abi.model_params(0, 131072, box, res, 3, case)
+
+
+@pytest.mark.parametrize("mtype,case,n", [(abi.FLUIDS, abi.CASE_FLUIDS_DAM, 131072),
+                                          (abi.FLUIDS, abi.CASE_FLUIDS_BOMB, 65536),
+                                          (abi.FLUIDS, abi.CASE_FLUIDS_DROP, 4096 + 65536),
+                                          (abi.BOIDS, abi.CASE_BOIDS_SMALL, 512),
+                                          (abi.BOIDS, abi.CASE_BOIDS_XLARGE, 131072)])
+def test_reset_cases(mtype, case, n):
+    with model.CreateModel(mtype, _ref_params(mtype, case)) as m:
+        m.reset()
+        assert m.nbParticles() == n
+        pos = m.download(abi.BUF_POS, m.maxNbParticles())
+        assert np.all(np.isfinite(pos[:n, :3]))
+        if n < m.maxNbParticles():
+            assert np.all(np.isinf(pos[n:, :3]))  # inactive slots at +inf (Fluids.cpp:383-384)
+        m.update(2)
+        assert np.all(np.isfinite(m.download(abi.BUF_POS)[:, :3]))
+
+
+def test_clouds_reset_case():
+    p = _ref_params(abi.CLOUDS, abi.CASE_CLOUDS_CUMULUS, box=(10.0, 20.0, 10.0), res=(30, 60, 30))
+    with model.Clouds(p) as m:
+        m.reset()
+        assert m.nbParticles() == 65536
+        t = m.download(abi.BUF_TEMP)
+        assert t.min() >= 223.0 - 1e-3 and t.max() <= 293.0 + 1e-3
+        m.update(3)
+        t = m.download(abi.BUF_TEMP)
+        assert np.all(np.isfinite(t))
+
+
+def test_json_inputs_and_wrong_path():
+    sc = scenes.dam_break(lattice=(8, 8, 8))
+    with model.Fluids(sc["model_params"]) as m:
+        m.updateInputJson({"Fluids": {"Rest Density": [500.0, 10.0, 1000.0], "Nb Jacobi Iterations": [3, 1, 6]}})
+        assert m.fluidParams().restDensity == 500.0
+        with pytest.raises(RuntimeError, match="Wrong Json parsing"):
+            m.updateModelWithInputJson({"Fluid": {}})
+
+
+def test_errors_and_capacity():
+    sc = scenes.dam_break(lattice=(8, 8, 8))
+    with model.Fluids(sc["model_params"]) as m:
+        with pytest.raises(RtpError) as e:
+            m.setNbParticles(10 ** 6)
+        assert e.value.code == abi.ERR_CAPACITY
+        with pytest.raises(RtpError):
+            m.upload(abi.BUF_POS, np.zeros((10 ** 6, 4), np.float32))
+        with pytest.raises(RtpError):
+            m.setBoundary(7)
+        with pytest.raises(RtpError) as e:
+            m.setDimension(2)
+        assert e.value.code == abi.ERR_NOT_SUPPORTED
+    with pytest.raises(RtpError):
+        model.Fluids(abi.model_params(10, 5, (1, 1, 1), (4, 4, 4)))
+
+
+def test_pause_profiling_and_device_pointers():
+    sc = scenes.dam_break(lattice=(8, 16, 16))
+    with model.Fluids(sc["model_params"]) as m:
+        m.setFluidParams(sc["fluid_params"])
+        m.upload(abi.BUF_POS, sc["pos"])
+        before = m.download(abi.BUF_POS)
+        m.pause(True)
+        m.update(3)
+        assert np.array_equal(m.download(abi.BUF_POS), before)
+        m.pause(False)
+        assert m.devicePtr(abi.BUF_POS) and m.stream()
+        m.enableProfiling(True)
+        assert m.isProfilingEnabled()
+        m.update(2)
+        kt = m.kernelTimes()
+        assert kt["fld_lambda"][0] == 2 * 2 and kt["fld_lambda"][1] > 0
+        assert kt["sort_pass_gather"][0] == 2
+        ms = m.timeSteps(3, flush_bytes=1 << 24)
+        assert ms > 0
+        with pytest.raises(RtpError):
+            m.download(abi.BUF_ACC)
