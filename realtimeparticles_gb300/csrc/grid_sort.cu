@@ -200,6 +200,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     if (valid) {
       const uint32_t d = dig[k];
       pos = s_base[d] + s_wc[warp][d] + rank[k];
+    }
+    // A consistent histogram gives pos < n; the guard keeps an inconsistent one (a bug)
+    // from writing out of bounds: the element is dropped and the parity tests fail.
+    const bool ok = valid && pos < n;
+    if (ok) {
       keys_out[pos] = key[k];
       const uint32_t src = idx_in ? __ldg(idx_in + e) : e;
       if (!LAST) {
@@ -212,9 +217,9 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     }
     if (!LAST) {
       // Next pass's tile histogram, aggregated over lanes hitting the same (tile, digit).
-      const uint32_t slot = valid ? (pos / kSortTile) * kMaxBins + ((key[k] >> next_shift) & nmask) : 0xFFFFFFFFu;
+      const uint32_t slot = ok ? (pos / kSortTile) * kMaxBins + ((key[k] >> next_shift) & nmask) : 0xFFFFFFFFu;
       const uint32_t peers = __match_any_sync(0xffffffffu, slot);
-      if (valid && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
+      if (ok && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
     }
   }
 }

@@ -184,7 +184,8 @@ int Launcher::begin(const char* name) {
     h->events.push_back(e);
   }
   h->slots.push_back({name, ev});
-  RTP_CUDA(cudaEventRecord(h->events[ev], stream));
+  // External record nodes: inside a capture a plain record only orders work.
+  RTP_CUDA(cudaEventRecordWithFlags(h->events[ev], stream, cudaEventRecordExternal));
   return RTP_OK;
 }
 
@@ -192,7 +193,7 @@ int Launcher::end(const char* name) {
   (void)name;
   if (!profiling || !owner) return RTP_OK;
   Handle* h = (Handle*)owner;
-  RTP_CUDA(cudaEventRecord(h->events[h->slots.back().ev + 1], stream));
+  RTP_CUDA(cudaEventRecordWithFlags(h->events[h->slots.back().ev + 1], stream, cudaEventRecordExternal));
   return RTP_OK;
 }
 

