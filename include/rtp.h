@@ -281,6 +281,25 @@ int rtp_radix_sort(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits,
 int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_keys,
                          uint32_t n, uint32_t* d_table2, void* stream);
 
+/* Radix sort that allocates nothing.  No counterpart in the reference (RadixSort owns
+ * its buffers, physics/utils/RadixSort.cpp:78-96).  For callers that cannot allocate device
+ * memory where they sort: a plugin whose host application owns the GPU heap, a frame loop
+ * that must not stall on cudaMalloc's implicit synchronisation, code that must not fail
+ * with out-of-memory after start-up.  Same result as rtp_radix_sort (stable, keys < 2^keyBits,
+ * perm_out optional), using a fixed scratch array inside the library instead of caller
+ * memory:
+ *  - at most RTP_NOALLOC_SORT_MAX_KEYS keys; more returns RTP_ERR_CAPACITY, nothing runs;
+ *  - the array (RTP_NOALLOC_SORT_SCRATCH_BYTES) is held by every GPU that loads the library
+ *    until the process exits;
+ *  - the first call on a device looks up the array's address on that device (make that
+ *    first call before any stream capture);
+ *  - every call shares the array, so calls that overlap on the GPU race: order them on one
+ *    stream or synchronise between them. */
+#define RTP_NOALLOC_SORT_MAX_KEYS 262144u
+#define RTP_NOALLOC_SORT_SCRATCH_BYTES 5251072u
+int rtp_radix_sort_noalloc(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint32_t* d_keys_out,
+                           uint32_t* d_perm_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

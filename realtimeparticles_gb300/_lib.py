@@ -69,6 +69,7 @@ _SIGS = {
     "rtp_radix_sort_scratch_bytes": [U32, U32, C.POINTER(C.c_size_t)],
     "rtp_radix_sort": [P, U32, U32, P, P, P, C.c_size_t, P],
     "rtp_build_cell_table": [C.POINTER(abi.GridConstants), P, U32, P, P],
+    "rtp_radix_sort_noalloc": [P, U32, U32, P, P, P],
 }
 _RESTYPES = {"rtp_last_error": C.c_char_p}
 
