@@ -197,6 +197,8 @@ typedef struct rtp_metrics {
   double kineticEnergy;     /* 0.5 * sum |v|^2 (unit mass) */
   double meanNeighbours;    /* mean neighbours within the effect radius */
   uint32_t neighbourHist[64];
+  uint32_t pairListOverflows; /* particles whose last recorded pair list overflowed */
+  uint32_t pairListMax;       /* longest recorded pair list of the last step */
 } rtp_metrics;
 
 /* Library. */

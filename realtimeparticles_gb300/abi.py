@@ -155,6 +155,8 @@ class Metrics(C.Structure):
         ("kineticEnergy", C.c_double),
         ("meanNeighbours", C.c_double),
         ("neighbourHist", C.c_uint32 * 64),
+        ("pairListOverflows", C.c_uint32),
+        ("pairListMax", C.c_uint32),
     ]
 
 

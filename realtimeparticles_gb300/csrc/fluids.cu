@@ -6,42 +6,22 @@
 //   sort passes           RadixSort::sort of {pos, vel, predPos} (+ particle ids)
 //   cell table            resetStartEndCell / fillStartCell / fillEndCell (+ cap on read)
 //   I x k_fluid_lambda    fld_applyBoundaryCondition (clamp on load) + fld_computeDensity
-//                         + fld_computeConstraintFactor in one neighbour sweep
+//                         + fld_computeConstraintFactor; records the pairs within h
 //   I x k_fluid_deltap    fld_computeConstraintCorrection + fld_correctPosition into a
-//                         second buffer (Jacobi); the last one also does fld_updateVel
-//   k_fluid_vorticity     fld_computeVorticity
+//                         second buffer (Jacobi), over the recorded pairs; the last one
+//                         also does fld_updateVel
+//   k_fluid_vorticity     fld_computeVorticity; records the pairs within h of the final
+//                         positions
 //   k_fluid_confine       fld_applyVorticityConfinement (in place: reads only vort of others)
 //   k_fluid_xsph_final    fld_applyXsphViscosityCorrection + fld_updatePosition, writing
 //                         the state back to the canonical pos/vel buffers
-// Neighbour sweeps visit the reference's 27 cells, wrapped modulo the grid resolution
-// (fluids.cl:101-123), in the same order.
+// The 27-cell searches (fluids.cl:101-123) run in two phases: a filter pass that only
+// compares distances and records the pairs within h in shared memory, then the SPH
+// arithmetic over that compact list, so lanes do not all pay for the arithmetic whenever
+// any lane of the warp has a neighbour.  The list sweeps give 4 lanes to each particle.
 #include "fluids.cuh"
 
 namespace rtp {
-
-template <class F>
-__device__ __forceinline__ void for_each_fluid_neighbour(const GridK& g, const uint2* __restrict__ table, float4 xi,
-                                                         F&& f) {
-  int cx, cy, cz;
-  cell3(g, xi, cx, cy, cz);
-  int xs[3], ys[3], zs[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    xs[d] = (cx + d - 1 + g.R[0]) % g.R[0];
-    ys[d] = (cy + d - 1 + g.R[1]) % g.R[1];
-    zs[d] = (cz + d - 1 + g.R[2]) % g.R[2];
-  }
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b) {
-      const uint32_t row = ((uint32_t)xs[a] * g.R[1] + (uint32_t)ys[b]) * g.R[2];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        uint32_t j0, j1;
-        cell_range(table, row + (uint32_t)zs[c], g.cap, j0, j1);
-        for (uint32_t j = j0; j < j1; ++j) f(j);
-      }
-    }
-}
 
 __device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
 
@@ -50,7 +30,7 @@ __device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return c
 __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK p, const float4* __restrict__ pos,
                                                                 const float4* __restrict__ vel, uint32_t n,
                                                                 float4* __restrict__ pred, uint32_t* __restrict__ keys,
-                                                                int bits0, uint32_t* __restrict__ hist0) {
+                                                                int bits0, uint32_t* __restrict__ hist0, int clampOut) {
   __shared__ uint32_t s_hist[kMaxBins];
   TileHistogram th;
   th.init(s_hist, bits0);
@@ -65,7 +45,10 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK 
       const float4 nv = f4(__fadd_rn(v.x, gx), __fadd_rn(v.y, gy), __fadd_rn(v.z, gx), __fadd_rn(v.w, gx));
       const float4 pp = f4(__fadd_rn(x.x, __fmul_rn(nv.x, dt)), __fadd_rn(x.y, __fmul_rn(nv.y, dt)),
                            __fadd_rn(x.z, __fmul_rn(nv.z, dt)), __fadd_rn(x.w, __fmul_rn(nv.w, dt)));
-      pred[i] = pp;
+      // The key comes from the unclamped prediction (fillCellIDs runs before the first
+      // fld_applyBoundaryCondition); the stored copy is clamped already when a Jacobi
+      // iteration (which starts with that clamp) consumes it.
+      pred[i] = clampOut ? bc_clamp(p, pp) : pp;
       const uint32_t key = cell_key(g, pp);
       keys[i] = key;
       th.add(key);
@@ -74,17 +57,24 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK 
   th.store(hist0);
 }
 
-// fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor.
-__global__ void __launch_bounds__(128) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
-                                                      const uint2* __restrict__ table, uint32_t n,
-                                                      float* __restrict__ lambda, float* __restrict__ density) {
+// fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor; records
+// the pairs within h for k_fluid_deltap.  One thread per particle: a filter pass over the
+// 27 cells keeps the pairs within h in shared memory, then the SPH terms are summed over
+// that list.
+__global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                                const uint2* __restrict__ table, uint32_t n,
+                                                                float* __restrict__ lambda,
+                                                                float* __restrict__ density, PairList pl) {
+  __shared__ uint32_t s_list[kSmemK * kSweepThreads];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
-  const float4 xi = bc_clamp(p, ld4(pred + i));
+  const float4 xi = ld4(pred + i);  // clamped by the producer (fld_applyBoundaryCondition)
+  SmemList sl(s_list);
+  filter_fluid_neighbours(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, sl);
   float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
-  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
-    const float4 xj = bc_clamp(p, ld4(pred + j));
+  auto body = [&](uint32_t j) {
+    const float4 xj = ld4(pred + j);
     const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
@@ -92,12 +82,13 @@ __global__ void __launch_bounds__(128) k_fluid_lambda(GridK g, FluidK p, const f
       float r;
       const float s = k.gs(r2, r);
       const float gxx = vx * s, gyy = vy * s, gzz = vz * s;
-      sgx += gxx;
-      sgy += gyy;
-      sgz += gzz;
+      sgx += gxx; sgy += gyy; sgz += gzz;
       ssq += gxx * gxx + gyy * gyy + gzz * gzz;
     }
-  });
+  };
+  if (!sl.overflow()) for (uint32_t kk = 0; kk < sl.n; ++kk) body(sl.at(kk));
+  else for_each_fluid_neighbour(g, table, xi, body);
+  publish(pl, i, sl);
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
@@ -105,36 +96,62 @@ __global__ void __launch_bounds__(128) k_fluid_lambda(GridK g, FluidK p, const f
   density[i] = rho;
 }
 
+// Visits the pairs recorded for particle i, one in kQuad per lane (lane q takes entries
+// q, q + kQuad, ...); an overflowed particle searches its 27 cells on lane 0.
+template <class F>
+__device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
+                                           uint32_t i, uint32_t q, float4 xi, F&& f) {
+  const uint32_t c = __ldg(L.count + i);
+  if (c != kListOverflow) {
+    const uint32_t* base = L.idx + i;
+    for (uint32_t kk = q; kk < c; kk += kQuad) f(__ldg(base + (size_t)kk * L.stride));
+  } else if (q == 0) {
+    for_each_fluid_neighbour(g, table, xi, f);
+  }
+}
+
 // fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
-// LAST adds fld_updateVel (fluids.cl:263-273).
+// LAST adds fld_updateVel (fluids.cl:263-273).  kQuad lanes per particle.  Input positions
+// are already clamped by fld_applyBoundaryCondition (done by their producer).
 template <bool LAST>
 __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut,
-                                                      const float4* __restrict__ posS, float4* __restrict__ velS) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = bc_clamp(p, ld4(pred + i));
-  const float li = __ldg(lambda + i);
+                                                      const float4* __restrict__ posS, float4* __restrict__ velS,
+                                                      PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
-    const float4 xj = bc_clamp(p, ld4(pred + j));
-    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      float sc = 0.0f;
-      if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
-      const float f = (li + __ldg(lambda + j) + sc) * s;
-      cx += vx * f;
-      cy += vy * f;
-      cz += vz * f;
-    }
-  });
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    const Sph k(g);
+    xi = ld4(pred + i);  // clamped by the producer
+    const float li = __ldg(lambda + i);
+    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
+      const float4 xj = ld4(pred + j);
+      const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        float sc = 0.0f;
+        if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
+        const float f = (li + __ldg(lambda + j) + sc) * s;
+        cx += vx * f;
+        cy += vy * f;
+        cz += vz * f;
+      }
+    });
+  }
+  cx = quad_sum(cx);
+  cy = quad_sum(cy);
+  cz = quad_sum(cz);
+  if (!active || q != 0) return;
   const float4 out = f4(xi.x + cx * p.invRho0, xi.y + cy * p.invRho0, xi.z + cz * p.invRho0, xi.w);
-  predOut[i] = out;
+  // The next iteration starts with fld_applyBoundaryCondition: store its result directly.
+  // After the last iteration the unclamped position is kept (fld_updateVel, fluids.cl:263).
+  predOut[i] = LAST ? out : bc_clamp(p, out);
   if (LAST) {
     const float4 x0 = ld4(posS + i);
     const float d = p.dt + kFloatEps;
@@ -155,16 +172,21 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
                     -g.maxVel, g.maxVel);
 }
 
-// fld_computeVorticity (fluids.cl:278-324).
-__global__ void __launch_bounds__(128) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
-                                                         const float4* __restrict__ velS, const uint2* __restrict__ table,
-                                                         uint32_t n, float4* __restrict__ vort) {
+// fld_computeVorticity (fluids.cl:278-324); records the pairs within h of the final
+// positions for confinement and XSPH (same two-phase scheme as k_fluid_lambda).
+__global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
+                                                                   const float4* __restrict__ velS,
+                                                                   const uint2* __restrict__ table, uint32_t n,
+                                                                   float4* __restrict__ vort, PairList pl) {
+  __shared__ uint32_t s_list[kSmemK * kSweepThreads];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
   const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  SmemList sl(s_list);
+  filter_fluid_neighbours(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, sl);
   float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
-  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+  auto body = [&](uint32_t j) {
     const float4 xj = ld4(pred + j);
     const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
     const float r2 = vx * vx + vy * vy + vz * vz;
@@ -172,38 +194,46 @@ __global__ void __launch_bounds__(128) k_fluid_vorticity(GridK g, const float4* 
       float r;
       const float s = k.gs(r2, r);
       const float4 dv = ld4(velS + j) - vi;
-      const float4 gr = f4(vx * s, vy * s, vz * s, 0.0f);
-      w = w + cross4(dv, gr);
+      w = w + cross4(dv, f4(vx * s, vy * s, vz * s, 0.0f));
     }
-  });
+  };
+  if (!sl.overflow()) for (uint32_t kk = 0; kk < sl.n; ++kk) body(sl.at(kk));
+  else for_each_fluid_neighbour(g, table, xi, body);
+  publish(pl, i, sl);
   vort[i] = w;
 }
 
-// fld_applyVorticityConfinement (fluids.cl:329-377).
+// fld_applyVorticityConfinement (fluids.cl:329-377), kQuad lanes per particle.
 __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
-                                                       uint32_t n, float4* __restrict__ velS) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i), wi = ld4(vort + i);
+                                                       uint32_t n, float4* __restrict__ velS, PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
-    const float4 xj = ld4(pred + j);
-    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      const float4 wj = ld4(vort + j);
-      const float f = sqrtf(dot4(wj, wj)) * s;
-      ex += vx * f;
-      ey += vy * f;
-      ez += vz * f;
-    }
-  });
-  const float4 nrm = normalize0(f4(ex, ey, ez, 0.0f));
-  const float4 c = cross4(nrm, wi);
+  if (active) {
+    const Sph k(g);
+    const float4 xi = ld4(pred + i);
+    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
+      const float4 xj = ld4(pred + j);
+      const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        const float4 wj = ld4(vort + j);
+        const float f = sqrtf(dot4(wj, wj)) * s;
+        ex += vx * f;
+        ey += vy * f;
+        ez += vz * f;
+      }
+    });
+  }
+  ex = quad_sum(ex);
+  ey = quad_sum(ey);
+  ez = quad_sum(ez);
+  if (!active || q != 0) return;
+  const float4 c = cross4(normalize0(f4(ex, ey, ez, 0.0f)), ld4(vort + i));
   const float s = p.vortCoeff * p.dt;
   float4 v = velS[i];
   v.x += c.x * s;
@@ -213,30 +243,41 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
 }
 
 // fld_applyXsphViscosityCorrection (fluids.cl:383-430) + fld_updatePosition (:444-450),
-// writing the canonical state buffers.
+// writing the canonical state buffers.  kQuad lanes per particle.
 __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, const float4* __restrict__ pred,
                                                           const float4* __restrict__ velS,
                                                           const uint2* __restrict__ table, uint32_t n,
                                                           const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
-                                                          float4* __restrict__ vel, uint32_t* __restrict__ ids) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+                                                          float4* __restrict__ vel, uint32_t* __restrict__ ids,
+                                                          PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float ax = 0.0f, ay = 0.0f, az = 0.0f, aw = 0.0f;
-  for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
-    const float4 xj = ld4(pred + j);
-    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      const float wv = k.w(r2);
-      const float4 vj = ld4(velS + j);
-      ax += (vj.x - vi.x) * wv;
-      ay += (vj.y - vi.y) * wv;
-      az += (vj.z - vi.z) * wv;
-      aw += (vj.w - vi.w) * wv;
-    }
-  });
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f), vi = xi;
+  if (active) {
+    const Sph k(g);
+    xi = ld4(pred + i);
+    vi = ld4(velS + i);
+    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
+      const float4 xj = ld4(pred + j);
+      const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        const float wv = k.w(r2);
+        const float4 vj = ld4(velS + j);
+        ax += (vj.x - vi.x) * wv;
+        ay += (vj.y - vi.y) * wv;
+        az += (vj.z - vi.z) * wv;
+        aw += (vj.w - vi.w) * wv;
+      }
+    });
+  }
+  ax = quad_sum(ax);
+  ay = quad_sum(ay);
+  az = quad_sum(az);
+  aw = quad_sum(aw);
+  if (!active || q != 0) return;
   vel[i] = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
   pos[i] = xi;
   if (ids) ids[i] = __ldg(idsS + i);
@@ -299,6 +340,15 @@ __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const 
   }
 }
 
+// Pair-list statistics: overflowed particles and the longest list (diagnostics).
+__global__ void k_pair_list_stats(const uint32_t* __restrict__ count, uint32_t n, uint32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t c = __ldg(count + i);
+  if (c == kListOverflow) atomicAdd(out, 1u);
+  else atomicMax(out + 1, c);
+}
+
 static int check(const char* what) {
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
@@ -307,27 +357,29 @@ static int check(const char* what) {
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
 int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
-                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, Launcher& L) {
+                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L) {
   L.begin("fld_predict");
-  k_fluid_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0);
+  k_fluid_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
+                                                                  clampOut ? 1 : 0);
   L.end("fld_predict");
   return check("k_fluid_predict");
 }
 
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table, uint32_t n,
-                    float* lambda, float* density, bool last, const float4* posS, float4* velS, Launcher& L) {
+                    float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
+                    Launcher& L) {
   L.begin("fld_lambda");
-  k_fluid_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, table, n, lambda, density);
+  k_fluid_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
   if (rc) return rc;
   if (last) {
     L.begin("fld_deltap_vel");
-    k_fluid_deltap<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS);
+    k_fluid_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS, pl);
     L.end("fld_deltap_vel");
   } else {
     L.begin("fld_deltap");
-    k_fluid_deltap<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS);
+    k_fluid_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS, pl);
     L.end("fld_deltap");
   }
   return check("k_fluid_deltap");
@@ -342,20 +394,21 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
 }
 
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
-               uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, Launcher& L) {
+               uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
+               Launcher& L) {
   if (p.vorticity) {
     L.begin("fld_vorticity");
-    k_fluid_vorticity<<<blocks(n, 128), 128, 0, L.stream>>>(g, pred, velS, table, n, vort);
+    k_fluid_vorticity<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, pred, velS, table, n, vort, pl);
     L.end("fld_vorticity");
     int rc = check("k_fluid_vorticity");
     if (rc) return rc;
     L.begin("fld_confine");
-    k_fluid_confine<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS);
+    k_fluid_confine<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
     L.end("fld_confine");
     rc = check("k_fluid_confine");
     if (rc) return rc;
     L.begin("fld_xsph_final");
-    k_fluid_xsph_final<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS, pos, vel, ids);
+    k_fluid_xsph_final<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS, pos, vel, ids, pl);
     L.end("fld_xsph_final");
     return check("k_fluid_xsph_final");
   }
@@ -374,4 +427,12 @@ int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const floa
   return check("k_fluid_metrics");
 }
 
+}  // namespace rtp
+
+namespace rtp {
+int pair_list_stats(const PairList& pl, uint32_t n, uint32_t* out2, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  k_pair_list_stats<<<(n + 255) / 256, 256, 0, L.stream>>>(pl.count, n, out2);
+  return check("k_pair_list_stats");
+}
 }  // namespace rtp

@@ -153,6 +153,7 @@ struct Handle {
   SortScratch ss{};
   double* mAcc = nullptr;
   uint32_t* mHist = nullptr;
+  PairList pairs{};
   std::vector<void*> allocs;
 
   // Graph executor.
@@ -236,6 +237,10 @@ static int alloc_buffers(Handle* h) {
     RTP_TRY(dalloc(h, &h->lambda, M));
     RTP_TRY(dalloc(h, &h->density, M));
     h->predFinal = h->predA;
+    RTP_TRY(dalloc(h, &h->pairs.idx, (size_t)kPairListK * M));
+    RTP_TRY(dalloc(h, &h->pairs.count, M));
+    h->pairs.stride = (uint32_t)M;
+    h->pairs.K = kPairListK;
   }
   if (h->model == RTP_MODEL_CLOUDS) {
     RTP_TRY(dalloc(h, &h->totCorr, M));
@@ -287,7 +292,7 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   RTP_TRY(launch_sort_clear(plan, h->ss, L));
   // Fluids.cpp:412-417: predict, cell ids, sort {pos, vel, predPos} (+ ids).
-  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, L));
+  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, h->iters > 0, L));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -306,13 +311,14 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   float4* cur = h->predA;
   float4* nxt = h->predB;
   for (uint32_t it = 0; it < h->iters; ++it) {
-    RTP_TRY(fluid_iteration(g, fk, cur, nxt, h->table, n, h->lambda, h->density, it + 1 == h->iters, h->posS, h->velS, L));
+    RTP_TRY(fluid_iteration(g, fk, cur, nxt, h->table, n, h->lambda, h->density, it + 1 == h->iters, h->posS, h->velS,
+                            h->pairs, L));
     std::swap(cur, nxt);
   }
   if (h->iters == 0) RTP_TRY(fluid_update_vel(g, fk, cur, h->posS, n, h->velS, L));
   h->predFinal = cur;
   // Fluids.cpp:444-457.
-  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, L);
+  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L);
 }
 
 static int record_boids_step(Handle* h, Launcher& L) {
@@ -1085,6 +1091,7 @@ int rtp_get_metrics(void* handle, rtp_metrics* out) {
   rtp_fluid_params fp = h->fp;
   if (h->model == RTP_MODEL_CLOUDS) fp.restDensity = h->fp.restDensity;
   RTP_TRY(fluid_metrics(h->g, make_fluidk(h->gc, fp), h->predFinal, h->vel, h->table, n, h->mAcc, h->mHist, L));
+  if (h->pairs.count) RTP_TRY(pair_list_stats(h->pairs, n, h->mHist + 70, L));
   double acc[4];
   uint32_t hist[80];
   RTP_CUDA(cudaMemcpyAsync(acc, h->mAcc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
@@ -1097,6 +1104,8 @@ int rtp_get_metrics(void* handle, rtp_metrics* out) {
   out->kineticEnergy = acc[1];
   out->meanNeighbours = acc[2] / n;
   for (int i = 0; i < 64; ++i) out->neighbourHist[i] = hist[i];
+  out->pairListOverflows = hist[70];
+  out->pairListMax = hist[71];
   return RTP_OK;
   RTP_GUARD_END
 }

@@ -107,3 +107,16 @@ def test_long_run_statistics_16k():
     tv = 0.5 * np.abs(hg / hg.sum() - ho / ho.sum()).sum()
     assert tv < 0.08, tv
     assert gm.meanNeighbours == pytest.approx(om.meanNeighbours, rel=0.05)
+
+
+def test_pair_lists_fit_in_the_dam_break():
+    """The recorded pair lists (64 per particle, 32 per x-plane) never overflow in the
+    131k dam break over 100 steps (an overflow falls back to a 27-cell search: correct
+    but slow, so this guards the performance path)."""
+    sc = scenes.dam_break(lattice=(32, 64, 64))
+    with fluids_model(sc, 3) as m:
+        for _ in range(5):
+            m.update(20)
+            mt = m.metrics()
+            assert mt.pairListOverflows == 0, (mt.pairListOverflows, mt.pairListMax)
+            assert 0 < mt.pairListMax <= 64
