@@ -16,14 +16,23 @@
 //   k_fluid_xsph_final    fld_applyXsphViscosityCorrection + fld_updatePosition, writing
 //                         the state back to the canonical pos/vel buffers
 // The 27-cell searches (fluids.cl:101-123) run in two phases: a filter pass that only
-// compares distances and records the pairs within h in shared memory, then the SPH
-// arithmetic over that compact list, so lanes do not all pay for the arithmetic whenever
-// any lane of the warp has a neighbour.  The list sweeps give 4 lanes to each particle.
+// compares distances and records the pairs within h, then the SPH arithmetic over that
+// compact list, so lanes do not all pay for the arithmetic whenever any lane of the warp
+// has a neighbour.  The list sweeps give 4 lanes to each particle.
 #include "fluids.cuh"
 
 namespace rtp {
 
 __device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
+
+// Operands of one pair loaded ahead of use: a position and a scalar, or two float4.
+struct Pair4 {
+  float4 x;
+  float s;
+};
+struct Pair44 {
+  float4 x, v;
+};
 
 // fld_predictPosition (fluids.cl:62-74) + fillCellIDs (grid.cl:76-86) + digit-0 histogram.
 // Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
@@ -59,22 +68,25 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK 
 
 // fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor; records
 // the pairs within h for k_fluid_deltap.  One thread per particle: a filter pass over the
-// 27 cells keeps the pairs within h in shared memory, then the SPH terms are summed over
-// that list.
-__global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+// 27 cells writes the pairs within h to the device list (kept for k_fluid_deltap), then
+// the SPH terms are summed over that list.
+__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
                                                                 float* __restrict__ density, PairList pl) {
-  __shared__ uint32_t s_list[kSmemK * kSweepThreads];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
-  const float4 xi = ld4(pred + i);  // clamped by the producer (fld_applyBoundaryCondition)
-  SmemList sl(s_list);
-  filter_fluid_neighbours(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, sl);
+  const float4 xi = ld4(pred + i);
+  uint32_t cnt = 0;
+  uint32_t* lst = pl.idx + i;
+  filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
+    ++cnt;
+  });
   float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
-  auto body = [&](uint32_t j) {
-    const float4 xj = ld4(pred + j);
+  auto ldp = [&](uint32_t j) { return ld4(pred + j); };
+  auto body = [&](uint32_t, float4 xj) {
     const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
@@ -82,13 +94,17 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_lambda(GridK g, Flui
       float r;
       const float s = k.gs(r2, r);
       const float gxx = vx * s, gyy = vy * s, gzz = vz * s;
-      sgx += gxx; sgy += gyy; sgz += gzz;
+      sgx += gxx;
+      sgy += gyy;
+      sgz += gzz;
       ssq += gxx * gxx + gyy * gyy + gzz * gzz;
     }
   };
-  if (!sl.overflow()) for (uint32_t kk = 0; kk < sl.n; ++kk) body(sl.at(kk));
-  else for_each_fluid_neighbour(g, table, xi, body);
-  publish(pl, i, sl);
+  if (cnt <= pl.K)
+    visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ldp, body);
+  else
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ldp(j)); });
+  pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
@@ -98,15 +114,15 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_lambda(GridK g, Flui
 
 // Visits the pairs recorded for particle i, one in kQuad per lane (lane q takes entries
 // q, q + kQuad, ...); an overflowed particle searches its 27 cells on lane 0.
-template <class F>
+template <class G, class F>
 __device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
-                                           uint32_t i, uint32_t q, float4 xi, F&& f) {
+                                           uint32_t i, uint32_t q, float4 xi, G&& ld, F&& f) {
   const uint32_t c = __ldg(L.count + i);
   if (c != kListOverflow) {
     const uint32_t* base = L.idx + i;
-    for (uint32_t kk = q; kk < c; kk += kQuad) f(__ldg(base + (size_t)kk * L.stride));
+    visit_list_x4(q, c, kQuad, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
   } else if (q == 0) {
-    for_each_fluid_neighbour(g, table, xi, f);
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
   }
 }
 
@@ -128,8 +144,9 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
     const Sph k(g);
     xi = ld4(pred + i);  // clamped by the producer
     const float li = __ldg(lambda + i);
-    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
-      const float4 xj = ld4(pred + j);
+    auto ld = [&](uint32_t j) { return Pair4{ld4(pred + j), __ldg(lambda + j)}; };
+    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair4 a) {
+      const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
@@ -137,7 +154,7 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
         const float s = k.gs(r2, r);
         float sc = 0.0f;
         if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
-        const float f = (li + __ldg(lambda + j) + sc) * s;
+        const float f = (li + a.s + sc) * s;
         cx += vx * f;
         cy += vy * f;
         cz += vz * f;
@@ -174,32 +191,36 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
 
 // fld_computeVorticity (fluids.cl:278-324); records the pairs within h of the final
 // positions for confinement and XSPH (same two-phase scheme as k_fluid_lambda).
-__global__ void __launch_bounds__(kSweepThreads, 8) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
-                                                                   const float4* __restrict__ velS,
-                                                                   const uint2* __restrict__ table, uint32_t n,
-                                                                   float4* __restrict__ vort, PairList pl) {
-  __shared__ uint32_t s_list[kSmemK * kSweepThreads];
+__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
+                                                                    const float4* __restrict__ velS,
+                                                                    const uint2* __restrict__ table, uint32_t n,
+                                                                    float4* __restrict__ vort, PairList pl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
   const float4 xi = ld4(pred + i), vi = ld4(velS + i);
-  SmemList sl(s_list);
-  filter_fluid_neighbours(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, sl);
+  uint32_t cnt = 0;
+  uint32_t* lst = pl.idx + i;
+  filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
+    ++cnt;
+  });
   float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
-  auto body = [&](uint32_t j) {
-    const float4 xj = ld4(pred + j);
-    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+  auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
+  auto body = [&](uint32_t, Pair44 a) {
+    const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
       float r;
       const float s = k.gs(r2, r);
-      const float4 dv = ld4(velS + j) - vi;
-      w = w + cross4(dv, f4(vx * s, vy * s, vz * s, 0.0f));
+      w = w + cross4(a.v - vi, f4(vx * s, vy * s, vz * s, 0.0f));
     }
   };
-  if (!sl.overflow()) for (uint32_t kk = 0; kk < sl.n; ++kk) body(sl.at(kk));
-  else for_each_fluid_neighbour(g, table, xi, body);
-  publish(pl, i, sl);
+  if (cnt <= pl.K)
+    visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ld, body);
+  else
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ld(j)); });
+  pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
   vort[i] = w;
 }
 
@@ -214,14 +235,15 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
   if (active) {
     const Sph k(g);
     const float4 xi = ld4(pred + i);
-    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
-      const float4 xj = ld4(pred + j);
+    auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(vort + j)}; };
+    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+      const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
         float r;
         const float s = k.gs(r2, r);
-        const float4 wj = ld4(vort + j);
+        const float4 wj = a.v;
         const float f = sqrtf(dot4(wj, wj)) * s;
         ex += vx * f;
         ey += vy * f;
@@ -259,13 +281,14 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
     const Sph k(g);
     xi = ld4(pred + i);
     vi = ld4(velS + i);
-    quad_pairs(g, table, pl, i, q, xi, [&](uint32_t j) {
-      const float4 xj = ld4(pred + j);
+    auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
+    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+      const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
         const float wv = k.w(r2);
-        const float4 vj = ld4(velS + j);
+        const float4 vj = a.v;
         ax += (vj.x - vi.x) * wv;
         ay += (vj.y - vi.y) * wv;
         az += (vj.z - vi.z) * wv;
