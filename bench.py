@@ -14,9 +14,10 @@ Metric: particle-steps/s.
   host memory, update(1), download pos/vel, timed on the host clock.
 * roofline: the dominant kernel's algorithmic bytes / its mean CUDA-event duration
   (captured event nodes inside the same graph replays), against MEASURED_PEAKS.json.
-* cpu_baseline: the CPU oracle (the reference's kernels restated in C++/OpenMP) on
-  the host cores, on a bounded sample of the same workload.
-* --impl reference: the CPU implementation alone (rank 0), same metric and config.
+* cpu_baseline: the reference's own kernels (physics/ocl/kernels/*.cl compiled for the
+  CPU by oracle/ref/build_ref.py, OpenMP over the host cores) on a bounded sample of the
+  same workload; the oracle's restatement when those are not built.
+* --impl reference: that CPU implementation alone (rank 0), same metric and config.
 Under torchrun (N > 1) each rank runs an independent replica of the workload on its
 own GPU (one scene does not shard): barrier + max-over-ranks timing.
 """
@@ -146,39 +147,51 @@ def barrier(ws):
 
 
 def cpu_baseline(steps_sample=None, budget_s=20.0, iters=3):
-    """The oracle on the host cores, on a bounded sample of the workload."""
+    """The CPU implementation (cpu_impl) on the host cores, on a bounded sample of the
+    workload."""
     import oracle
     oracle.set_threads(0)
     cores = oracle.get_threads()
+    step, kind = cpu_impl()
     sc = scenes.dam_break(lattice=(32, 64, 64))
     c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
     st = oracle.new_state(sc["pos"].shape[0], c)
     st["pos"][:] = sc["pos"]
     st["vel"][:] = sc["vel"]
-    oracle.fluids_step(c, sc["fluid_params"], iters, st)  # warm-up
+    step(c, sc["fluid_params"], iters, st)  # warm-up
     n = sc["pos"].shape[0]
     t0 = time.perf_counter()
     k = 0
     while True:
-        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+        step(c, sc["fluid_params"], iters, st)
         k += 1
         el = time.perf_counter() - t0
         if (steps_sample and k >= steps_sample) or (not steps_sample and el >= budget_s):
             break
-    return {"value": n * k / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+    return {"value": n * k / el, "unit": "particle-steps/s", "cores": cores, "kind": kind,
             "sample": "%d steps of the %d-particle dam break (I=%d), %.1f s" % (k, n, iters, el)}
 
 
+def cpu_impl():
+    """The CPU implementation of the step: the reference's own kernels compiled for the CPU
+    (oracle/_ref, kind "reference") when built, else the oracle's restatement (kind "port")."""
+    import oracle
+    if oracle.ref_available():
+        return oracle.ref_fluids_step, "reference"
+    return oracle.fluids_step, "port"
+
+
 def run_reference(args):
-    """The CPU implementation of the step (the oracle: the reference's kernels restated in
-    C++/OpenMP) on all host cores: W warm-up updates, then K timed updates of the same
-    131k workload (stopping early after REF_BUDGET_S, reported in the sample)."""
+    """The CPU implementation of the step on all host cores: W warm-up updates, then K timed
+    updates of the same 131k workload (stopping early after REF_BUDGET_S, reported in the
+    sample)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     import oracle
     oracle.set_threads(0)
     cores = oracle.get_threads()
+    step, kind = cpu_impl()
     iters = 3
     sc = scenes.dam_break(lattice=(32, 64, 64))
     n = sc["pos"].shape[0]
@@ -187,24 +200,27 @@ def run_reference(args):
     st["pos"][:] = sc["pos"]
     st["vel"][:] = sc["vel"]
     for _ in range(args.warmup):
-        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+        step(c, sc["fluid_params"], iters, st)
     t0 = time.perf_counter()
     k = 0
     while k < args.steps:
-        oracle.fluids_step(c, sc["fluid_params"], iters, st)
+        step(c, sc["fluid_params"], iters, st)
         k += 1
         if time.perf_counter() - t0 > REF_BUDGET_S:
             break
     el = time.perf_counter() - t0
     value = n * k / el
-    sample = "%d of %d requested updates of the %d-particle dam break (I=%d) in %.1f s" % (k, args.steps, n, iters, el)
+    what = "the reference's kernels (physics/ocl/kernels) compiled for the CPU" if kind == "reference" else \
+        "the oracle's restatement of the reference's kernels"
+    sample = "%d of %d requested updates of the %d-particle dam break (I=%d) in %.1f s; %s, OpenMP over %d threads" % (
+        k, args.steps, n, iters, el, what, cores)
     line = {"metric": "PBF particle-steps/s @131k (plain, 3 Jacobi iterations)", "value": value,
             "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
             "ms_per_step": 1000.0 * el / k, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0},
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

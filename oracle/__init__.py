@@ -200,3 +200,66 @@ def fluid_metrics(c, fp, pred, vel, table):
     m = abi.Metrics()
     lib().or_fluid_metrics(C.byref(c), C.byref(fp), _p(pred), _p(vel), _p(table), pred.shape[0], C.byref(m))
     return m
+
+
+# ---- the reference's own kernels, compiled for the CPU (oracle/ref/build_ref.py) -------
+_REF = None
+REF_LIB_PATH = os.path.join(_HERE, "_ref", "libref.so")
+
+
+def ref_available():
+    return os.path.exists(REF_LIB_PATH)
+
+
+def ref_lib():
+    """libref.so: the reference's step kernels driven in the reference's update() order."""
+    global _REF
+    if _REF is None:
+        if not ref_available():
+            raise RuntimeError("oracle/_ref/libref.so not built (python oracle/ref/build_ref.py)")
+        L = C.CDLL(REF_LIB_PATH)
+        P = C.c_void_p
+        G = C.POINTER(abi.GridConstants)
+        L.ref_fill_cell_ids.argtypes = [G, P, C.c_uint32, P]
+        L.ref_cell_table.argtypes = [G, P, C.c_uint32, P]
+        L.ref_fluids_step.argtypes = [G, C.POINTER(abi.FluidParams), C.c_uint32, C.c_uint32, P]
+        L.ref_boids_step.argtypes = [G, C.POINTER(abi.BoidsParams), C.c_float, C.c_int, C.c_uint32, P]
+        L.ref_clouds_step.argtypes = [G, C.POINTER(abi.FluidParams), C.POINTER(abi.CloudParams), C.c_uint32,
+                                      C.c_uint32, P]
+        L.ref_clouds_init.argtypes = [G, C.POINTER(abi.CloudParams), C.c_uint32, P]
+        _REF = L
+    return _REF
+
+
+def ref_fill_cell_ids(c, pos):
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    keys = np.empty(pos.shape[0], np.uint32)
+    ref_lib().ref_fill_cell_ids(C.byref(c), _p(pos), pos.shape[0], _p(keys))
+    return keys
+
+
+def ref_cell_table(c, sorted_keys):
+    sorted_keys = np.ascontiguousarray(sorted_keys, dtype=np.uint32)
+    t = np.empty((c.numCells, 2), np.uint32)
+    ref_lib().ref_cell_table(C.byref(c), _p(sorted_keys), sorted_keys.shape[0], _p(t))
+    return t
+
+
+def ref_fluids_step(c, fp, iters, st):
+    s = _state(st)
+    ref_lib().ref_fluids_step(C.byref(c), C.byref(fp), int(iters), st["pos"].shape[0], C.byref(s))
+
+
+def ref_boids_step(c, bp, dt, boundary, st):
+    s = _state(st)
+    ref_lib().ref_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), st["pos"].shape[0], C.byref(s))
+
+
+def ref_clouds_step(c, fp, cp, iters, st):
+    s = _state(st)
+    ref_lib().ref_clouds_step(C.byref(c), C.byref(fp), C.byref(cp), int(iters), st["pos"].shape[0], C.byref(s))
+
+
+def ref_clouds_init(c, cp, st):
+    s = _state(st)
+    ref_lib().ref_clouds_init(C.byref(c), C.byref(cp), st["pos"].shape[0], C.byref(s))

@@ -1,0 +1,89 @@
+"""The oracle against the reference's own step kernels (oracle/_ref/libref.so, built by
+oracle/ref/build_ref.py from physics/ocl/kernels/*.cl) on fresh seeded scenes: every output
+array must match bit for bit.  Skipped when the reference kernels are not built."""
+import numpy as np
+import pytest
+
+import oracle
+from realtimeparticles_gb300 import abi, scenes
+
+pytestmark = pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref/libref.so not built")
+
+
+def _same(a, b):
+    return np.array_equal(a.view(np.uint32) if a.dtype == np.float32 else a,
+                          b.view(np.uint32) if b.dtype == np.float32 else b)
+
+
+def _pair(n, c, model):
+    return oracle.new_state(n, c, model), oracle.new_state(n, c, model)
+
+
+@pytest.mark.parametrize("iters,vort,ap", [(3, 1, 1), (0, 1, 1), (1, 0, 1), (2, 1, 0)])
+def test_fluids_matches_reference(iters, vort, ap):
+    sc = scenes.dam_break(lattice=(8, 16, 12), seed=iters * 10 + vort)
+    fp = sc["fluid_params"]
+    fp.isVorticityConfEnabled = vort
+    fp.isArtPressureEnabled = ap
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    a, b = _pair(sc["pos"].shape[0], c, abi.FLUIDS)
+    for st in (a, b):
+        st["pos"][:] = sc["pos"]
+        st["vel"][:] = sc["vel"]
+    for _ in range(4):
+        oracle.fluids_step(c, fp, iters, a)
+        oracle.ref_fluids_step(c, fp, iters, b)
+        for k in ("pos", "vel", "predPos", "density", "lambda", "id", "cellId", "table"):
+            assert _same(a[k], b[k]), k
+
+
+def test_fluids_reference_geometry():
+    # The reference's own defaults: box 10, grid 30^3, JSON defaults (Fluids.cpp:52-74).
+    n = 4096
+    mp = abi.model_params(n, n, (10.0,) * 3, (30,) * 3)
+    c = oracle.derive_constants(abi.FLUIDS, mp)
+    fp = abi.FluidParams(450.0, 600.0, 0.01, 3, 1, 0.006, 0.001, 4, 1, 0.0004, 0.0001)
+    rng = np.random.default_rng(3)
+    a, b = _pair(n, c, abi.FLUIDS)
+    for st in (a, b):
+        st["pos"][:, :3] = rng.uniform(-5.0, 0.0, (n, 3)).astype(np.float32) if st is a else a["pos"][:, :3]
+    for _ in range(3):
+        oracle.fluids_step(c, fp, 2, a)
+        oracle.ref_fluids_step(c, fp, 2, b)
+        for k in ("pos", "vel", "id", "table"):
+            assert _same(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("boundary,dt", [(abi.CYCLIC_WALL, 0.01), (abi.BOUNCING_WALL, 0.1)])
+def test_boids_matches_reference(boundary, dt):
+    sb = scenes.boids_cloud(n=5000, seed=boundary + 2)
+    c = oracle.derive_constants(abi.BOIDS, sb["model_params"])
+    a, b = _pair(5000, c, abi.BOIDS)
+    for st in (a, b):
+        st["pos"][:] = sb["pos"]
+        st["vel"][:] = sb["vel"]
+    for _ in range(4):
+        oracle.boids_step(c, sb["boids_params"], dt, boundary, a)
+        oracle.ref_boids_step(c, sb["boids_params"], dt, boundary, b)
+        for k in ("pos", "vel", "acc", "id", "table"):
+            assert _same(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("smoothing,iters", [(1, 1), (0, 2)])
+def test_clouds_matches_reference(smoothing, iters):
+    scc = scenes.clouds_cumulus(n=4000, noise=False, seed=smoothing + 3)
+    cp = scc["cloud_params"]
+    cp.isTempSmoothingEnabled = smoothing
+    c = oracle.derive_constants(abi.CLOUDS, scc["model_params"])
+    env = scenes.cloud_env_reference()
+    a, b = _pair(4000, c, abi.CLOUDS)
+    for st in (a, b):
+        st["pos"][:] = scc["pos"]
+        st["vel"][:] = scc["vel"]
+    oracle.clouds_init(c, cp, env, None, a)
+    oracle.ref_clouds_init(c, cp, b)
+    for _ in range(4):
+        oracle.clouds_step(c, scc["fluid_params"], cp, env, None, iters, a)
+        oracle.ref_clouds_step(c, scc["fluid_params"], cp, iters, b)
+        for k in ("pos", "vel", "predPos", "totCorrPos", "temp", "vapor", "cloud", "buoyancy", "id", "cellId"):
+            assert _same(a[k], b[k]), k
