@@ -13,7 +13,9 @@
 //                           totCorrPos) + the mixed boundary; the last adds cld_updateVel
 //   vorticity, confinement, XSPH + cld_updatePosition (wind drift), state written back.
 // Neighbour sweeps follow clouds.cl:326-356: x and z periodic with image shifts of
-// 2W * sign, y walls.
+// 2W * sign, y walls.  As in fluids.cu, the first sweep at given positions records the pairs
+// within h (entry = particle index | image code << 28) for the sweeps that follow at the
+// same positions, which give 4 lanes to each particle.
 #include "clouds.cuh"
 
 namespace rtp {
@@ -40,6 +42,84 @@ __device__ __forceinline__ void for_each_cloud_neighbour(const GridK& g, const u
         for (uint32_t j = j0; j < j1; ++j) f(j, shx, shz);
       }
     }
+  }
+}
+
+// Image code of a recorded pair: bits 0-1 x shift, bits 2-3 z shift (1 = +2W, 2 = -2W).
+__device__ __forceinline__ uint32_t image_code(float shx, float shz) {
+  return (shx > 0.f ? 1u : (shx < 0.f ? 2u : 0u)) | ((shz > 0.f ? 1u : (shz < 0.f ? 2u : 0u)) << 2);
+}
+__device__ __forceinline__ void image_shift(const GridK& g, uint32_t code, float& shx, float& shz) {
+  const uint32_t cx = code & 3u, cz = (code >> 2) & 3u;
+  shx = cx == 1u ? 2.0f * g.W[0] : (cx == 2u ? -2.0f * g.W[0] : 0.0f);
+  shz = cz == 1u ? 2.0f * g.W[2] : (cz == 2u ? -2.0f * g.W[2] : 0.0f);
+}
+
+// Filter pass over the clouds neighbourhood: add(entry) for each candidate within h2, in
+// visiting order, four position loads in flight.
+template <class ADD>
+__device__ __forceinline__ void filter_cloud_neighbours(const GridK& g, const uint2* __restrict__ table,
+                                                        const float4* __restrict__ pos, float4 xi, float h2,
+                                                        ADD&& add) {
+  int cx, cy, cz;
+  cell3(g, xi, cx, cy, cz);
+#pragma unroll 1
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int ux = cx + dx;
+    const int nx = (ux + g.R[0]) % g.R[0];
+    const float shx = ux >= g.R[0] ? 2.0f * g.W[0] : (ux < 0 ? -2.0f * g.W[0] : 0.0f);
+#pragma unroll 1
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int ny = cy + dy;
+      if (ny >= g.R[1] || ny < 0) continue;
+      const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
+#pragma unroll 1
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int uz = cz + dz;
+        const int nz = (uz + g.R[2]) % g.R[2];
+        const float shz = uz >= g.R[2] ? 2.0f * g.W[2] : (uz < 0 ? -2.0f * g.W[2] : 0.0f);
+        const uint32_t code = image_code(shx, shz) << 28;
+        uint32_t j0, j1;
+        cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
+        visit_range_x4(j0, j1, [&](uint32_t j) { return ld4(pos + j); }, [&](uint32_t j, float4 xj) {
+          const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+          if (vx * vx + vy * vy + vz * vz < h2) add(j | code);
+        });
+      }
+    }
+  }
+}
+
+// Records add(entry) into the device list of particle i; returns the count.
+struct ListWriter {
+  const PairList& L;
+  uint32_t* lst;
+  uint32_t n = 0;
+  __device__ __forceinline__ ListWriter(const PairList& l, uint32_t i) : L(l), lst(l.idx + i) {}
+  __device__ __forceinline__ void operator()(uint32_t e) {
+    if (n < L.K) lst[(size_t)n * L.stride] = e;
+    ++n;
+  }
+  __device__ __forceinline__ bool ok() const { return n <= L.K; }
+  __device__ __forceinline__ uint32_t at(uint32_t k) const { return lst[(size_t)k * L.stride]; }
+};
+
+// Visits the recorded pairs of particle i on lane q of its quad (f(j, shx, shz)), or its
+// 27 cells on lane 0 when the list overflowed.
+template <class F>
+__device__ __forceinline__ void quad_cloud_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
+                                                 uint32_t i, uint32_t q, float4 xi, F&& f) {
+  const uint32_t c = __ldg(L.count + i);
+  if (c != kListOverflow) {
+    const uint32_t* base = L.idx + i;
+    for (uint32_t kk = q; kk < c; kk += kQuad) {
+      const uint32_t e = __ldg(base + (size_t)kk * L.stride);
+      float shx, shz;
+      image_shift(g, e >> 28, shx, shz);
+      f(e & 0x0FFFFFFFu, shx, shz);
+    }
+  } else if (q == 0) {
+    for_each_cloud_neighbour(g, table, xi, f);
   }
 }
 
@@ -113,18 +193,21 @@ __global__ void __launch_bounds__(kSortThreads) k_cloud_thermo_predict(
   th.store(hist0);
 }
 
-// cld_computeLaplacianTemp + cld_computeConstraintFactorTemp, on p_pos (Clouds.cpp:253-255).
-__global__ void __launch_bounds__(128) k_cloud_temp_lambda(GridK g, CloudK c, const float4* __restrict__ pos,
-                                                           const float* __restrict__ temp,
-                                                           const uint2* __restrict__ table, uint32_t n,
-                                                           float* __restrict__ lamT) {
+// cld_computeLaplacianTemp + cld_computeConstraintFactorTemp, on p_pos (Clouds.cpp:253-255);
+// records the pairs within h of p_pos for k_cloud_temp_correct.
+__global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g, CloudK c, const float4* __restrict__ pos,
+                                                                         const float* __restrict__ temp,
+                                                                         const uint2* __restrict__ table, uint32_t n,
+                                                                         float* __restrict__ lamT, PairList pl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
   const float4 xi = ld4(pos + i);
   const float ti = __ldg(temp + i);
+  ListWriter lw(pl, i);
+  filter_cloud_neighbours(g, table, pos, xi, k.h2, lw);
   float lap = 0.0f, sg = 0.0f, ssq = 0.0f;
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+  auto body = [&](uint32_t j, float shx, float shz) {
     const float4 xj = ld4(pos + j);
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
@@ -137,48 +220,66 @@ __global__ void __launch_bounds__(128) k_cloud_temp_lambda(GridK g, CloudK c, co
       sg += d;
       ssq += d * d;
     }
-  });
+  };
+  if (lw.ok()) {
+    for (uint32_t kk = 0; kk < lw.n; ++kk) {
+      const uint32_t e = lw.at(kk);
+      float shx, shz;
+      image_shift(g, e >> 28, shx, shz);
+      body(e & 0x0FFFFFFFu, shx, shz);
+    }
+  } else {
+    for_each_cloud_neighbour(g, table, xi, body);
+  }
+  pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   lap /= c.cloudRho0;
   ssq += sg * sg;
   lamT[i] = -lap / (ssq + c.cloudRelax);
 }
 
 // cld_computeConstraintCorrectionTemp + cld_correctTemperature (in place: the sweep reads
-// only lamT and positions of the neighbours).
+// only lamT and positions of the neighbours).  kQuad lanes per particle.
 __global__ void __launch_bounds__(128) k_cloud_temp_correct(GridK g, CloudK c, const float4* __restrict__ pos,
                                                             const float* __restrict__ lamT,
                                                             const uint2* __restrict__ table, uint32_t n,
-                                                            float* __restrict__ temp) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pos + i);
-  const float li = __ldg(lamT + i);
+                                                            float* __restrict__ temp, PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float corr = 0.0f;
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pos + j);
-    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      const float d = r2 * s / (r2 * c.cloudRho0 + kFloatEps);
-      corr += (li + __ldg(lamT + j)) * d;
-    }
-  });
-  temp[i] += 0.3f * corr;
+  if (active) {
+    const Sph k(g);
+    const float4 xi = ld4(pos + i);
+    const float li = __ldg(lamT + i);
+    quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(pos + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        const float d = r2 * s / (r2 * c.cloudRho0 + kFloatEps);
+        corr += (li + __ldg(lamT + j)) * d;
+      }
+    });
+  }
+  corr = quad_sum(corr);
+  if (active && q == 0) temp[i] += 0.3f * corr;
 }
 
-// cld_computeDensity + cld_computeConstraintFactor.
-__global__ void __launch_bounds__(128) k_cloud_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
-                                                      const uint2* __restrict__ table, uint32_t n,
-                                                      float* __restrict__ lambda, float* __restrict__ density) {
+// cld_computeDensity + cld_computeConstraintFactor; records the pairs within h.
+__global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                                    const uint2* __restrict__ table, uint32_t n,
+                                                                    float* __restrict__ lambda,
+                                                                    float* __restrict__ density, PairList pl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
   const float4 xi = ld4(pred + i);
+  ListWriter lw(pl, i);
+  filter_cloud_neighbours(g, table, pred, xi, k.h2, lw);
   float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+  auto body = [&](uint32_t j, float shx, float shz) {
     const float4 xj = ld4(pred + j);
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
@@ -192,7 +293,18 @@ __global__ void __launch_bounds__(128) k_cloud_lambda(GridK g, FluidK p, const f
       sgz += cc;
       ssq += a * a + b * b + cc * cc;
     }
-  });
+  };
+  if (lw.ok()) {
+    for (uint32_t kk = 0; kk < lw.n; ++kk) {
+      const uint32_t e = lw.at(kk);
+      float shx, shz;
+      image_shift(g, e >> 28, shx, shz);
+      body(e & 0x0FFFFFFFu, shx, shz);
+    }
+  } else {
+    for_each_cloud_neighbour(g, table, xi, body);
+  }
+  pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
@@ -201,40 +313,48 @@ __global__ void __launch_bounds__(128) k_cloud_lambda(GridK g, FluidK p, const f
 }
 
 // cld_computeConstraintCorrection, cld_correctPosition x2 and the mixed boundary
-// (Clouds.cpp:577-586); LAST adds cld_updateVel (clouds.cl:958-966).
+// (Clouds.cpp:577-586); LAST adds cld_updateVel (clouds.cl:958-966).  kQuad lanes.
 template <bool LAST>
 __global__ void __launch_bounds__(128) k_cloud_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut, float4* __restrict__ tot,
-                                                      float4* __restrict__ velS) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i);
-  const float li = __ldg(lambda + i);
+                                                      float4* __restrict__ velS, PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pred + j);
-    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      float sc = 0.0f;
-      if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
-      const float f = (li + __ldg(lambda + j) + sc) * s;
-      ax += vx * f;
-      ay += vy * f;
-      az += vz * f;
-    }
-  });
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    const Sph k(g);
+    xi = ld4(pred + i);
+    const float li = __ldg(lambda + i);
+    quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(pred + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        float sc = 0.0f;
+        if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
+        const float f = (li + __ldg(lambda + j) + sc) * s;
+        ax += vx * f;
+        ay += vy * f;
+        az += vz * f;
+      }
+    });
+  }
+  ax = quad_sum(ax);
+  ay = quad_sum(ay);
+  az = quad_sum(az);
+  if (!active || q != 0) return;
   const float4 dp = f4(ax * p.invRho0, ay * p.invRho0, az * p.invRho0, 0.0f);
   predOut[i] = mixed_bc(g, xi + dp);
-  const float4 t = tot[i] + dp;
-  tot[i] = t;
+  const float4 tt = tot[i] + dp;
+  tot[i] = tt;
   if (LAST) {
     const float d = p.dt + kFloatEps;
-    velS[i] = clamp4s(f4(__fdiv_rn(t.x, d), __fdiv_rn(t.y, d), __fdiv_rn(t.z, d), __fdiv_rn(t.w, d)), -g.maxVel,
+    velS[i] = clamp4s(f4(__fdiv_rn(tt.x, d), __fdiv_rn(tt.y, d), __fdiv_rn(tt.z, d), __fdiv_rn(tt.w, d)), -g.maxVel,
                       g.maxVel);
   }
 }
@@ -248,16 +368,20 @@ __global__ void k_cloud_update_vel(GridK g, FluidK p, const float4* __restrict__
   velS[i] = clamp4s(f4(__fdiv_rn(t.x, d), __fdiv_rn(t.y, d), __fdiv_rn(t.z, d), __fdiv_rn(t.w, d)), -g.maxVel, g.maxVel);
 }
 
-// cld_computeVorticity (clouds.cl:727-785).
-__global__ void __launch_bounds__(128) k_cloud_vorticity(GridK g, const float4* __restrict__ pred,
-                                                         const float4* __restrict__ velS, const uint2* __restrict__ table,
-                                                         uint32_t n, float4* __restrict__ vort) {
+// cld_computeVorticity (clouds.cl:727-785); records the pairs within h of the final
+// positions for confinement and XSPH.
+__global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, const float4* __restrict__ pred,
+                                                                       const float4* __restrict__ velS,
+                                                                       const uint2* __restrict__ table, uint32_t n,
+                                                                       float4* __restrict__ vort, PairList pl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
   const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+  ListWriter lw(pl, i);
+  filter_cloud_neighbours(g, table, pred, xi, k.h2, lw);
   float4 w = f4(0.f, 0.f, 0.f, 0.f);
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+  auto body = [&](uint32_t j, float shx, float shz) {
     const float4 xj = ld4(pred + j);
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
@@ -266,70 +390,96 @@ __global__ void __launch_bounds__(128) k_cloud_vorticity(GridK g, const float4* 
       const float s = k.gs(r2, r);
       w = w + cross4(ld4(velS + j) - vi, f4(vx * s, vy * s, vz * s, 0.0f));
     }
-  });
+  };
+  if (lw.ok()) {
+    for (uint32_t kk = 0; kk < lw.n; ++kk) {
+      const uint32_t e = lw.at(kk);
+      float shx, shz;
+      image_shift(g, e >> 28, shx, shz);
+      body(e & 0x0FFFFFFFu, shx, shz);
+    }
+  } else {
+    for_each_cloud_neighbour(g, table, xi, body);
+  }
+  pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   vort[i] = w;
 }
 
-// cld_applyVorticityConfinement (clouds.cl:790-850).
+// cld_applyVorticityConfinement (clouds.cl:790-850).  kQuad lanes per particle.
 __global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
-                                                       uint32_t n, float4* __restrict__ velS) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i), wi = ld4(vort + i);
+                                                       uint32_t n, float4* __restrict__ velS, PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
   float ex = 0.f, ey = 0.f, ez = 0.f;
-  for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pred + j);
-    const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      const float4 wj = ld4(vort + j);
-      const float f = sqrtf(dot4(wj, wj)) * s;
-      ex += vx * f;
-      ey += vy * f;
-      ez += vz * f;
-    }
-  });
-  const float4 c = cross4(normalize0(f4(ex, ey, ez, 0.0f)), wi);
-  const float s = p.vortCoeff * p.dt;
-  float4 v = velS[i];
-  v.x += c.x * s;
-  v.y += c.y * s;
-  v.z += c.z * s;
-  velS[i] = v;
-}
-
-// cld_applyXsphViscosityCorrection (clouds.cl:856-915) + cld_updatePosition (:942-953);
-// writes the canonical state (pos, vel, temp, vapor, cloud, buoyancy, ids).
-__global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
-                                                     const float4* __restrict__ velS, const uint2* __restrict__ table,
-                                                     uint32_t n, CloudState s) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
-  float4 out = vi;
-  if (p.vorticity) {
-    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
-    for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+  if (active) {
+    const Sph k(g);
+    const float4 xi = ld4(pred + i);
+    quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
       const float4 xj = ld4(pred + j);
       const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
-        const float wv = k.w(r2);
-        const float4 vj = ld4(velS + j);
-        ax += (vj.x - vi.x) * wv;
-        ay += (vj.y - vi.y) * wv;
-        az += (vj.z - vi.z) * wv;
-        aw += (vj.w - vi.w) * wv;
+        float r;
+        const float s = k.gs(r2, r);
+        const float4 wj = ld4(vort + j);
+        const float f = sqrtf(dot4(wj, wj)) * s;
+        ex += vx * f;
+        ey += vy * f;
+        ez += vz * f;
       }
     });
-    out = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
   }
-  s.vel[i] = out;
+  ex = quad_sum(ex);
+  ey = quad_sum(ey);
+  ez = quad_sum(ez);
+  if (!active || q != 0) return;
+  const float4 cr = cross4(normalize0(f4(ex, ey, ez, 0.0f)), ld4(vort + i));
+  const float s = p.vortCoeff * p.dt;
+  float4 v = velS[i];
+  v.x += cr.x * s;
+  v.y += cr.y * s;
+  v.z += cr.z * s;
+  velS[i] = v;
+}
+
+// cld_applyXsphViscosityCorrection (clouds.cl:856-915) + cld_updatePosition (:942-953);
+// writes the canonical state (pos, vel, temp, vapor, cloud, buoyancy, ids).  kQuad lanes.
+__global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
+                                                     const float4* __restrict__ velS, const uint2* __restrict__ table,
+                                                     uint32_t n, CloudState s, PairList pl) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
+  float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f), vi = xi;
+  if (active) {
+    xi = ld4(pred + i);
+    vi = ld4(velS + i);
+    if (p.vorticity) {
+      const Sph k(g);
+      quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
+        const float4 xj = ld4(pred + j);
+        const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+        const float r2 = vx * vx + vy * vy + vz * vz;
+        if (r2 < k.h2) {
+          const float wv = k.w(r2);
+          const float4 vj = ld4(velS + j);
+          ax += (vj.x - vi.x) * wv;
+          ay += (vj.y - vi.y) * wv;
+          az += (vj.z - vi.z) * wv;
+          aw += (vj.w - vi.w) * wv;
+        }
+      });
+    }
+  }
+  ax = quad_sum(ax);
+  ay = quad_sum(ay);
+  az = quad_sum(az);
+  aw = quad_sum(aw);
+  if (!active || q != 0) return;
+  s.vel[i] = p.vorticity ? f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw) : vi;
   float4 x = xi;
   const float alt = xi.y + g.W[1];
   x.x += (1.0f - expf(-alt * c.windX)) * c.wind * c.dt * (float)(c.dim - 2u);
@@ -371,30 +521,33 @@ int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const floa
 }
 
 int cloud_temperature(const GridK& g, const CloudK& c, const float4* posS, float* tempS, float* lamT, const uint2* table,
-                      uint32_t n, Launcher& L) {
+                      uint32_t n, const PairList& pl, Launcher& L) {
   L.begin("cld_temp_lambda");
-  k_cloud_temp_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, c, posS, tempS, table, n, lamT);
+  k_cloud_temp_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, c, posS, tempS, table, n, lamT, pl);
   L.end("cld_temp_lambda");
   int rc = check("k_cloud_temp_lambda");
   if (rc) return rc;
   L.begin("cld_temp_correct");
-  k_cloud_temp_correct<<<blocks(n, 128), 128, 0, L.stream>>>(g, c, posS, lamT, table, n, tempS);
+  k_cloud_temp_correct<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, c, posS, lamT, table, n, tempS, pl);
   L.end("cld_temp_correct");
   return check("k_cloud_temp_correct");
 }
 
 int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, float4* totS,
-                    const uint2* table, uint32_t n, float* lambda, float* density, bool last, float4* velS, Launcher& L) {
+                    const uint2* table, uint32_t n, float* lambda, float* density, bool last, float4* velS,
+                    const PairList& pl, Launcher& L) {
   L.begin("cld_lambda");
-  k_cloud_lambda<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, table, n, lambda, density);
+  k_cloud_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl);
   L.end("cld_lambda");
   int rc = check("k_cloud_lambda");
   if (rc) return rc;
   L.begin(last ? "cld_deltap_vel" : "cld_deltap");
   if (last)
-    k_cloud_deltap<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS);
+    k_cloud_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS,
+                                                                        pl);
   else
-    k_cloud_deltap<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS);
+    k_cloud_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS,
+                                                                         velS, pl);
   L.end(last ? "cld_deltap_vel" : "cld_deltap");
   return check("k_cloud_deltap");
 }
@@ -407,21 +560,21 @@ int cloud_update_vel(const GridK& g, const FluidK& p, const float4* totS, uint32
 }
 
 int cloud_post(const GridK& g, const FluidK& p, const CloudK& c, const float4* pred, float4* velS, float4* vort,
-               const uint2* table, uint32_t n, const CloudState& s, Launcher& L) {
+               const uint2* table, uint32_t n, const CloudState& s, const PairList& pl, Launcher& L) {
   if (p.vorticity) {
     L.begin("cld_vorticity");
-    k_cloud_vorticity<<<blocks(n, 128), 128, 0, L.stream>>>(g, pred, velS, table, n, vort);
+    k_cloud_vorticity<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, pred, velS, table, n, vort, pl);
     L.end("cld_vorticity");
     int rc = check("k_cloud_vorticity");
     if (rc) return rc;
     L.begin("cld_confine");
-    k_cloud_confine<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS);
+    k_cloud_confine<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
     L.end("cld_confine");
     rc = check("k_cloud_confine");
     if (rc) return rc;
   }
   L.begin("cld_xsph_final");
-  k_cloud_final<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, c, pred, velS, table, n, s);
+  k_cloud_final<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, c, pred, velS, table, n, s, pl);
   L.end("cld_xsph_final");
   return check("k_cloud_final");
 }

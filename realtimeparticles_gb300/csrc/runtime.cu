@@ -415,13 +415,13 @@ int record_clouds_step(Handle* h, Launcher& L) {
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
   RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
   // Clouds.cpp:554-567.
-  if (ck.smoothing) RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, L));
+  if (ck.smoothing) RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, h->pairs, L));
   // Clouds.cpp:570-590.
   float4* cur = h->predA;
   float4* nxt = h->predB;
   for (uint32_t it = 0; it < h->iters; ++it) {
     RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == h->iters,
-                            h->velS, L));
+                            h->velS, h->pairs, L));
     std::swap(cur, nxt);
   }
   if (h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
@@ -440,7 +440,7 @@ int record_clouds_step(Handle* h, Launcher& L) {
   s.buoyS = h->buoyS;
   s.ids = h->ids;
   s.idsS = h->idsS;
-  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, L);
+  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, h->pairs, L);
 }
 
 // ---- Model::reset: reference defaults + the case's initial particles ------------------
@@ -722,8 +722,8 @@ int rtp_create(int model, const rtp_model_params* params, void** out_handle) {
   if (!params || !out_handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: null argument");
   *out_handle = nullptr;
   if (model < RTP_MODEL_BOIDS || model > RTP_MODEL_CLOUDS) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: unknown model");
-  if (params->maxNbParticles == 0 || params->maxNbParticles > 0x7FFFFFFFull)
-    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: maxNbParticles must be in [1, 2^31)");
+  if (params->maxNbParticles == 0 || params->maxNbParticles > (1ull << 28))
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: maxNbParticles must be in [1, 2^28]");
   if (params->currNbParticles > params->maxNbParticles)
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: currNbParticles > maxNbParticles");
   if (params->dimension != 3 && params->dimension != 2)
