@@ -17,6 +17,13 @@ Metric: particle-steps/s.
 * cpu_baseline: the reference's own kernels (physics/ocl/kernels/*.cl compiled for the
   CPU by oracle/ref/build_ref.py, OpenMP over the host cores) on a bounded sample of the
   same workload; the oracle's restatement when those are not built.
+* warm_start (default workload): the learned warm start measured against the plain solver
+  at equal solver-output density error.  A network is trained on the GPU by the library's
+  kernels (2.1M samples from 8 seeded plain 8-iteration runs of the same lattice, seeds 1-8),
+  then the plain solver (1-24 iterations) and the warm start (+0-3 plain iterations) each
+  run K device-timed steps of the seed-0 scene with the solver statistics on; the speed-up
+  at equal error compares each warm-started configuration with the plain curve
+  interpolated (log-log) at its error.
 * --impl reference: that CPU implementation alone (rank 0), same metric and config.
 Under torchrun (N > 1) each rank runs an independent replica of the workload on its
 own GPU (one scene does not shard): barrier + max-over-ranks timing.
@@ -277,6 +284,82 @@ def run_reference(args):
     return 0
 
 
+PLAIN_ITERS = (1, 2, 3, 4, 6, 8, 12, 16, 24)
+WARM_EXTRA = (0, 1, 2, 3)
+
+
+def _timed_config(lattice, iters, net, extra, tol, steps, warmup):
+    """(ms per step, mean solver-output density error, reruns) of one configuration."""
+    from realtimeparticles_gb300 import model
+    sc = scenes.dam_break(lattice=lattice)
+    with model.Fluids(sc["model_params"]) as m:
+        m.setFluidParams(sc["fluid_params"])
+        m.setJacobiIterations(iters)
+        m.upload(abi.BUF_POS, sc["pos"])
+        m.upload(abi.BUF_VEL, sc["vel"])
+        m.enableSolverStats(True)
+        if net is not None:
+            m.setWarmStart(net, extra_iterations=extra, guard_tolerance=tol)
+        m.update(warmup)
+        m.resetSolverStats()
+        ms = m.timeSteps(steps, flush_bytes=L2_FLUSH_BYTES) / steps
+        st = m.solverStats()
+    return ms, st["mean"], st["reruns"]
+
+
+def _plain_at(curve, err):
+    """Throughput of the plain solver at mean error `err`, log-log interpolated on the
+    measured curve (list of (error, particle-steps/s) with error decreasing); None outside it."""
+    pts = sorted(curve, key=lambda p: -p[0])
+    for (e0, v0), (e1, v1) in zip(pts, pts[1:]):
+        if e1 <= err <= e0 and e0 > 0 and e1 > 0:
+            t = (np.log(err) - np.log(e0)) / (np.log(e1) - np.log(e0)) if e0 != e1 else 0.0
+            return float(np.exp(np.log(v0) + t * (np.log(v1) - np.log(v0))))
+    return None
+
+
+def warm_start_study(w, steps, warmup):
+    from realtimeparticles_gb300 import warmstart
+    lattice = w["lattice"]
+    n = int(np.prod(lattice))
+    t0 = time.perf_counter()
+    feats, targets = warmstart.generate_samples(seeds=range(1, 9), lattice=lattice, steps=400, record_every=25,
+                                                stride=8, reference_iterations=8)
+    t1 = time.perf_counter()
+    net, hist = warmstart.train(feats, targets, epochs=16, batch=8192, learning_rate=2e-3, seed=0)
+    t2 = time.perf_counter()
+    out = {"training": {"samples": int(feats.shape[0]), "reference_iterations": 8, "runs": 8,
+                        "epochs": len(hist), "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+                        "sample_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2)}}
+    del feats, targets
+    plain, curve = [], []
+    for it in PLAIN_ITERS:
+        ms, err, _ = _timed_config(lattice, it, None, 0, 0.0, steps, warmup)
+        v = n / (ms / 1000.0)
+        plain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err})
+        curve.append((err, v))
+    learned = []
+    for e in WARM_EXTRA:
+        ms, err, rr = _timed_config(lattice, 8, net, e, 0.0, steps, warmup)
+        v = n / (ms / 1000.0)
+        ref = _plain_at(curve, err)
+        learned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
+                        "mean_density_error": err, "plain_at_equal_error": ref,
+                        "speedup_at_equal_error": (v / ref) if ref else None})
+    # The guard: tolerance = the plain 3-iteration error; reruns use 3 iterations.
+    tol = next(p["mean_density_error"] for p in plain if p["iterations"] == 3)
+    ms, err, rr = _timed_config(lattice, 3, net, 1, tol, steps, warmup)
+    guarded = {"extra_iterations": 1, "guard_tolerance": tol, "plain_iterations": 3,
+               "particle_steps_per_s": n / (ms / 1000.0), "mean_density_error": err, "reruns": rr,
+               "steps": steps}
+    speedups = [x["speedup_at_equal_error"] for x in learned if x["speedup_at_equal_error"]]
+    out.update(plain=plain, learned=learned, guarded=guarded,
+               best_speedup_at_equal_error=max(speedups) if speedups else None,
+               note="speed-up < 1 or null: the warm start does not reach the plain solver's "
+                    "throughput at its own error on this workload")
+    return out
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -375,6 +458,8 @@ def run_ours(args):
                                   "pair_list_overflows": metrics.pairListOverflows}
         if cb:
             out["cpu_baseline"] = cb
+        if w["kind"] == "fluids" and args.workload == WORKLOAD and not args.no_warm_start:
+            out["warm_start"] = warm_start_study(w, args.steps, max(3, args.warmup))
         print(json.dumps(out))
     if ws > 1:
         import torch.distributed as dist
@@ -390,6 +475,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-warm-start", action="store_true", help="skip the learned warm-start study")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.warmup < 3:

@@ -178,7 +178,10 @@ typedef enum rtp_buffer {
   RTP_BUF_CELL_ID = 10,   /* uint   p_cellID: sorted cell keys of the last step */
   RTP_BUF_CELL_TABLE = 11,/* uint2  c_startEndPartID in the reference's inclusive format */
   RTP_BUF_VORTICITY = 12, /* float4 p_vort */
-  RTP_BUF_ACC = 13        /* float4 p_acc (boids) */
+  RTP_BUF_ACC = 13,       /* float4 p_acc (boids) */
+  RTP_BUF_LAMBDA_TOTAL = 14 /* float: lambda summed over the iterations of the last warm-started
+                               or sample-recording step (fluids; the warm start's multiplier
+                               plus the extra iterations' lambdas).  Cleared by uploading POS. */
 } rtp_buffer;
 
 /* Per-kernel device time, collected when profiling is enabled (the reference's
@@ -197,6 +200,7 @@ typedef struct rtp_metrics {
   double kineticEnergy;     /* 0.5 * sum |v|^2 (unit mass) */
   double meanNeighbours;    /* mean neighbours within the effect radius */
   uint32_t neighbourHist[64];
+  double meanCompression;     /* mean max(rho_i / rho0 - 1, 0): compression only */
   uint32_t pairListOverflows; /* particles whose last recorded pair list overflowed */
   uint32_t pairListMax;       /* longest recorded pair list of the last step */
 } rtp_metrics;
@@ -301,6 +305,100 @@ int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_k
 #define RTP_NOALLOC_SORT_SCRATCH_BYTES 5251072u
 int rtp_radix_sort_noalloc(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint32_t* d_keys_out,
                            uint32_t* d_perm_out, void* stream);
+
+/* ---- Learned warm start of the fluids' constraint solve (new: no counterpart in the
+ * reference, whose Jacobi loop starts every substep from a zero correction,
+ * physics/ocl/Fluids.cpp:427-442).
+ *
+ * A per-particle MLP, RTP_MLP_IN features -> 64 GELU -> 64 GELU -> RTP_MLP_OUT, evaluated
+ * with BF16 tensor-core MMAs (FP32 accumulate) inside the first density/lambda sweep of each
+ * substep, at the predicted positions.  Features, in order, with h the effect radius,
+ * rho0 the rest density, dt the time step and sums over neighbours j != i within h:
+ *   0 neighbour count             1 rho_i / rho0 - 1
+ *   2-4 h/rho0 * sum grad W_ij    5 (h/rho0)^2 * sum |grad W_ij|^2
+ *   6 dt/rho0 * sum (v_j - v_i) . grad W_ij   (v = the step's input velocities)
+ *   7-9 wall proximity per axis: clamp(2 - (x - lo)/h, 0, 2) - clamp(2 - (hi - x)/h, 0, 2)
+ *       with lo, hi the fld_applyBoundaryCondition bounds
+ *   10 lambda_i of the plain first iteration
+ *   11 |v_i| dt / h
+ * Outputs: lambda_i, to use in place of the first iteration's lambda (trained on the sum of
+ * lambda over the reference iterations), and a residual displacement r_i (3).  The first
+ * correction is x_i += dp_i(lambda) + r_i, then `extraIterations` plain Jacobi iterations run.
+ * Guard: the solver output's mean |rho_i/rho0 - 1| is measured in the vorticity sweep; a
+ * step above `guardTolerance` reruns from the same predicted positions with the plain
+ * iteration count (rtp_set_jacobi_iterations) before vorticity confinement and XSPH. */
+#define RTP_MLP_IN 12
+#define RTP_MLP_HIDDEN 64
+#define RTP_MLP_OUT 4
+typedef struct rtp_mlp {
+  float inMean[RTP_MLP_IN]; /* network input = (feature - inMean) * inScale */
+  float inScale[RTP_MLP_IN];
+  float w1[RTP_MLP_HIDDEN][RTP_MLP_IN];
+  float b1[RTP_MLP_HIDDEN];
+  float w2[RTP_MLP_HIDDEN][RTP_MLP_HIDDEN];
+  float b2[RTP_MLP_HIDDEN];
+  float w3[RTP_MLP_OUT][RTP_MLP_HIDDEN];
+  float b3[RTP_MLP_OUT];
+  float outScale[RTP_MLP_OUT]; /* output o = network value o * outScale[o] */
+} rtp_mlp;
+
+typedef struct rtp_warm_start_config {
+  uint32_t enabled;         /* 0: plain solver */
+  uint32_t extraIterations; /* plain Jacobi iterations after the warm-started one */
+  float guardTolerance;     /* mean |rho/rho0 - 1| that triggers a plain rerun; <= 0: no guard */
+  uint32_t reserved;
+} rtp_warm_start_config;
+
+typedef struct rtp_solver_stats {
+  uint64_t steps;            /* warm-started steps since the last reset */
+  uint64_t reruns;           /* steps the guard sent back to the plain solver */
+  double sumDensityError;    /* sum over steps of the accepted solver output's mean |rho/rho0 - 1| */
+  double maxDensityError;    /* largest of those means */
+  double sumFirstError;      /* sum over steps of the warm-started output's mean (before reruns) */
+} rtp_solver_stats;
+
+/* Installs (or with cfg->enabled == 0 removes) the warm start on a fluids handle. */
+int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_config* cfg);
+/* Also measure the plain solver's output error per step (warm-started steps always do). */
+int rtp_enable_solver_stats(void* handle, int enable);
+int rtp_get_solver_stats(void* handle, rtp_solver_stats* out);
+int rtp_reset_solver_stats(void* handle);
+
+/* Training data: runs one plain step with `referenceIterations` Jacobi iterations (the
+ * simulation advances) and writes one sample for each cell-sorted particle index
+ * phase, phase + stride, ... < n: its RTP_MLP_IN raw features (as above) into
+ * d_features[k][RTP_MLP_IN] and its targets into d_targets[k][RTP_MLP_OUT]: the sum of
+ * lambda over the iterations, then x_final - x_0 - dp(lambda sum) evaluated at x_0 (3).
+ * At most `capacity` samples are written; *written receives the count. */
+int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, uint32_t stride, uint32_t phase,
+                                  float* d_features, float* d_targets, uint64_t capacity, uint64_t* written);
+
+typedef struct rtp_train_config {
+  uint32_t epochs;
+  uint32_t batch;          /* samples per Adam step */
+  float learningRate;      /* cosine-decayed to learningRate * finalLrFraction */
+  float finalLrFraction;
+  float beta1, beta2, eps; /* Adam */
+  float weightDecay;       /* decoupled (AdamW) */
+  float lossWeights[RTP_MLP_OUT];
+  uint64_t seed;           /* initialisation and shuffling */
+} rtp_train_config;
+
+/* Trains `net` on n samples in device memory: sets the input and output normalisation from
+ * the data (mean / standard deviation of each feature, root mean square of each target),
+ * initialises the weights from cfg->seed, then runs cfg->epochs of shuffled minibatch AdamW
+ * with the library's BF16 tensor-core forward / backward kernels.  loss_history (host,
+ * cfg->epochs floats, may be NULL) receives each epoch's mean loss. */
+int rtp_train_warm_start(const float* d_features, const float* d_targets, uint64_t n, const rtp_train_config* cfg,
+                         rtp_mlp* net, float* loss_history, void* stream);
+/* Loss and gradient of `net` over n samples (forward and backward kernels of the trainer):
+ *   loss = 1/n sum_s sum_o lossWeights[o] * (y_so - t_so / outScale[o])^2,
+ * y the network value.  grad gets d loss / d (w1, b1, w2, b2, w3, b3); its normalisation
+ * fields are zero. */
+int rtp_mlp_loss_grad(const rtp_mlp* net, const float* lossWeights, const float* d_features, const float* d_targets,
+                      uint64_t n, double* loss, rtp_mlp* grad, void* stream);
+/* Inference kernel of the warm start on stand-alone features: d_out[s][o] = y_so * outScale[o]. */
+int rtp_mlp_forward(const rtp_mlp* net, const float* d_features, uint64_t n, float* d_out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -55,6 +55,15 @@ def lib():
                                         C.c_uint32, P]
         L.or_fluid_metrics.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P, P,
                                        C.c_uint32, C.POINTER(abi.Metrics)]
+        L.or_ws_features.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P, P,
+                                     C.c_uint32, P]
+        L.or_mlp_forward.argtypes = [C.POINTER(abi.Mlp), P, C.c_uint64, C.c_int, P]
+        L.or_mlp_loss_grad.argtypes = [C.POINTER(abi.Mlp), P, P, P, C.c_uint64, C.c_int, C.POINTER(C.c_double), P]
+        L.or_ws_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.POINTER(abi.Mlp),
+                                 C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, P, P, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int)]
+        L.or_ws_record_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.c_uint32,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, C.POINTER(C.c_uint32)]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_threads.restype = C.c_int
         _LIB = L
@@ -200,6 +209,72 @@ def fluid_metrics(c, fp, pred, vel, table):
     m = abi.Metrics()
     lib().or_fluid_metrics(C.byref(c), C.byref(fp), _p(pred), _p(vel), _p(table), pred.shape[0], C.byref(m))
     return m
+
+
+# ---- learned warm start (restates the GPU method) ---------------------------------------
+MLP_GRAD_SHAPES = (("w1", (64, 12)), ("b1", (64,)), ("w2", (64, 64)), ("b2", (64,)), ("w3", (4, 64)), ("b3", (4,)))
+
+
+def ws_features(c, fp, x0, vel, table):
+    x0 = np.ascontiguousarray(x0, dtype=np.float32)
+    vel = np.ascontiguousarray(vel, dtype=np.float32)
+    table = np.ascontiguousarray(table, dtype=np.uint32)
+    n = x0.shape[0]
+    out = np.empty((n, 12), np.float32)
+    lib().or_ws_features(C.byref(c), C.byref(fp), _p(x0), _p(vel), _p(table), n, _p(out))
+    return out
+
+
+def mlp_forward(net, feats, emulate=True):
+    feats = np.ascontiguousarray(feats, dtype=np.float32)
+    out = np.empty((feats.shape[0], 4), np.float32)
+    lib().or_mlp_forward(C.byref(net), _p(feats), feats.shape[0], 1 if emulate else 0, _p(out))
+    return out
+
+
+def mlp_loss_grad(net, loss_weights, feats, targets, emulate=True):
+    """(loss, {name: gradient array}) in double precision."""
+    feats = np.ascontiguousarray(feats, dtype=np.float32)
+    targets = np.ascontiguousarray(targets, dtype=np.float32)
+    lw = np.ascontiguousarray(loss_weights, dtype=np.float32)
+    g = np.empty(5252, np.float64)
+    loss = C.c_double()
+    lib().or_mlp_loss_grad(C.byref(net), _p(lw), _p(feats), _p(targets), feats.shape[0], 1 if emulate else 0,
+                           C.byref(loss), _p(g))
+    out, o = {}, 0
+    for name, shape in MLP_GRAD_SHAPES:
+        size = int(np.prod(shape))
+        out[name] = g[o:o + size].reshape(shape)
+        o += size
+    return loss.value, out
+
+
+def ws_step(c, fp, net, extra_iters, guard_tol, plain_iters, st, lam_tot):
+    """One warm-started step in place; returns (solver-output mean error, rerun flag)."""
+    n = st["pos"].shape[0]
+    s = _state(st)
+    err = C.c_double()
+    rr = C.c_int()
+    rc = lib().or_ws_step(C.byref(c), C.byref(fp), C.byref(net), int(extra_iters), float(guard_tol),
+                          int(plain_iters), n, C.byref(s), _p(lam_tot), C.byref(err), C.byref(rr))
+    if rc != 0:
+        raise ValueError("or_ws_step failed: %d" % rc)
+    return err.value, bool(rr.value)
+
+
+def ws_record_step(c, fp, iters, stride, phase, st, lam_tot):
+    """One plain step in place that also returns (features, targets) of the sampled particles."""
+    n = st["pos"].shape[0]
+    s = _state(st)
+    cap = max(0, (n - phase + stride - 1) // stride)
+    feats = np.zeros((max(cap, 1), 12), np.float32)
+    tg = np.zeros((max(cap, 1), 4), np.float32)
+    cnt = C.c_uint32()
+    rc = lib().or_ws_record_step(C.byref(c), C.byref(fp), int(iters), int(stride), int(phase), n, C.byref(s),
+                                 _p(lam_tot), _p(feats), _p(tg), C.byref(cnt))
+    if rc != 0:
+        raise ValueError("or_ws_record_step failed: %d" % rc)
+    return feats[:cnt.value], tg[:cnt.value]
 
 
 # ---- the reference's own kernels, compiled for the CPU (oracle/ref/build_ref.py) -------

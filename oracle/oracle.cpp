@@ -369,54 +369,77 @@ void or_fld_correction(const rtp_grid_constants* c, const rtp_fluid_params* p, c
   }
 }
 
-int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters,
-                   uint32_t n, or_state* s) {
-  if (!c || !p || !s || !s->pos || !s->vel || !s->predPos) return RTP_ERR_INVALID_ARGUMENT;
-  const Grid g(c);
-  const Sph k(c);
+}  // extern "C"
+
+namespace {
+
+// Fluids.cpp:412-424: fld_predictPosition, fillCellIDs(predPos), sort of {pos, col, vel,
+// predPos} (col is render-only) + ids + `extra` (one float per particle), cell table.
+void fluid_presort(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t n, or_state* s,
+                   std::vector<uint32_t>& table, float* extra) {
   const float dt = p->timeStep;
   float* pos = s->pos;
   float* vel = s->vel;
   float* pred = s->predPos;
-
-  // fld_predictPosition, fluids.cl:62-74 (Fluids.cpp:412).
+  // fld_predictPosition, fluids.cl:62-74.
   OR_PARALLEL_FOR
   for (int64_t i = 0; i < (int64_t)n; ++i) {
     const f4 gdt = mk(0.0f * dt, -ABS_GRAVITY_ACC_Y * dt, 0.0f * dt, 0.0f * dt);
     const f4 newVel = ld4(vel, i) + gdt;
     st4(pred, i, ld4(pos, i) + newVel * dt);
   }
-  // fillCellIDs(predPos) (Fluids.cpp:415), sort of {pos, col, vel, predPos} (:417; col is
-  // render-only), cell table (:419-424).
   std::vector<uint32_t> keys(n), perm;
   or_fill_cell_ids(c, pred, n, keys.data());
-  std::vector<uint32_t> table(2 * (size_t)c->numCells);
+  table.assign(2 * (size_t)c->numCells, 0u);
   sort_and_table(c, n, keys, perm, s->cellId, table.data());
   gather4(pos, perm, n);
   gather4(vel, perm, n);
   gather4(pred, perm, n);
   gather1(s->id, perm, n);
+  gather1(extra, perm, n);
   if (s->table) std::memcpy(s->table, table.data(), sizeof(uint32_t) * table.size());
+}
 
-  std::vector<float> density(n), lambda(n), corr(4 * (size_t)n);
-  const f4 lo = mk(-g.W[0] + 0.01f, -g.W[1] + 0.01f, -g.W[2] + 0.01f, 0.0f);
-  const f4 hi = mk(g.W[0] - 0.1f, g.W[1] - 0.1f, g.W[2] - 0.1f, 0.0f);
-  // Jacobi loop, Fluids.cpp:427-439.
+struct Bounds {
+  f4 lo, hi;
+  explicit Bounds(const Grid& g)
+      : lo(mk(-g.W[0] + 0.01f, -g.W[1] + 0.01f, -g.W[2] + 0.01f, 0.0f)),
+        hi(mk(g.W[0] - 0.1f, g.W[1] - 0.1f, g.W[2] - 0.1f, 0.0f)) {}
+};
+
+// Jacobi loop, Fluids.cpp:427-439 (`iters` iterations on pred).  With lamTot the lambdas
+// of the iterations are added to it.
+void fluid_jacobi(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters, float* pred,
+                  const uint32_t* table, uint32_t n, std::vector<float>& density, std::vector<float>& lambda,
+                  float* lamTot) {
+  const Grid g(c);
+  const Bounds b(g);
+  std::vector<float> corr(4 * (size_t)n);
   for (uint32_t it = 0; it < iters; ++it) {
     // fld_applyBoundaryCondition, fluids.cl:435-439.
     OR_PARALLEL_FOR
-    for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, clamp4(ld4(pred, i), lo, hi));
-    or_fld_density(c, p, pred, table.data(), n, density.data());
-    or_fld_lambda(c, p, pred, density.data(), table.data(), n, lambda.data());
-    or_fld_correction(c, p, pred, lambda.data(), table.data(), n, corr.data());
+    for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, clamp4(ld4(pred, i), b.lo, b.hi));
+    or_fld_density(c, p, pred, table, n, density.data());
+    or_fld_lambda(c, p, pred, density.data(), table, n, lambda.data());
+    or_fld_correction(c, p, pred, lambda.data(), table, n, corr.data());
     // fld_correctPosition, fluids.cl:252-258.
     OR_PARALLEL_FOR
     for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, ld4(pred, i) + ld4(corr.data(), i));
+    if (lamTot)
+      for (uint32_t i = 0; i < n; ++i) lamTot[i] += lambda[i];
   }
-  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
-  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+}
 
-  // fld_updateVel, fluids.cl:263-273 (Fluids.cpp:442).
+// fld_updateVel (Fluids.cpp:442), vorticity confinement + XSPH (:444-454), updatePosition.
+void fluid_post(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t n, or_state* s,
+                const uint32_t* table) {
+  const Grid g(c);
+  const Sph k(c);
+  const float dt = p->timeStep;
+  float* pos = s->pos;
+  float* vel = s->vel;
+  float* pred = s->predPos;
+  // fld_updateVel, fluids.cl:263-273.
   OR_PARALLEL_FOR
   for (int64_t i = 0; i < (int64_t)n; ++i)
     st4(vel, i, clamp4s((ld4(pred, i) - ld4(pos, i)) / (dt + FLOAT_EPS), -c->maxVel, c->maxVel));
@@ -428,9 +451,7 @@ int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint3
     for (int64_t i = 0; i < (int64_t)n; ++i) {
       const f4 x = ld4(pred, i), v = ld4(vel, i);
       f4 w = splat(0.0f);
-      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
-        w = w + cross(ld4(vel, e) - v, k.grad(x - ld4(pred, e)));
-      });
+      fluid_neighbours(g, table, x, [&](uint32_t e) { w = w + cross(ld4(vel, e) - v, k.grad(x - ld4(pred, e))); });
       st4(vort.data(), i, w);
     }
     // fld_applyVorticityConfinement, fluids.cl:329-377 (writes only vel[ID]).
@@ -438,9 +459,7 @@ int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint3
     for (int64_t i = 0; i < (int64_t)n; ++i) {
       const f4 x = ld4(pred, i), w = ld4(vort.data(), i);
       f4 eta = splat(0.0f);
-      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
-        eta = eta + flen(ld4(vort.data(), e)) * k.grad(x - ld4(pred, e));
-      });
+      fluid_neighbours(g, table, x, [&](uint32_t e) { eta = eta + flen(ld4(vort.data(), e)) * k.grad(x - ld4(pred, e)); });
       st4(vel, i, ld4(vel, i) + p->vorticityConfCoeff * cross(fnormalize(eta), w) * dt);
     }
     // copyBuffer(p_vel, p_velInViscosity), Fluids.cpp:451.
@@ -450,15 +469,298 @@ int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint3
     for (int64_t i = 0; i < (int64_t)n; ++i) {
       const f4 x = ld4(pred, i), v = ld4(velIn.data(), i);
       f4 visc = splat(0.0f);
-      fluid_neighbours(g, table.data(), x, [&](uint32_t e) {
-        visc = visc + (ld4(velIn.data(), e) - v) * k.poly6(x - ld4(pred, e));
-      });
+      fluid_neighbours(g, table, x, [&](uint32_t e) { visc = visc + (ld4(velIn.data(), e) - v) * k.poly6(x - ld4(pred, e)); });
       st4(vel, i, v + p->xsphViscosityCoeff * visc);
     }
     if (s->vort) std::memcpy(s->vort, vort.data(), sizeof(float) * 4 * n);
   }
   // fld_updatePosition, fluids.cl:444-450.
   std::memcpy(pos, pred, sizeof(float) * 4 * n);
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters,
+                   uint32_t n, or_state* s) {
+  if (!c || !p || !s || !s->pos || !s->vel || !s->predPos) return RTP_ERR_INVALID_ARGUMENT;
+  std::vector<uint32_t> table;
+  fluid_presort(c, p, n, s, table, nullptr);
+  std::vector<float> density(n), lambda(n);
+  fluid_jacobi(c, p, iters, s->predPos, table.data(), n, density, lambda, nullptr);
+  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
+  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+  fluid_post(c, p, n, s, table.data());
+  return RTP_OK;
+}
+
+// ---- learned warm start (new: no reference counterpart) ---------------------------------
+// Restates the GPU method of warmstart.cu / mlp.cuh / mlp_train.cu: the feature sums of the
+// first lambda sweep, the network (optionally with the GPU's BF16 operand rounding), its
+// loss gradient, and the warm-started step with the density-error guard.
+
+}  // extern "C"
+
+namespace {
+
+// Round-to-nearest-even to bfloat16 (the upper 16 bits of an IEEE float).
+inline float bf16r(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  u &= 0xffff0000u;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+inline double q(double v, bool emu) { return emu ? (double)bf16r((float)v) : v; }
+
+// GELU, tanh form (Hendrycks & Gimpel 2016), and its derivative.
+constexpr double kGA = 0.7978845608028654, kGB = 0.044715;
+inline double gelu(double x) { return 0.5 * x * (1.0 + std::tanh(kGA * (x + kGB * x * x * x))); }
+inline double gelu_grad(double x) {
+  const double t = std::tanh(kGA * (x + kGB * x * x * x));
+  return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * kGA * (1.0 + 3.0 * kGB * x * x);
+}
+
+struct NetD {
+  const rtp_mlp* n;
+  bool emu;
+  // Operand copies of the weights (rounded to BF16 when emulating).
+  std::vector<double> w1, w2, w3;
+  NetD(const rtp_mlp* net, bool e) : n(net), emu(e), w1(64 * 12), w2(64 * 64), w3(4 * 64) {
+    for (int o = 0; o < 64; ++o)
+      for (int k = 0; k < 12; ++k) w1[o * 12 + k] = q(net->w1[o][k], emu);
+    for (int o = 0; o < 64; ++o)
+      for (int k = 0; k < 64; ++k) w2[o * 64 + k] = q(net->w2[o][k], emu);
+    for (int o = 0; o < 4; ++o)
+      for (int k = 0; k < 64; ++k) w3[o * 64 + k] = q(net->w3[o][k], emu);
+  }
+  struct Act {
+    double x[12], z1[64], h1[64], z2[64], h2[64], y[4];
+  };
+  void forward(const float* f, Act& a) const {
+    for (int k = 0; k < 12; ++k) a.x[k] = q((double)((f[k] - n->inMean[k]) * n->inScale[k]), emu);
+    for (int o = 0; o < 64; ++o) {
+      double z = 0.0;
+      for (int k = 0; k < 12; ++k) z += a.x[k] * w1[o * 12 + k];
+      a.z1[o] = z + n->b1[o];
+      a.h1[o] = q(gelu(a.z1[o]), emu);
+    }
+    for (int o = 0; o < 64; ++o) {
+      double z = 0.0;
+      for (int k = 0; k < 64; ++k) z += a.h1[k] * w2[o * 64 + k];
+      a.z2[o] = z + n->b2[o];
+      a.h2[o] = q(gelu(a.z2[o]), emu);
+    }
+    for (int o = 0; o < 4; ++o) {
+      double z = 0.0;
+      for (int k = 0; k < 64; ++k) z += a.h2[k] * w3[o * 64 + k];
+      a.y[o] = z + n->b3[o];
+    }
+  }
+};
+
+// Feature sums of particle i at x0 (warmstart.cu ws_sweep + k_ws_lambda), using the
+// reference's neighbour loop and kernels.
+void ws_features_one(const Grid& g, const Sph& k, const rtp_fluid_params* p, const float* x0, const float* vel,
+                     const uint32_t* table, int64_t i, float lo[3], float hi[3], float* f, float* lambda0) {
+  const f4 pos = ld4(x0, i), vi = ld4(vel, i);
+  float rho = 0.0f, ssq = 0.0f, div = 0.0f;
+  f4 sg = splat(0.0f);
+  uint32_t cnt = 0;
+  const float h2 = k.h * k.h;
+  fluid_neighbours(g, table, pos, [&](uint32_t e) {
+    const f4 v = pos - ld4(x0, e);
+    rho += k.poly6(v);
+    const f4 gr = k.grad(v);
+    sg = sg + gr;
+    ssq += dot(gr, gr);
+    const float r2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if ((int64_t)e != i && r2 < h2) {
+      ++cnt;
+      const f4 dv = ld4(vel, e) - vi;
+      div += dv.x * gr.x + dv.y * gr.y + dv.z * gr.z;
+    }
+  });
+  const float C = rho / p->restDensity - 1.0f;
+  float sq = ssq + dot(sg, sg);
+  sq /= p->restDensity * p->restDensity;
+  const float lam = -C / (sq + p->relaxCFM);
+  const float hr = k.h / p->restDensity, invH = 1.0f / k.h;
+  auto prox = [&](float x, float l, float u) {
+    return std::fmin(std::fmax(2.0f - (x - l) * invH, 0.0f), 2.0f) - std::fmin(std::fmax(2.0f - (u - x) * invH, 0.0f), 2.0f);
+  };
+  f[0] = (float)cnt;
+  f[1] = C;
+  f[2] = sg.x * hr;
+  f[3] = sg.y * hr;
+  f[4] = sg.z * hr;
+  f[5] = ssq * hr * hr;
+  f[6] = div * (p->timeStep / p->restDensity);
+  f[7] = prox(pos.x, lo[0], hi[0]);
+  f[8] = prox(pos.y, lo[1], hi[1]);
+  f[9] = prox(pos.z, lo[2], hi[2]);
+  f[10] = lam;
+  f[11] = std::sqrt(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * p->timeStep * invH;
+  if (lambda0) *lambda0 = lam;
+}
+
+// Mean |rho / rho0 - 1| at x (fld_computeDensity with the step's table).
+double mean_density_error(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* x,
+                          const uint32_t* table, uint32_t n) {
+  std::vector<float> rho(n);
+  or_fld_density(c, p, x, table, n, rho.data());
+  double s = 0.0;
+  for (uint32_t i = 0; i < n; ++i) s += std::fabs(rho[i] / p->restDensity - 1.0f);
+  return n ? s / n : 0.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void or_ws_features(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* x0, const float* vel,
+                    const uint32_t* table, uint32_t n, float* feats) {
+  const Grid g(c);
+  const Sph k(c);
+  const Bounds b(g);
+  float lo[3] = {b.lo.x, b.lo.y, b.lo.z}, hi[3] = {b.hi.x, b.hi.y, b.hi.z};
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i)
+    ws_features_one(g, k, p, x0, vel, table, i, lo, hi, feats + 12 * i, nullptr);
+}
+
+void or_mlp_forward(const rtp_mlp* net, const float* feats, uint64_t n, int emulate, float* out) {
+  const NetD d(net, emulate != 0);
+  OR_PARALLEL_FOR
+  for (int64_t s = 0; s < (int64_t)n; ++s) {
+    NetD::Act a;
+    d.forward(feats + 12 * s, a);
+    for (int o = 0; o < 4; ++o) out[4 * s + o] = (float)(a.y[o] * net->outScale[o]);
+  }
+}
+
+void or_mlp_loss_grad(const rtp_mlp* net, const float* lossW, const float* feats, const float* targets, uint64_t n,
+                      int emulate, double* loss, double* grad) {
+  // grad: w1 (64x12), b1 (64), w2 (64x64), b2 (64), w3 (4x64), b3 (4) = 5252 doubles.
+  const bool emu = emulate != 0;
+  const NetD d(net, emu);
+  const int W1 = 0, B1 = W1 + 768, W2 = B1 + 64, B2 = W2 + 4096, W3 = B2 + 64, B3 = W3 + 256, NP = B3 + 4;
+  std::vector<double> G(NP, 0.0);
+  double L = 0.0;
+  const double invN = 1.0 / (double)n;
+  for (uint64_t s = 0; s < n; ++s) {
+    NetD::Act a;
+    d.forward(feats + 12 * s, a);
+    double dy[4];
+    for (int o = 0; o < 4; ++o) {
+      const double t = (double)(targets[4 * s + o] / net->outScale[o]);
+      const double e = a.y[o] - t;
+      L += lossW[o] * e * e;
+      dy[o] = q(2.0 * lossW[o] * e * invN, emu);
+    }
+    double dz2[64], dz1[64];
+    for (int h = 0; h < 64; ++h) {
+      double v = 0.0;
+      for (int o = 0; o < 4; ++o) v += dy[o] * d.w3[o * 64 + h];
+      dz2[h] = q(v * gelu_grad(a.z2[h]), emu);
+    }
+    for (int h = 0; h < 64; ++h) {
+      double v = 0.0;
+      for (int o = 0; o < 64; ++o) v += dz2[o] * d.w2[o * 64 + h];
+      dz1[h] = q(v * gelu_grad(a.z1[h]), emu);
+    }
+    for (int o = 0; o < 4; ++o) {
+      for (int h = 0; h < 64; ++h) G[W3 + o * 64 + h] += dy[o] * a.h2[h];
+      G[B3 + o] += dy[o];
+    }
+    for (int o = 0; o < 64; ++o) {
+      for (int h = 0; h < 64; ++h) G[W2 + o * 64 + h] += dz2[o] * a.h1[h];
+      G[B2 + o] += dz2[o];
+      for (int k = 0; k < 12; ++k) G[W1 + o * 12 + k] += dz1[o] * a.x[k];
+      G[B1 + o] += dz1[o];
+    }
+  }
+  *loss = L * invN;
+  std::memcpy(grad, G.data(), sizeof(double) * NP);
+}
+
+int or_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, uint32_t extraIters,
+               float guardTol, uint32_t plainIters, uint32_t n, or_state* s, float* lamTot, double* solverErr,
+               int* rerun) {
+  if (!c || !p || !net || !s || !s->pos || !s->vel || !s->predPos || !lamTot) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const Bounds b(g);
+  std::vector<uint32_t> table;
+  fluid_presort(c, p, n, s, table, nullptr);
+  float* pred = s->predPos;
+  // x0 = fld_applyBoundaryCondition(predPos) (the first iteration's clamp).
+  std::vector<float> x0(4 * (size_t)n);
+  for (uint32_t i = 0; i < n; ++i) st4(x0.data(), i, clamp4(ld4(pred, i), b.lo, b.hi));
+  // Features and the network (BF16 operand rounding as on the GPU).
+  std::vector<float> feats(12 * (size_t)n), out(4 * (size_t)n);
+  or_ws_features(c, p, x0.data(), s->vel, table.data(), n, feats.data());
+  or_mlp_forward(net, feats.data(), n, 1, out.data());
+  std::vector<float> lam(n), corr(4 * (size_t)n), density(n), lambdaBuf(n);
+  for (uint32_t i = 0; i < n; ++i) lam[i] = out[4 * i];
+  // x1 = x0 + dp(lambda_net) + r_net; clamped when plain iterations follow.
+  or_fld_correction(c, p, x0.data(), lam.data(), table.data(), n, corr.data());
+  for (uint32_t i = 0; i < n; ++i) {
+    f4 x = ld4(x0.data(), i) + ld4(corr.data(), i) + mk(out[4 * i + 1], out[4 * i + 2], out[4 * i + 3], 0.0f);
+    st4(pred, i, x);
+    lamTot[i] = lam[i];
+  }
+  fluid_jacobi(c, p, extraIters, pred, table.data(), n, density, lambdaBuf, lamTot);
+  double err = mean_density_error(c, p, pred, table.data(), n);
+  int rr = 0;
+  if (guardTol > 0.0f && err > (double)guardTol) {
+    rr = 1;
+    std::memcpy(pred, x0.data(), sizeof(float) * 4 * n);
+    std::fill(lamTot, lamTot + n, 0.0f);
+    fluid_jacobi(c, p, plainIters, pred, table.data(), n, density, lambdaBuf, lamTot);
+    err = mean_density_error(c, p, pred, table.data(), n);
+  }
+  if (solverErr) *solverErr = err;
+  if (rerun) *rerun = rr;
+  fluid_post(c, p, n, s, table.data());
+  return RTP_OK;
+}
+
+int or_ws_record_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters, uint32_t stride,
+                      uint32_t phase, uint32_t n, or_state* s, float* lamTot, float* feats, float* targets,
+                      uint32_t* count) {
+  if (!c || !p || !s || !lamTot || stride == 0 || iters == 0) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Bounds b(g);
+  std::vector<uint32_t> table;
+  fluid_presort(c, p, n, s, table, nullptr);
+  float* pred = s->predPos;
+  std::vector<float> x0(4 * (size_t)n);
+  for (uint32_t i = 0; i < n; ++i) st4(x0.data(), i, clamp4(ld4(pred, i), b.lo, b.hi));
+  std::vector<float> f(12 * (size_t)n);
+  or_ws_features(c, p, x0.data(), s->vel, table.data(), n, f.data());
+  std::fill(lamTot, lamTot + n, 0.0f);
+  std::vector<float> density(n), lambda(n);
+  fluid_jacobi(c, p, iters, pred, table.data(), n, density, lambda, lamTot);
+  // Targets: total lambda and xFinal - x0 - dp(total lambda) at x0.
+  std::vector<float> corr(4 * (size_t)n);
+  or_fld_correction(c, p, x0.data(), lamTot, table.data(), n, corr.data());
+  uint32_t m = 0;
+  for (uint32_t i = phase; i < n; i += stride, ++m) {
+    std::memcpy(feats + 12 * (size_t)m, f.data() + 12 * (size_t)i, 12 * sizeof(float));
+    const f4 d = ld4(pred, i) - (ld4(x0.data(), i) + ld4(corr.data(), i));
+    targets[4 * m] = lamTot[i];
+    targets[4 * m + 1] = d.x;
+    targets[4 * m + 2] = d.y;
+    targets[4 * m + 3] = d.z;
+  }
+  *count = m;
+  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
+  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+  fluid_post(c, p, n, s, table.data());
   return RTP_OK;
 }
 
@@ -483,10 +785,12 @@ void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, co
     rho[i] = r;
     nb[i] = cnt;
   }
-  double sum = 0.0, mx = 0.0, ke = 0.0, nsum = 0.0;
+  double sum = 0.0, mx = 0.0, ke = 0.0, nsum = 0.0, comp = 0.0;
   for (uint32_t i = 0; i < n; ++i) {
-    const double err = std::fabs((double)rho[i] / (double)p->restDensity - 1.0);
+    const double cdev = (double)rho[i] / (double)p->restDensity - 1.0;
+    const double err = std::fabs(cdev);
     sum += err;
+    comp += std::max(cdev, 0.0);
     mx = std::max(mx, err);
     const f4 v = ld4(vel, i);
     ke += 0.5 * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
@@ -497,6 +801,7 @@ void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, co
   m->maxDensityError = mx;
   m->kineticEnergy = ke;
   m->meanNeighbours = nsum / n;
+  m->meanCompression = comp / n;
 }
 
 int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary,

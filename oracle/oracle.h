@@ -84,6 +84,28 @@ void or_fld_correction(const rtp_grid_constants* c, const rtp_fluid_params* p,
 void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* predPos,
                       const float* vel, const uint32_t* table, uint32_t n, rtp_metrics* m);
 
+/* ---- learned warm start (new; restates the GPU method, not a reference kernel) ---------- */
+/* Raw features (rtp.h, RTP_MLP_IN per particle) at the clamped predicted positions x0 of a
+ * sorted state: vel = the step's input velocities. */
+void or_ws_features(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* x0, const float* vel,
+                    const uint32_t* table, uint32_t n, float* feats);
+/* Network outputs in target units, double arithmetic; emulate = round the operands to BF16
+ * where the GPU's tensor-core GEMMs do. */
+void or_mlp_forward(const rtp_mlp* net, const float* feats, uint64_t n, int emulate, float* out);
+/* Loss and gradient (w1, b1, w2, b2, w3, b3 as 5252 doubles), as rtp_mlp_loss_grad. */
+void or_mlp_loss_grad(const rtp_mlp* net, const float* lossW, const float* feats, const float* targets, uint64_t n,
+                      int emulate, double* loss, double* grad);
+/* One warm-started Fluids step; lamTot receives the multiplier totals (sorted order). */
+int or_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, uint32_t extraIters,
+               float guardTol, uint32_t plainIters, uint32_t n, or_state* s, float* lamTot, double* solverErr,
+               int* rerun);
+/* One plain step with `iters` iterations (lamTot receives the lambda sums) that also returns
+ * the samples of particles
+ * phase, phase + stride, ... (features and targets as rtp_record_warm_start_samples). */
+int or_ws_record_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters, uint32_t stride,
+                      uint32_t phase, uint32_t n, or_state* s, float* lamTot, float* feats, float* targets,
+                      uint32_t* count);
+
 #ifdef __cplusplus
 }
 #endif

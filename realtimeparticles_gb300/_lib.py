@@ -70,6 +70,14 @@ _SIGS = {
     "rtp_radix_sort": [P, U32, U32, P, P, P, C.c_size_t, P],
     "rtp_build_cell_table": [C.POINTER(abi.GridConstants), P, U32, P, P],
     "rtp_radix_sort_noalloc": [P, U32, U32, P, P, P],
+    "rtp_set_warm_start": [P, C.POINTER(abi.Mlp), C.POINTER(abi.WarmStartConfig)],
+    "rtp_enable_solver_stats": [P, C.c_int],
+    "rtp_get_solver_stats": [P, C.POINTER(abi.SolverStats)],
+    "rtp_reset_solver_stats": [P],
+    "rtp_record_warm_start_samples": [P, U32, U32, U32, P, P, U64, C.POINTER(U64)],
+    "rtp_train_warm_start": [P, P, U64, C.POINTER(abi.TrainConfig), C.POINTER(abi.Mlp), P, P],
+    "rtp_mlp_loss_grad": [C.POINTER(abi.Mlp), P, P, P, U64, C.POINTER(C.c_double), C.POINTER(abi.Mlp), P],
+    "rtp_mlp_forward": [C.POINTER(abi.Mlp), P, U64, P, P],
 }
 _RESTYPES = {"rtp_last_error": C.c_char_p}
 

@@ -53,6 +53,7 @@ BUF_CELL_ID = 10
 BUF_CELL_TABLE = 11
 BUF_VORTICITY = 12
 BUF_ACC = 13
+BUF_LAMBDA_TOTAL = 14
 
 
 class ModelParams(C.Structure):
@@ -155,9 +156,84 @@ class Metrics(C.Structure):
         ("kineticEnergy", C.c_double),
         ("meanNeighbours", C.c_double),
         ("neighbourHist", C.c_uint32 * 64),
+        ("meanCompression", C.c_double),
         ("pairListOverflows", C.c_uint32),
         ("pairListMax", C.c_uint32),
     ]
+
+
+MLP_IN = 12
+MLP_HIDDEN = 64
+MLP_OUT = 4
+
+
+class Mlp(C.Structure):
+    """rtp_mlp: the warm-start network (weights row-major [out][in])."""
+    _fields_ = [
+        ("inMean", C.c_float * MLP_IN),
+        ("inScale", C.c_float * MLP_IN),
+        ("w1", (C.c_float * MLP_IN) * MLP_HIDDEN),
+        ("b1", C.c_float * MLP_HIDDEN),
+        ("w2", (C.c_float * MLP_HIDDEN) * MLP_HIDDEN),
+        ("b2", C.c_float * MLP_HIDDEN),
+        ("w3", (C.c_float * MLP_HIDDEN) * MLP_OUT),
+        ("b3", C.c_float * MLP_OUT),
+        ("outScale", C.c_float * MLP_OUT),
+    ]
+
+
+class WarmStartConfig(C.Structure):
+    _fields_ = [
+        ("enabled", C.c_uint32),
+        ("extraIterations", C.c_uint32),
+        ("guardTolerance", C.c_float),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class SolverStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_uint64),
+        ("reruns", C.c_uint64),
+        ("sumDensityError", C.c_double),
+        ("maxDensityError", C.c_double),
+        ("sumFirstError", C.c_double),
+    ]
+
+
+class TrainConfig(C.Structure):
+    _fields_ = [
+        ("epochs", C.c_uint32),
+        ("batch", C.c_uint32),
+        ("learningRate", C.c_float),
+        ("finalLrFraction", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+        ("weightDecay", C.c_float),
+        ("lossWeights", C.c_float * MLP_OUT),
+        ("seed", C.c_uint64),
+    ]
+
+
+MLP_ARRAYS = ("inMean", "inScale", "w1", "b1", "w2", "b2", "w3", "b3", "outScale")
+MLP_TRAINABLE = ("w1", "b1", "w2", "b2", "w3", "b3")
+
+
+def mlp_to_arrays(net):
+    """rtp_mlp -> dict of numpy float32 arrays."""
+    import numpy as np
+    return {k: np.ctypeslib.as_array(getattr(net, k)).astype(np.float32).copy() for k in MLP_ARRAYS}
+
+
+def mlp_from_arrays(d):
+    """dict of arrays (as mlp_to_arrays) -> rtp_mlp."""
+    import numpy as np
+    net = Mlp()
+    for k in MLP_ARRAYS:
+        dst = np.ctypeslib.as_array(getattr(net, k))
+        dst[...] = np.asarray(d[k], dtype=np.float32).reshape(dst.shape)
+    return net
 
 
 def struct_to_dict(s):

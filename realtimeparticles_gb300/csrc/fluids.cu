@@ -23,17 +23,6 @@
 
 namespace rtp {
 
-__device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
-
-// Operands of one pair loaded ahead of use: a position and a scalar, or two float4.
-struct Pair4 {
-  float4 x;
-  float s;
-};
-struct Pair44 {
-  float4 x, v;
-};
-
 // fld_predictPosition (fluids.cl:62-74) + fillCellIDs (grid.cl:76-86) + digit-0 histogram.
 // Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
 __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK p, const float4* __restrict__ pos,
@@ -73,7 +62,8 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK 
 __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
-                                                                float* __restrict__ density, PairList pl) {
+                                                                float* __restrict__ density, PairList pl,
+                                                                float* __restrict__ lamTot, int totMode) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
@@ -108,22 +98,12 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, Flu
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
-  lambda[i] = -C / (ssq + p.relaxCFM);
+  const float lam = -C / (ssq + p.relaxCFM);
+  lambda[i] = lam;
   density[i] = rho;
-}
-
-// Visits the pairs recorded for particle i, one in kQuad per lane (lane q takes entries
-// q, q + kQuad, ...); an overflowed particle searches its 27 cells on lane 0.
-template <class G, class F>
-__device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
-                                           uint32_t i, uint32_t q, float4 xi, G&& ld, F&& f) {
-  const uint32_t c = __ldg(L.count + i);
-  if (c != kListOverflow) {
-    const uint32_t* base = L.idx + i;
-    visit_list_x4(q, c, kQuad, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
-  } else if (q == 0) {
-    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
-  }
+  // Total lambda of the step (warm start): kTotWrite starts it, kTotAdd accumulates.
+  if (totMode == kTotWrite) lamTot[i] = lam;
+  else if (totMode == kTotAdd) lamTot[i] += lam;
 }
 
 // fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
@@ -134,7 +114,7 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut,
                                                       const float4* __restrict__ posS, float4* __restrict__ velS,
-                                                      PairList pl) {
+                                                      PairList pl, const float4* __restrict__ res) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -165,7 +145,13 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
   cy = quad_sum(cy);
   cz = quad_sum(cz);
   if (!active || q != 0) return;
-  const float4 out = f4(xi.x + cx * p.invRho0, xi.y + cy * p.invRho0, xi.z + cz * p.invRho0, xi.w);
+  float4 out = f4(xi.x + cx * p.invRho0, xi.y + cy * p.invRho0, xi.z + cz * p.invRho0, xi.w);
+  if (res) {  // warm start: the network's residual displacement
+    const float4 r = ld4(res + i);
+    out.x += r.x;
+    out.y += r.y;
+    out.z += r.z;
+  }
   // The next iteration starts with fld_applyBoundaryCondition: store its result directly.
   // After the last iteration the unclamped position is kept (fld_updateVel, fluids.cl:263).
   predOut[i] = LAST ? out : bc_clamp(p, out);
@@ -191,37 +177,47 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
 
 // fld_computeVorticity (fluids.cl:278-324); records the pairs within h of the final
 // positions for confinement and XSPH (same two-phase scheme as k_fluid_lambda).
-__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, const float4* __restrict__ pred,
+// GUARD also evaluates fld_computeDensity at those positions and writes each block's sum
+// of |rho_i / rho0 - 1| to errPartial[blockIdx.x] (warm-start guard, solver statistics).
+template <bool GUARD>
+__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                     const float4* __restrict__ velS,
                                                                     const uint2* __restrict__ table, uint32_t n,
-                                                                    float4* __restrict__ vort, PairList pl) {
+                                                                    float4* __restrict__ vort, PairList pl,
+                                                                    float* __restrict__ errPartial) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Sph k(g);
-  const float4 xi = ld4(pred + i), vi = ld4(velS + i);
-  uint32_t cnt = 0;
-  uint32_t* lst = pl.idx + i;
-  filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
-    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
-    ++cnt;
-  });
-  float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
-  auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
-  auto body = [&](uint32_t, Pair44 a) {
-    const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
-    const float r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < k.h2) {
-      float r;
-      const float s = k.gs(r2, r);
-      w = w + cross4(a.v - vi, f4(vx * s, vy * s, vz * s, 0.0f));
-    }
-  };
-  if (cnt <= pl.K)
-    visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ld, body);
-  else
-    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ld(j)); });
-  pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
-  vort[i] = w;
+  float err = 0.0f;
+  if (i < n) {
+    const Sph k(g);
+    const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+    uint32_t cnt = 0;
+    uint32_t* lst = pl.idx + i;
+    filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+      if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
+      ++cnt;
+    });
+    float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    float rho = 0.0f;
+    auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
+    auto body = [&](uint32_t, Pair44 a) {
+      const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        if (GUARD) rho += k.w(r2);
+        float r;
+        const float s = k.gs(r2, r);
+        w = w + cross4(a.v - vi, f4(vx * s, vy * s, vz * s, 0.0f));
+      }
+    };
+    if (cnt <= pl.K)
+      visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ld, body);
+    else
+      for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ld(j)); });
+    pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
+    vort[i] = w;
+    if (GUARD) err = fabsf(rho / p.rho0 - 1.0f);
+  }
+  if (GUARD) block_error_partial(err, errPartial);
 }
 
 // fld_applyVorticityConfinement (fluids.cl:329-377), kQuad lanes per particle.
@@ -322,9 +318,10 @@ __global__ void k_fluid_final(const float4* __restrict__ pred, const float4* __r
 __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const float4* __restrict__ pos,
                                                        const float4* __restrict__ vel, const uint2* __restrict__ table,
                                                        uint32_t n, double* __restrict__ acc, uint32_t* __restrict__ hist) {
-  // acc: [0] sum |rho/rho0 - 1|, [1] kinetic energy, [2] neighbour count; hist[64] = max error bits.
+  // acc: [0] sum |rho/rho0 - 1|, [1] kinetic energy, [2] neighbour count, [3] sum max(rho/rho0 - 1, 0);
+  // hist[64] = max error bits.
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  double err = 0.0, ke = 0.0, nb = 0.0;
+  double err = 0.0, ke = 0.0, nb = 0.0, comp = 0.0;
   float mx = 0.0f;
   if (i < n) {
     const Sph k(g);
@@ -340,8 +337,10 @@ __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const 
         if (j != i) ++cnt;
       }
     });
-    const float e = fabsf(rho / p.rho0 - 1.0f);
+    const float cdev = rho / p.rho0 - 1.0f;
+    const float e = fabsf(cdev);
     err = e;
+    comp = fmaxf(cdev, 0.0f);
     mx = e;
     const float4 v = ld4(vel + i);
     ke = 0.5 * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
@@ -353,12 +352,14 @@ __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const 
     err += __shfl_down_sync(0xffffffffu, err, o);
     ke += __shfl_down_sync(0xffffffffu, ke, o);
     nb += __shfl_down_sync(0xffffffffu, nb, o);
+    comp += __shfl_down_sync(0xffffffffu, comp, o);
     mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
   }
   if ((threadIdx.x & 31) == 0) {
     atomicAdd(acc + 0, err);
     atomicAdd(acc + 1, ke);
     atomicAdd(acc + 2, nb);
+    atomicAdd(acc + 3, comp);
     atomicMax(hist + 64, __float_as_uint(mx));  // mx >= 0: uint order == float order
   }
 }
@@ -390,19 +391,28 @@ int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const floa
 
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table, uint32_t n,
                     float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
-                    Launcher& L) {
+                    Launcher& L, float* lamTot, int totMode) {
   L.begin("fld_lambda");
-  k_fluid_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl);
+  k_fluid_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl,
+                                                                           lamTot, totMode);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
   if (rc) return rc;
+  return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L);
+}
+
+int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
+                 const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
+                 const float4* res, Launcher& L) {
   if (last) {
     L.begin("fld_deltap_vel");
-    k_fluid_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS, pl);
+    k_fluid_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS,
+                                                                        velS, pl, res);
     L.end("fld_deltap_vel");
   } else {
     L.begin("fld_deltap");
-    k_fluid_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS, velS, pl);
+    k_fluid_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS,
+                                                                         velS, pl, res);
     L.end("fld_deltap");
   }
   return check("k_fluid_deltap");
@@ -416,15 +426,28 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
   return check("k_fluid_update_vel");
 }
 
+int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
+                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L) {
+  L.begin("fld_vorticity");
+  if (errPartial)
+    k_fluid_vorticity<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort,
+                                                                                      pl, errPartial);
+  else
+    k_fluid_vorticity<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort,
+                                                                                       pl, nullptr);
+  L.end("fld_vorticity");
+  return check("k_fluid_vorticity");
+}
+
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L) {
+               Launcher& L, bool vorticityDone) {
   if (p.vorticity) {
-    L.begin("fld_vorticity");
-    k_fluid_vorticity<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, pred, velS, table, n, vort, pl);
-    L.end("fld_vorticity");
-    int rc = check("k_fluid_vorticity");
-    if (rc) return rc;
+    int rc = RTP_OK;
+    if (!vorticityDone) {
+      rc = fluid_vorticity(g, p, pred, velS, vort, table, n, pl, nullptr, L);
+      if (rc) return rc;
+    }
     L.begin("fld_confine");
     k_fluid_confine<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
     L.end("fld_confine");

@@ -21,18 +21,51 @@ struct FluidK {
 
 FluidK make_fluidk(const rtp_grid_constants& c, const rtp_fluid_params& p);
 
+#ifdef __CUDACC__
+__device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
 
+// Operands of one pair loaded ahead of use: a position and a scalar, or two float4.
+struct Pair4 {
+  float4 x;
+  float s;
+};
+struct Pair44 {
+  float4 x, v;
+};
+
+// Block sum of v (blockDim.x == kSweepThreads, every thread of the block calls once)
+// written to out[blockIdx.x].
+__device__ __forceinline__ void block_error_partial(float v, float* out) {
+  static_assert(kSweepThreads == 64, "two warps per block");
+  __shared__ float s_part[2];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) out[blockIdx.x] = s_part[0] + s_part[1];
+}
+#endif
+
+// Total-lambda bookkeeping of k_fluid_lambda (warm start).
+constexpr int kTotNone = 0, kTotWrite = 1, kTotAdd = 2;
 
 int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L);
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table,
                     uint32_t n, float* lambda, float* density, bool last, const float4* posS, float4* velS,
-                    const PairList& pl, Launcher& L);
+                    const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone);
+// Position correction alone with given lambdas (+ an optional residual displacement).
+int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
+                 const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
+                 const float4* res, Launcher& L);
+// fld_computeVorticity; with errPartial also the per-block density-error sums.
+int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
+                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L);
 int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const float4* posS, uint32_t n, float4* velS,
                      Launcher& L);
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L);
+               Launcher& L, bool vorticityDone = false);
 int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, const uint2* table, uint32_t n,
                   double* acc, uint32_t* hist, Launcher& L);
 

@@ -21,6 +21,7 @@
 #include "clouds.cuh"
 #include "fluids.cuh"
 #include "rtp_internal.hpp"
+#include "warmstart.cuh"
 
 namespace rtp {
 
@@ -173,6 +174,20 @@ struct Handle {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
 
   bool hasStep = false;  // a step ran since the last upload (cell table / keys valid)
+
+  // Learned warm start (fluids).
+  bool wsOn = false;
+  uint32_t wsExtra = 0;
+  float wsTol = 0.0f;
+  bool statsOn = false;        // solver statistics in plain steps
+  void* mlpBlock = nullptr;    // packed network
+  float* mlpTmp = nullptr;     // upload staging for the packer
+  float* lamTot = nullptr;     // lambda summed over the last warm-started / recording step
+  float4* wsRes = nullptr;     // the network's residual displacements
+  float* errPartial = nullptr; // per-block density-error sums
+  SolverStatsDev* solverStats = nullptr;
+  PairList pairsRec{};         // pairs at the predicted positions while recording samples
+  cudaStream_t stream2 = nullptr;  // captures the guard's rerun body
 };
 
 int Launcher::begin(const char* name) {
@@ -242,6 +257,7 @@ static int alloc_buffers(Handle* h) {
     h->pairs.stride = (uint32_t)M;
     h->pairs.K = kPairListK;
   }
+  if (h->model == RTP_MODEL_FLUIDS) RTP_TRY(dalloc(h, &h->lamTot, M));
   if (h->model == RTP_MODEL_CLOUDS) {
     RTP_TRY(dalloc(h, &h->totCorr, M));
     RTP_TRY(dalloc(h, &h->totCorrS, M));
@@ -278,21 +294,53 @@ static void free_handle(Handle* h) {
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   delete h;
+}
+
+// Buffers of the warm start and of the solver statistics (allocated on first use).
+static int ws_alloc(Handle* h) {
+  if (h->wsRes) return RTP_OK;
+  const size_t M = h->maxN;
+  RTP_TRY(dalloc(h, &h->wsRes, M));
+  RTP_TRY(dalloc(h, &h->errPartial, ws_error_blocks((uint32_t)M)));
+  RTP_TRY(dalloc(h, &h->solverStats, 1));
+  char* blk = nullptr;
+  RTP_TRY(dalloc(h, &blk, MlpLayout::bytes));
+  h->mlpBlock = blk;
+  RTP_TRY(dalloc(h, &h->mlpTmp, mlp_upload_tmp_floats()));
+  if (!h->stream2) RTP_CUDA(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+  return RTP_OK;
+}
+
+static int ws_alloc_rec(Handle* h) {
+  RTP_TRY(ws_alloc(h));
+  if (h->pairsRec.idx) return RTP_OK;
+  const size_t M = h->maxN;
+  RTP_TRY(dalloc(h, &h->pairsRec.idx, (size_t)kPairListK * M));
+  RTP_TRY(dalloc(h, &h->pairsRec.count, M));
+  h->pairsRec.stride = (uint32_t)M;
+  h->pairsRec.K = kPairListK;
+  return RTP_OK;
+}
+
+// A new state has no lambda totals yet.
+static int ws_forget(Handle* h) {
+  if (h->lamTot) RTP_CUDA(cudaMemsetAsync(h->lamTot, 0, sizeof(float) * h->maxN, h->stream));
+  return RTP_OK;
 }
 
 static void invalidate(Handle* h) { h->graphValid = false; }
 
 // ---- one model step (the update() sequences) ------------------------------------------
-static int record_fluids_step(Handle* h, Launcher& L) {
+// Fluids.cpp:412-424: predict, cell ids, sort {pos, vel, predPos} (+ ids), cell table.
+// clampOut: store the clamped prediction (a Jacobi iteration or correction consumes it).
+static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOut) {
   const uint32_t n = (uint32_t)h->curN;
-  if (n == 0) return RTP_OK;
   const GridK& g = h->g;
-  const FluidK fk = make_fluidk(h->gc, h->fp);
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   RTP_TRY(launch_sort_clear(plan, h->ss, L));
-  // Fluids.cpp:412-417: predict, cell ids, sort {pos, vel, predPos} (+ ids).
-  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, h->iters > 0, L));
+  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -305,8 +353,48 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   gl.dst1[0] = h->idsS;
   gl.n1 = 1;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
-  // Fluids.cpp:419-424.
-  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  return launch_cell_table(g, h->cellId, n, h->table, L);
+}
+
+// `count` plain Jacobi iterations from `in`; the outputs alternate between dest and spare
+// so that the last lands in dest.  With trackTot the total lambda is accumulated (started
+// by the first iteration unless firstAdds).
+static int plain_iterations(Handle* h, Launcher& L, const FluidK& fk, const float4* in, uint32_t count, float4* dest,
+                            float4* spare, bool trackTot, bool firstAdds) {
+  const uint32_t n = (uint32_t)h->curN;
+  const float4* cur = in;
+  for (uint32_t it = 0; it < count; ++it) {
+    float4* out = ((count - it) % 2 == 1) ? dest : spare;
+    const int mode = !trackTot ? kTotNone : ((it == 0 && !firstAdds) ? kTotWrite : kTotAdd);
+    RTP_TRY(fluid_iteration(h->g, fk, cur, out, h->table, n, h->lambda, h->density, it + 1 == count, h->posS, h->velS,
+                            h->pairs, L, h->lamTot, mode));
+    cur = out;
+  }
+  return RTP_OK;
+}
+
+// Solver-output density error into errPartial: fused into the vorticity sweep when that
+// runs (returns true), else a separate sweep.
+static int solver_error(Handle* h, Launcher& L, const FluidK& fk, const float4* x, bool* vortDone) {
+  const uint32_t n = (uint32_t)h->curN;
+  if (fk.vorticity) {
+    RTP_TRY(fluid_vorticity(h->g, fk, x, h->velS, h->vort, h->table, n, h->pairs, h->errPartial, L));
+    *vortDone = true;
+    return RTP_OK;
+  }
+  *vortDone = false;
+  return ws_density_error(h->g, fk, x, h->table, n, h->errPartial, L);
+}
+
+static int record_fluids_ws_step(Handle* h, Launcher& L);
+
+static int record_fluids_step(Handle* h, Launcher& L) {
+  const uint32_t n = (uint32_t)h->curN;
+  if (n == 0) return RTP_OK;
+  if (h->wsOn) return record_fluids_ws_step(h, L);
+  const GridK& g = h->g;
+  const FluidK fk = make_fluidk(h->gc, h->fp);
+  RTP_TRY(fluids_presort(h, L, fk, h->iters > 0));
   // Fluids.cpp:427-442.
   float4* cur = h->predA;
   float4* nxt = h->predB;
@@ -317,8 +405,105 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   }
   if (h->iters == 0) RTP_TRY(fluid_update_vel(g, fk, cur, h->posS, n, h->velS, L));
   h->predFinal = cur;
+  bool vortDone = false;
+  if (h->statsOn) {
+    RTP_TRY(solver_error(h, L, fk, cur, &vortDone));
+    RTP_TRY(ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, false, L));
+  }
   // Fluids.cpp:444-457.
-  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L);
+  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L, vortDone);
+}
+
+// Warm-started substep: the network's lambda and residual give the first correction, then
+// wsExtra plain iterations; the guard reruns the solve with the plain iteration count from
+// the same predicted positions (predA) inside a conditional graph node.  The solver output
+// always ends in predB (predTmp, free after the sort, is the third buffer).
+static int record_fluids_ws_step(Handle* h, Launcher& L) {
+  const uint32_t n = (uint32_t)h->curN;
+  const GridK& g = h->g;
+  const FluidK fk = make_fluidk(h->gc, h->fp);
+  RTP_TRY(fluids_presort(h, L, fk, true));
+  RTP_TRY(ws_lambda_infer(g, fk, h->predA, h->velS, h->table, n, h->lambda, h->density, h->lamTot,
+                          h->pairs, h->mlpBlock, h->wsRes, L));
+  const uint32_t E = h->wsExtra;
+  float4* warmOut = (E % 2 == 0) ? h->predB : h->predTmp;
+  RTP_TRY(fluid_deltap(g, fk, h->predA, warmOut, h->lambda, h->table, n, E == 0, h->posS, h->velS, h->pairs, h->wsRes, L));
+  RTP_TRY(plain_iterations(h, L, fk, warmOut, E, h->predB, h->predTmp, true, true));
+  h->predFinal = h->predB;
+  bool vortDone = false;
+  RTP_TRY(solver_error(h, L, fk, h->predB, &vortDone));
+  const bool guard = h->wsTol > 0.0f;
+  cudaGraphConditionalHandle hnd = 0;
+  cudaGraph_t capGraph = nullptr;
+  if (guard) {
+    cudaStreamCaptureStatus st;
+    RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, nullptr, nullptr, nullptr));
+    if (st != cudaStreamCaptureStatusActive) return fail(RTP_ERR_STATE, "warm-start guard needs a captured step");
+    RTP_CUDA(cudaGraphConditionalHandleCreate(&hnd, capGraph, 0, cudaGraphCondAssignDefault));
+  }
+  RTP_TRY(ws_guard(h->errPartial, n, h->wsTol, h->solverStats, hnd, guard, false, L));
+  if (guard) {
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, &deps, &edges, &nd));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hnd;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    RTP_CUDA(cudaGraphAddNode(&node, capGraph, deps, edges, nd, &np));
+    RTP_CUDA(cudaStreamUpdateCaptureDependencies(L.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    // Conditional bodies take kernels, memsets and copies only: no profiling events there.
+    Launcher L2;
+    L2.stream = h->stream2;
+    RTP_CUDA(cudaStreamBeginCaptureToGraph(h->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = RTP_OK;
+    if (h->iters > 0) {
+      rc = plain_iterations(h, L2, fk, h->predA, h->iters, h->predB, h->predTmp, true, false);
+    } else {
+      const cudaError_t ce =
+          cudaMemcpyAsync(h->predB, h->predA, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream2);
+      rc = ce == cudaSuccess ? RTP_OK : cuda_fail(ce, "cudaMemcpyAsync");
+      if (!rc) rc = fluid_update_vel(g, fk, h->predB, h->posS, n, h->velS, L2);
+      if (!rc) rc = cudaMemsetAsync(h->lamTot, 0, sizeof(float) * n, h->stream2) == cudaSuccess
+                        ? RTP_OK
+                        : fail(RTP_ERR_CUDA, "cudaMemsetAsync");
+    }
+    bool vd2 = false;
+    if (!rc) rc = solver_error(h, L2, fk, h->predB, &vd2);
+    if (!rc) rc = ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, true, L2);
+    cudaGraph_t bodyOut = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream2, &bodyOut);
+    if (rc) return rc;
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(guard body)");
+  }
+  return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
+                    vortDone);
+}
+
+// One plain step with `iters` iterations that also writes training samples.
+static int record_sample_step(Handle* h, uint32_t iters, uint32_t stride, uint32_t phase, float* feats, float* targets,
+                              uint32_t count) {
+  const uint32_t n = (uint32_t)h->curN;
+  const GridK& g = h->g;
+  const FluidK fk = make_fluidk(h->gc, h->fp);
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(fluids_presort(h, L, fk, true));
+  RTP_TRY(ws_lambda_record(g, fk, h->predA, h->velS, h->table, n, h->lambda, h->density, h->lamTot,
+                           h->pairsRec, stride, phase, feats, count, L));
+  float4* out0 = (iters % 2 == 1) ? h->predB : h->predTmp;
+  RTP_TRY(fluid_deltap(g, fk, h->predA, out0, h->lambda, h->table, n, iters == 1, h->posS, h->velS, h->pairsRec,
+                       nullptr, L));
+  RTP_TRY(plain_iterations(h, L, fk, out0, iters - 1, h->predB, h->predTmp, true, true));
+  RTP_TRY(ws_record_targets(g, fk, h->predA, h->lamTot, h->table, n, h->predB, h->pairsRec, stride, phase, count,
+                            targets, L));
+  h->predFinal = h->predB;
+  return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L);
 }
 
 static int record_boids_step(Handle* h, Launcher& L) {
@@ -557,6 +742,7 @@ static int init_case(Handle* h) {
   RTP_CUDA(cudaMemcpyAsync(h->vel, vel.data(), sizeof(float4) * h->maxN, cudaMemcpyHostToDevice, h->stream));
   RTP_CUDA(cudaMemcpyAsync(h->ids, id.data(), sizeof(uint32_t) * h->maxN, cudaMemcpyHostToDevice, h->stream));
   h->curN = n;
+  RTP_TRY(ws_forget(h));
   if (h->model == RTP_MODEL_CLOUDS) {
     Launcher L;
     L.stream = h->stream;
@@ -946,6 +1132,7 @@ static int buffer_info(Handle* h, int buf, void** dptr, size_t* elem, uint64_t* 
     case RTP_BUF_CELL_TABLE: *dptr = h->tableRef; *elem = 8; *cap = h->gc.numCells; break;
     case RTP_BUF_VORTICITY: *dptr = h->vort; *elem = 16; break;
     case RTP_BUF_ACC: *dptr = h->acc; *elem = 16; break;
+    case RTP_BUF_LAMBDA_TOTAL: *dptr = h->lamTot; *elem = 4; break;
     default: return fail(RTP_ERR_INVALID_ARGUMENT, "unknown buffer");
   }
   if (!*dptr) return fail(RTP_ERR_INVALID_ARGUMENT, "buffer not used by this model");
@@ -964,6 +1151,7 @@ int rtp_upload(void* handle, int buffer, const void* host, uint64_t count) {
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_upload: derived buffer is read-only");
   if (count > cap) return fail(RTP_ERR_CAPACITY, "rtp_upload: count exceeds capacity");
   RTP_CUDA(cudaMemcpyAsync(d, host, elem * count, cudaMemcpyHostToDevice, h->stream));
+  if (buffer == RTP_BUF_POS) RTP_TRY(ws_forget(h));
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   return RTP_OK;
   RTP_GUARD_END
@@ -1103,9 +1291,102 @@ int rtp_get_metrics(void* handle, rtp_metrics* out) {
   out->maxDensityError = mx;
   out->kineticEnergy = acc[1];
   out->meanNeighbours = acc[2] / n;
+  out->meanCompression = acc[3] / n;
   for (int i = 0; i < 64; ++i) out->neighbourHist[i] = hist[i];
   out->pairListOverflows = hist[70];
   out->pairListMax = hist[71];
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_config* cfg) {
+  RTP_GUARD_BEGIN
+  if (!handle || !cfg) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: null argument");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: fluids only");
+  if (!cfg->enabled) {
+    h->wsOn = false;
+    invalidate(h);
+    return RTP_OK;
+  }
+  if (!net) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: null network");
+  if (cfg->extraIterations > 64) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: at most 64 extra iterations");
+  for (int k = 0; k < RTP_MLP_IN; ++k)
+    if (!std::isfinite(net->inMean[k]) || !std::isfinite(net->inScale[k]))
+      return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: non-finite normalisation");
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  RTP_TRY(ws_alloc(h));
+  RTP_TRY(mlp_upload_packed(*net, h->mlpTmp, h->mlpBlock, h->stream));
+  h->wsOn = true;
+  h->wsExtra = cfg->extraIterations;
+  h->wsTol = cfg->guardTolerance;
+  invalidate(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_enable_solver_stats(void* handle, int enable) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_enable_solver_stats: fluids only");
+  if (enable) RTP_TRY(ws_alloc(h));
+  h->statsOn = enable != 0;
+  invalidate(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_get_solver_stats(void* handle, rtp_solver_stats* out) {
+  RTP_GUARD_BEGIN
+  if (!handle || !out) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  std::memset(out, 0, sizeof *out);
+  if (!h->solverStats) return RTP_OK;
+  SolverStatsDev d;
+  RTP_CUDA(cudaMemcpyAsync(&d, h->solverStats, sizeof d, cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  out->steps = d.steps;
+  out->reruns = d.reruns;
+  out->sumDensityError = d.sumErr;
+  out->maxDensityError = d.maxErr;
+  out->sumFirstError = d.sumFirst;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_reset_solver_stats(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  Handle* h = H(handle);
+  if (!h->solverStats) return RTP_OK;
+  RTP_CUDA(cudaMemsetAsync(h->solverStats, 0, sizeof(SolverStatsDev), h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, uint32_t stride, uint32_t phase,
+                                  float* d_features, float* d_targets, uint64_t capacity, uint64_t* written) {
+  RTP_GUARD_BEGIN
+  if (!handle || !written) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: null argument");
+  *written = 0;
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_record_warm_start_samples: fluids only");
+  if (referenceIterations == 0 || referenceIterations > 64)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: referenceIterations must be in [1, 64]");
+  if (stride == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: stride must be > 0");
+  const uint32_t n = (uint32_t)h->curN;
+  const uint64_t avail = phase < n ? (uint64_t)(n - phase + stride - 1) / stride : 0;
+  const uint32_t count = (uint32_t)std::min<uint64_t>(avail, capacity);
+  if (count && (!d_features || !d_targets))
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: null sample arrays");
+  if (n == 0 || h->paused) return RTP_OK;
+  RTP_TRY(ws_alloc_rec(h));
+  RTP_TRY(record_sample_step(h, referenceIterations, stride, phase, d_features, d_targets, count));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasStep = true;
+  *written = count;
   return RTP_OK;
   RTP_GUARD_END
 }

@@ -146,6 +146,20 @@ __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const
   });
 }
 
+// Visits the pairs recorded for particle i, one in kQuad per lane (lane q takes entries
+// q, q + kQuad, ...); an overflowed particle searches its 27 cells on lane 0.
+template <class G, class F>
+__device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
+                                           uint32_t i, uint32_t q, float4 xi, G&& ld, F&& f) {
+  const uint32_t c = __ldg(L.count + i);
+  if (c != kListOverflow) {
+    const uint32_t* base = L.idx + i;
+    visit_list_x4(q, c, kQuad, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
+  } else if (q == 0) {
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
+  }
+}
+
 // Sum of v over the kQuad lanes of a particle (all 32 lanes of the warp must call).
 __device__ __forceinline__ float quad_sum(float v) {
   v += __shfl_xor_sync(0xffffffffu, v, 1);

@@ -1,0 +1,295 @@
+// warmstart.cu - learned warm start of the PBF constraint solve (new: the reference's Jacobi
+// loop, physics/ocl/Fluids.cpp:427-442, always starts from a zero correction).
+//
+// Per substep with the warm start on:
+//   k_ws_lambda<kInfer>   the first density / lambda sweep (fld_computeDensity +
+//                         fld_computeConstraintFactor at the predicted positions) also sums
+//                         the network's features, then each warp evaluates the MLP for its 32
+//                         particles on the tensor cores and writes lambda_i (the network's,
+//                         in place of the plain one) and a residual displacement r_i
+//   k_fluid_deltap        x_i += dp_i(lambda) + r_i, then the extra plain iterations
+//   vorticity sweep       also sums |rho_i / rho0 - 1| per block at the solver output
+//   k_ws_guard            mean error -> statistics; sets the graph's conditional to rerun the
+//                         step's solve with the plain iteration count when above tolerance
+// Training samples come from plain steps: k_ws_lambda<kRecord> writes the features of the
+// sampled particles, k_ws_record_targets their targets once the plain solve has finished.
+#include "warmstart.cuh"
+
+namespace rtp {
+
+constexpr int kRecord = 0, kInfer = 1;
+
+// Neighbour sums of the feature sweep.
+struct WsSums {
+  float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f, div = 0.0f;
+  uint32_t cnt = 0;
+};
+
+// fld_computeDensity + fld_computeConstraintFactor at xi (as k_fluid_lambda: filter pass into
+// the pair list, then the list in order) plus the feature sums.
+__device__ __forceinline__ void ws_sweep(const GridK& g, const uint2* __restrict__ table,
+                                         const float4* __restrict__ pred, const float4* __restrict__ velS, uint32_t i,
+                                         float4 xi, float4 vi, const PairList& pl, WsSums& S) {
+  const Sph k(g);
+  uint32_t cnt = 0;
+  uint32_t* lst = pl.idx + i;
+  filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
+    ++cnt;
+  });
+  auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
+  auto body = [&](uint32_t j, Pair44 a) {
+    const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      S.rho += k.w(r2);
+      float r;
+      const float s = k.gs(r2, r);
+      const float gxx = vx * s, gyy = vy * s, gzz = vz * s;
+      S.sgx += gxx;
+      S.sgy += gyy;
+      S.sgz += gzz;
+      S.ssq += gxx * gxx + gyy * gyy + gzz * gzz;
+      if (j != i) {
+        ++S.cnt;
+        S.div += (a.v.x - vi.x) * gxx + (a.v.y - vi.y) * gyy + (a.v.z - vi.z) * gzz;
+      }
+    }
+  };
+  if (cnt <= pl.K)
+    visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ld, body);
+  else
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ld(j)); });
+  pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
+}
+
+// Wall proximity along one axis: positive within 2h of the low wall, negative within 2h of
+// the high wall, 0 in between.
+__device__ __forceinline__ float wall_proximity(float x, float lo, float hi, float invH) {
+  return fminf(fmaxf(2.0f - (x - lo) * invH, 0.0f), 2.0f) - fminf(fmaxf(2.0f - (hi - x) * invH, 0.0f), 2.0f);
+}
+
+// Inference holds the network's fragments after the sweep: 14 blocks of 64 threads per SM
+// (73 registers) still keep 131,072 particles in one wave on 152 SMs.
+template <int MODE>
+__global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
+    k_ws_lambda(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ velS,
+                const uint2* __restrict__ table, uint32_t n,
+                float* __restrict__ lambda, float* __restrict__ density, float* __restrict__ lamTot, PairList pl,
+                uint32_t stride, uint32_t phase, float* __restrict__ feats, uint32_t capacity, MlpDev m,
+                float4* __restrict__ res) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  float f[kMlpIn];
+#pragma unroll
+  for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+  float lam = 0.0f;
+  if (active) {
+    const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+    WsSums S;
+    ws_sweep(g, table, pred, velS, i, xi, vi, pl, S);
+    // fld_computeConstraintFactor, same operations as k_fluid_lambda.
+    const float C = S.rho / p.rho0 - 1.0f;
+    const float ssqAll = (S.ssq + (S.sgx * S.sgx + S.sgy * S.sgy + S.sgz * S.sgz)) * p.invRho0Sq;
+    lam = -C / (ssqAll + p.relaxCFM);
+    density[i] = S.rho;
+    const float hr = g.h * p.invRho0, invH = 1.0f / g.h;
+    f[0] = (float)S.cnt;
+    f[1] = C;
+    f[2] = S.sgx * hr;
+    f[3] = S.sgy * hr;
+    f[4] = S.sgz * hr;
+    f[5] = S.ssq * hr * hr;
+    f[6] = S.div * (p.dt * p.invRho0);
+    f[7] = wall_proximity(xi.x, p.lo.x, p.hi.x, invH);
+    f[8] = wall_proximity(xi.y, p.lo.y, p.hi.y, invH);
+    f[9] = wall_proximity(xi.z, p.lo.z, p.hi.z, invH);
+    f[10] = lam;
+    f[11] = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * p.dt * invH;
+  }
+  if constexpr (MODE == kRecord) {
+    if (!active) return;
+    lambda[i] = lam;
+    lamTot[i] = lam;
+    if (i >= phase && (i - phase) % stride == 0) {
+      const uint32_t s = (i - phase) / stride;
+      if (s < capacity) {
+        float* o = feats + (size_t)s * kMlpIn;
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) o[k] = f[k];
+      }
+    }
+  } else {
+    // Inference: every lane of the warp takes part (inactive lanes with zero inputs).
+    __shared__ uint32_t s_stage[kSweepThreads / 32][32 * 9];
+    float x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) x[k] = active ? (f[k] - __ldg(m.inMean + k)) * __ldg(m.inScale + k) : 0.0f;
+    __syncwarp();
+    float y[kMlpOut];
+    mlp_warp_forward(m, x, y, s_stage[threadIdx.x >> 5]);
+    if (!active) return;
+    const float lw = y[0] * __ldg(m.outScale + 0);
+    lambda[i] = lw;
+    lamTot[i] = lw;
+    res[i] = f4(y[1] * __ldg(m.outScale + 1), y[2] * __ldg(m.outScale + 2), y[3] * __ldg(m.outScale + 3), 0.0f);
+  }
+}
+
+// Targets of sample s (particle i = phase + s * stride): (Lambda_i, xFinal_i - x0_i -
+// dp_i(Lambda)), dp as fld_computeConstraintCorrection over the pairs recorded at x0.
+__global__ void __launch_bounds__(128) k_ws_record_targets(GridK g, FluidK p, const float4* __restrict__ x0,
+                                                           const float* __restrict__ lamTot,
+                                                           const uint2* __restrict__ table, uint32_t n,
+                                                           const float4* __restrict__ xFinal, PairList pl0,
+                                                           uint32_t stride, uint32_t phase, uint32_t count,
+                                                           float* __restrict__ targets) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t s = t / kQuad, q = t % kQuad;
+  const uint32_t i = phase + s * stride;
+  const bool active = s < count && i < n;
+  float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f);
+  float li = 0.0f;
+  if (active) {
+    const Sph k(g);
+    xi = ld4(x0 + i);
+    li = __ldg(lamTot + i);
+    auto ld = [&](uint32_t j) { return Pair4{ld4(x0 + j), __ldg(lamTot + j)}; };
+    quad_pairs(g, table, pl0, i, q, xi, ld, [&](uint32_t, Pair4 a) {
+      const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float sg = k.gs(r2, r);
+        float sc = 0.0f;
+        if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
+        const float f = (li + a.s + sc) * sg;
+        cx += vx * f;
+        cy += vy * f;
+        cz += vz * f;
+      }
+    });
+  }
+  cx = quad_sum(cx);
+  cy = quad_sum(cy);
+  cz = quad_sum(cz);
+  if (!active || q != 0) return;
+  const float4 xf = ld4(xFinal + i);
+  float* o = targets + (size_t)s * kMlpOut;
+  o[0] = li;
+  o[1] = xf.x - (xi.x + cx * p.invRho0);
+  o[2] = xf.y - (xi.y + cy * p.invRho0);
+  o[3] = xf.z - (xi.z + cz * p.invRho0);
+}
+
+__global__ void __launch_bounds__(kSweepThreads) k_ws_density_error(GridK g, FluidK p, const float4* __restrict__ pos,
+                                                                    const uint2* __restrict__ table, uint32_t n,
+                                                                    float* __restrict__ errPartial) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float err = 0.0f;
+  if (i < n) {
+    const Sph k(g);
+    const float4 xi = ld4(pos + i);
+    float rho = 0.0f;
+    for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) {
+      const float4 xj = ld4(pos + j);
+      const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) rho += k.w(r2);
+    });
+    err = fabsf(rho / p.rho0 - 1.0f);
+  }
+  block_error_partial(err, errPartial);
+}
+
+// One block: the partial sums in a fixed order (deterministic), then the decision.
+constexpr int kGuardThreads = 256;
+__global__ void __launch_bounds__(kGuardThreads) k_ws_guard(const float* __restrict__ part, uint32_t nblk, uint32_t n,
+                                                           float tol, SolverStatsDev* st,
+                                                           cudaGraphConditionalHandle hnd, int hasCond, int accept) {
+  __shared__ double s_sum[kGuardThreads];
+  double v = 0.0;
+  for (uint32_t b = threadIdx.x; b < nblk; b += kGuardThreads) v += (double)part[b];
+  s_sum[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = kGuardThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s_sum[threadIdx.x] += s_sum[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double mean = n ? s_sum[0] / (double)n : 0.0;
+  if (accept) {
+    st->sumErr += mean;
+    st->maxErr = fmax(st->maxErr, mean);
+    return;
+  }
+  st->steps += 1;
+  st->sumFirst += mean;
+  const bool rerun = hasCond && tol > 0.0f && mean > (double)tol;
+  if (rerun) {
+    st->reruns += 1;
+  } else {
+    st->sumErr += mean;
+    st->maxErr = fmax(st->maxErr, mean);
+  }
+  if (hasCond) cudaGraphSetConditional(hnd, rerun ? 1u : 0u);
+}
+
+static int check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
+}
+
+static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
+
+int ws_lambda_record(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, const uint2* table, uint32_t n, float* lambda, float* density, float* lamTot, const PairList& pl,
+                     uint32_t stride, uint32_t phase, float* feats, uint32_t capacity, Launcher& L) {
+  if (stride == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "sample stride must be > 0");
+  MlpDev m{};
+  L.begin("ws_lambda_record");
+  k_ws_lambda<kRecord><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+      g, p, pred, velS, table, n, lambda, density, lamTot, pl, stride, phase, feats, capacity, m, nullptr);
+  L.end("ws_lambda_record");
+  return check("k_ws_lambda<record>");
+}
+
+int ws_lambda_infer(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, const uint2* table, uint32_t n, float* lambda, float* density, float* lamTot, const PairList& pl,
+                    const void* mlpBlock, float4* res, Launcher& L) {
+  const MlpDev m = mlp_dev(mlpBlock);
+  L.begin("ws_lambda_mlp");
+  k_ws_lambda<kInfer><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+      g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
+  L.end("ws_lambda_mlp");
+  return check("k_ws_lambda<infer>");
+}
+
+int ws_record_targets(const GridK& g, const FluidK& p, const float4* x0, const float* lamTot, const uint2* table,
+                      uint32_t n, const float4* xFinal, const PairList& pl0, uint32_t stride, uint32_t phase,
+                      uint32_t count, float* targets, Launcher& L) {
+  if (count == 0) return RTP_OK;
+  L.begin("ws_record_targets");
+  k_ws_record_targets<<<blocks(count * kQuad, 128), 128, 0, L.stream>>>(g, p, x0, lamTot, table, n, xFinal, pl0, stride,
+                                                                         phase, count, targets);
+  L.end("ws_record_targets");
+  return check("k_ws_record_targets");
+}
+
+int ws_density_error(const GridK& g, const FluidK& p, const float4* pos, const uint2* table, uint32_t n,
+                     float* errPartial, Launcher& L) {
+  L.begin("ws_density_error");
+  k_ws_density_error<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
+  L.end("ws_density_error");
+  return check("k_ws_density_error");
+}
+
+int ws_guard(const float* errPartial, uint32_t n, float tol, SolverStatsDev* st, cudaGraphConditionalHandle hnd,
+             bool hasCond, bool accept, Launcher& L) {
+  L.begin(accept ? "ws_accept" : "ws_guard");
+  k_ws_guard<<<1, kGuardThreads, 0, L.stream>>>(errPartial, ws_error_blocks(n), n, tol, st, hnd, hasCond ? 1 : 0,
+                                                accept ? 1 : 0);
+  L.end(accept ? "ws_accept" : "ws_guard");
+  return check("k_ws_guard");
+}
+
+}  // namespace rtp

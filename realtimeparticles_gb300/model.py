@@ -279,6 +279,37 @@ class Fluids(Model):
     def setJacobiIterations(self, it):
         call("rtp_set_jacobi_iterations", self._h, int(it))
 
+    # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
+    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):
+        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off."""
+        cfg = abi.WarmStartConfig()
+        cfg.enabled = 0 if net is None else 1
+        cfg.extraIterations = int(extra_iterations)
+        cfg.guardTolerance = float(guard_tolerance)
+        call("rtp_set_warm_start", self._h, None if net is None else C.byref(net), C.byref(cfg))
+
+    def enableSolverStats(self, enable=True):
+        call("rtp_enable_solver_stats", self._h, 1 if enable else 0)
+
+    def solverStats(self):
+        """dict: steps, reruns, mean (accepted solver-output mean |rho/rho0-1| per step),
+        max, mean_first (before reruns)."""
+        st = abi.SolverStats()
+        call("rtp_get_solver_stats", self._h, C.byref(st))
+        k = max(1, st.steps)
+        return {"steps": int(st.steps), "reruns": int(st.reruns), "mean": st.sumDensityError / k,
+                "max": st.maxDensityError, "mean_first": st.sumFirstError / k}
+
+    def resetSolverStats(self):
+        call("rtp_reset_solver_stats", self._h)
+
+    def recordWarmStartSamples(self, reference_iterations, stride, phase, d_features, d_targets, capacity):
+        """One plain step that writes training samples into device memory (pointers)."""
+        w = C.c_uint64()
+        call("rtp_record_warm_start_samples", self._h, int(reference_iterations), int(stride), int(phase),
+             C.c_void_p(d_features), C.c_void_p(d_targets), int(capacity), C.byref(w))
+        return int(w.value)
+
     # Fluids::transferJsonInputsToModel (Fluids.cpp:218-251).
     def transferJsonInputsToModel(self, js):
         f = js["Fluids"]
@@ -337,6 +368,37 @@ class Clouds(Model):
 
     def setJacobiIterations(self, it):
         call("rtp_set_jacobi_iterations", self._h, int(it))
+
+    # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
+    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):
+        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off."""
+        cfg = abi.WarmStartConfig()
+        cfg.enabled = 0 if net is None else 1
+        cfg.extraIterations = int(extra_iterations)
+        cfg.guardTolerance = float(guard_tolerance)
+        call("rtp_set_warm_start", self._h, None if net is None else C.byref(net), C.byref(cfg))
+
+    def enableSolverStats(self, enable=True):
+        call("rtp_enable_solver_stats", self._h, 1 if enable else 0)
+
+    def solverStats(self):
+        """dict: steps, reruns, mean (accepted solver-output mean |rho/rho0-1| per step),
+        max, mean_first (before reruns)."""
+        st = abi.SolverStats()
+        call("rtp_get_solver_stats", self._h, C.byref(st))
+        k = max(1, st.steps)
+        return {"steps": int(st.steps), "reruns": int(st.reruns), "mean": st.sumDensityError / k,
+                "max": st.maxDensityError, "mean_first": st.sumFirstError / k}
+
+    def resetSolverStats(self):
+        call("rtp_reset_solver_stats", self._h)
+
+    def recordWarmStartSamples(self, reference_iterations, stride, phase, d_features, d_targets, capacity):
+        """One plain step that writes training samples into device memory (pointers)."""
+        w = C.c_uint64()
+        call("rtp_record_warm_start_samples", self._h, int(reference_iterations), int(stride), int(phase),
+             C.c_void_p(d_features), C.c_void_p(d_targets), int(capacity), C.byref(w))
+        return int(w.value)
 
     def setEnvironment(self, env, ground=None):
         g = None

@@ -75,3 +75,19 @@ def assert_close_by_id(ids_a, a, ids_b, b, atol, what):
     assert np.all(np.isfinite(A)) and np.all(np.isfinite(B)), what + ": non-finite values"
     assert worst <= atol, "%s: max |diff| %.3g > %.3g" % (what, worst, atol)
     return worst
+
+
+def random_net(rng, scale=0.5, out_scale=None):
+    """A random warm-start network (abi.Mlp) with weights of a trained network's magnitude."""
+    net = abi.Mlp()
+    a = abi.mlp_to_arrays(net)
+    a["inMean"][:] = rng.normal(0, 0.3, 12)
+    a["inScale"][:] = rng.uniform(0.5, 2.0, 12)
+    a["w1"][:] = rng.normal(0, scale, (64, 12))
+    a["b1"][:] = rng.normal(0, 0.1, 64)
+    a["w2"][:] = rng.normal(0, scale / 4, (64, 64))
+    a["b2"][:] = rng.normal(0, 0.1, 64)
+    a["w3"][:] = rng.normal(0, scale / 4, (4, 64))
+    a["b3"][:] = rng.normal(0, 0.1, 4)
+    a["outScale"][:] = rng.uniform(0.5, 2.0, 4) if out_scale is None else out_scale
+    return abi.mlp_from_arrays(a)

@@ -31,7 +31,9 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
     structs = {"rtp_model_params": abi.ModelParams, "rtp_fluid_params": abi.FluidParams,
                "rtp_boids_params": abi.BoidsParams, "rtp_cloud_params": abi.CloudParams,
                "rtp_cloud_env": abi.CloudEnv, "rtp_grid_constants": abi.GridConstants,
-               "rtp_kernel_time": abi.KernelTime, "rtp_metrics": abi.Metrics}
+               "rtp_kernel_time": abi.KernelTime, "rtp_metrics": abi.Metrics, "rtp_mlp": abi.Mlp,
+               "rtp_warm_start_config": abi.WarmStartConfig, "rtp_solver_stats": abi.SolverStats,
+               "rtp_train_config": abi.TrainConfig}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s/include/rtp.h"' % ROOT, "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
