@@ -56,6 +56,10 @@ WORKLOADS = {
                                metric="PBF particle-steps/s @131k (plain, 3 Jacobi iterations)"),
     "pbf_dam_break_16k": dict(kind="fluids", lattice=(16, 32, 32), iters=3,
                               metric="PBF particle-steps/s @16k (plain, 3 Jacobi iterations)"),
+    # 16.7M particles (256^3 lattice, box 6.4 = 256 cells of h per axis): the grid/sort path
+    # at a size where its HBM traffic, not launch latency, sets the time.
+    "pbf_dam_break_16m": dict(kind="fluids", lattice=(256, 256, 256), box=6.4, iters=3, max_steps=10,
+                              metric="PBF particle-steps/s @16.7M (plain, 3 Jacobi iterations)"),
     "boids_131k": dict(kind="boids", n=131072, metric="boids particle-steps/s @131k"),
     "clouds_131k": dict(kind="clouds", n=131072, iters=1, metric="clouds particle-steps/s @131k"),
 }
@@ -65,7 +69,7 @@ def make_model(w):
     """The model of workload w with its seeded inputs uploaded."""
     from realtimeparticles_gb300 import model
     if w["kind"] == "fluids":
-        sc = scenes.dam_break(lattice=w["lattice"])
+        sc = scenes.dam_break(lattice=w["lattice"], box=w.get("box", 1.0))
         m = model.Fluids(sc["model_params"])
         m.setFluidParams(sc["fluid_params"])
         m.setJacobiIterations(w["iters"])
@@ -360,6 +364,31 @@ def warm_start_study(w, steps, warmup):
     return out
 
 
+GRID_SORT_KERNELS = ("fld_predict", "sort_clear", "sort_scan", "sort_pass", "sort_pass_gather", "cellTableClear",
+                     "cellTable")
+
+
+def grid_sort_summary(kt, steps, n, c, nonempty, peak):
+    """HBM roofline of the grid/sort path of the PBF step (predict + cell keys, stable radix
+    sort with the payload gather, cell table): algorithmic bytes of its kernels per step
+    over their summed device time."""
+    passes = max(1, -(-int(c.keyBits) // 9))
+    per_step = {
+        "fld_predict": 52 * n,                                   # pos, vel in; predPos, key out
+        "sort_clear": 0, "sort_scan": 0,                         # sort bookkeeping, not algorithmic
+        "sort_pass": (12 + 16 * max(0, passes - 2)) * n if passes > 1 else 0,  # keys (+ index) in and out
+        "sort_pass_gather": 112 * n,                             # key, index in; key out; 3 float4 + id moved
+        "cellTableClear": 8 * int(c.numCells),                   # the table is written whole
+        "cellTable": 4 * n + 8 * nonempty,                       # sorted keys in; begin/end of each cell
+    }
+    ms = sum(kt[k][1] for k in GRID_SORT_KERNELS if k in kt) / max(1, steps)
+    b = sum(per_step.values())
+    gbs = b / (ms / 1000.0) / 1e9 if ms > 0 else None
+    return {"kernels": [k for k in GRID_SORT_KERNELS if k in kt], "algorithmic_bytes_per_step": b,
+            "ms_per_step": ms, "achieved_gbs": gbs, "peak_gbs": peak, "frac": (gbs / peak) if gbs else None,
+            "sort_passes": passes, "cells": int(c.numCells), "nonempty_cells": nonempty}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -373,6 +402,8 @@ def run_ours(args):
         import torch
         torch.cuda.set_device(local)
     w = WORKLOADS[args.workload]
+    if "max_steps" in w:
+        args.steps = min(args.steps, w["max_steps"])
     m, n = make_model(w)
 
     # Warm-up (graph capture happens here).
@@ -403,6 +434,11 @@ def run_ours(args):
     alg = KERNEL_BYTES.get(dom_name, 0) * n
     achieved = alg / (dom_avg_ms / 1000.0) / 1e9
     share = {k: round(v[1] / sum(x[1] for x in kt.values()), 4) for k, v in kt.items()}
+    grid_sort = None
+    if w["kind"] == "fluids":
+        tab = m.download(abi.BUF_CELL_TABLE)
+        nonempty = int(np.count_nonzero(tab[:, 1] >= tab[:, 0]))
+        grid_sort = grid_sort_summary(kt, args.steps, n, m.constants(), nonempty, peak)
 
     # End to end through the public API with pinned host buffers.
     try:
@@ -452,6 +488,8 @@ def run_ours(args):
             "kernel_share": share,
             "clocks": clk,
         }
+        if grid_sort:
+            out["grid_sort"] = grid_sort
         if metrics is not None:
             out["state_check"] = {"mean_density_error": metrics.meanDensityError,
                                   "kinetic_energy": metrics.kineticEnergy,

@@ -302,7 +302,7 @@ int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_k
  *  - every call shares the array, so calls that overlap on the GPU race: order them on one
  *    stream or synchronise between them. */
 #define RTP_NOALLOC_SORT_MAX_KEYS 262144u
-#define RTP_NOALLOC_SORT_SCRATCH_BYTES 5251072u
+#define RTP_NOALLOC_SORT_SCRATCH_BYTES 5253120u
 int rtp_radix_sort_noalloc(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint32_t* d_keys_out,
                            uint32_t* d_perm_out, void* stream);
 

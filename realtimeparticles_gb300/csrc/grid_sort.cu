@@ -37,11 +37,17 @@ SortPlan make_sort_plan(uint32_t n, uint32_t keyBits) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Tile groups of the two-kernel digit scan (1 = the single-kernel scan).
+static uint32_t scan_groups(uint32_t tiles) {
+  return std::min<uint32_t>(kScanGroupsMax, (tiles + kScanTilesPerGroup - 1) / kScanTilesPerGroup);
+}
+
 size_t sort_scratch_bytes(const SortPlan& p) {
   const size_t nk = align256(sizeof(uint32_t) * (size_t)std::max<uint32_t>(p.n, 1));
   const size_t h = align256(sizeof(uint32_t) * (size_t)p.passes * p.tiles * kMaxBins);
   const size_t t = align256(sizeof(uint32_t) * (size_t)p.passes * kMaxBins);
-  return 4 * nk + h + t;
+  const size_t g = align256(sizeof(uint32_t) * (size_t)scan_groups(p.tiles) * kMaxBins);
+  return 4 * nk + h + t + g;
 }
 
 void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s) {
@@ -58,6 +64,8 @@ void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s) {
   s.hist = (uint32_t*)b;
   b += align256(sizeof(uint32_t) * (size_t)p.passes * p.tiles * kMaxBins);
   s.totals = (uint32_t*)b;
+  b += align256(sizeof(uint32_t) * (size_t)p.passes * kMaxBins);
+  s.scanPart = (uint32_t*)b;
 }
 
 // fillCellIDs (grid.cl:76-86).
@@ -66,9 +74,9 @@ __global__ void k_fill_cell_ids(GridK g, const float4* __restrict__ pos, uint32_
   if (i < n) keys[i] = cell_key(g, ld4(pos + i));
 }
 
-// Digit-0 histogram per tile of externally supplied keys.
-__global__ void __launch_bounds__(kSortThreads) k_sort_hist0(const uint32_t* __restrict__ keys, uint32_t n, int bits,
-                                                             uint32_t* __restrict__ hist0) {
+// Per-tile histogram of the digit at `shift` (pass 0 of externally supplied keys).
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                            int bits, uint32_t* __restrict__ hist) {
   __shared__ uint32_t s_hist[kMaxBins];
   TileHistogram th;
   th.init(s_hist, bits);
@@ -76,13 +84,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_hist0(const uint32_t* __r
 #pragma unroll
   for (int k = 0; k < kSortItems; ++k) {
     const uint32_t e = base + k * kSortThreads + threadIdx.x;
-    if (e < n) th.add(__ldg(keys + e));
+    if (e < n) th.add(__ldg(keys + e) >> shift);
   }
-  th.store(hist0);
+  th.store(hist);
 }
 
 // In-place exclusive scan over tiles of each digit's column; totals[d] = column sum.
 // Block = 8 warps, lane = digit within a group of 32, warp = contiguous range of tiles.
+// Used when the tiles fit one block per digit group (up to kScanTilesPerGroup tiles).
 __global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, uint32_t tiles, int bins,
                                                    uint32_t* __restrict__ totals) {
   __shared__ uint32_t s_part[8][32];
@@ -117,23 +126,121 @@ __global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, 
   }
 }
 
+// Large tile counts: the tiles are split into blockIdx.y groups.  Pass 1 sums each
+// (digit group, tile group) into part[group][digit]; pass 2 starts each group from the sum
+// of the groups before it and scans in place (the last group also writes the totals).
+__device__ __forceinline__ void scan_group_range(uint32_t tiles, uint32_t groups, uint32_t g, uint32_t& t0,
+                                                 uint32_t& t1) {
+  const uint32_t per = (tiles + groups - 1) / groups;
+  t0 = min(tiles, g * per);
+  t1 = min(tiles, t0 + per);
+}
+
+__global__ void __launch_bounds__(256) k_sort_scan_part(const uint32_t* __restrict__ hist, uint32_t tiles, int bins,
+                                                        uint32_t* __restrict__ part) {
+  __shared__ uint32_t s_part[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + lane;
+  uint32_t g0, g1;
+  scan_group_range(tiles, gridDim.y, blockIdx.y, g0, g1);
+  const uint32_t chunk = (g1 - g0 + 7) / 8;
+  const uint32_t t0 = min(g1, g0 + warp * chunk), t1 = min(g1, t0 + chunk);
+  uint32_t sum = 0;
+  if (d < bins)
+    for (uint32_t t = t0; t < t1; ++t) sum += __ldg(hist + (size_t)t * kMaxBins + d);
+  s_part[warp][lane] = sum;
+  __syncthreads();
+  if (warp == 0 && d < bins) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) run += s_part[w][lane];
+    part[(size_t)blockIdx.y * kMaxBins + d] = run;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sort_scan_final(uint32_t* __restrict__ hist, uint32_t tiles, int bins,
+                                                         const uint32_t* __restrict__ part,
+                                                         uint32_t* __restrict__ totals) {
+  __shared__ uint32_t s_part[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + lane;
+  uint32_t g0, g1;
+  scan_group_range(tiles, gridDim.y, blockIdx.y, g0, g1);
+  const uint32_t chunk = (g1 - g0 + 7) / 8;
+  const uint32_t t0 = min(g1, g0 + warp * chunk), t1 = min(g1, t0 + chunk);
+  uint32_t sum = 0;
+  if (d < bins)
+    for (uint32_t t = t0; t < t1; ++t) sum += hist[(size_t)t * kMaxBins + d];
+  s_part[warp][lane] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t run = 0;
+    if (d < bins)
+      for (uint32_t gg = 0; gg < blockIdx.y; ++gg) run += __ldg(part + (size_t)gg * kMaxBins + d);
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      const uint32_t v = s_part[w][lane];
+      s_part[w][lane] = run;
+      run += v;
+    }
+    if (d < bins && blockIdx.y == gridDim.y - 1) totals[d] = run;
+  }
+  __syncthreads();
+  if (d < bins) {
+    uint32_t run = s_part[warp][lane];
+    for (uint32_t t = t0; t < t1; ++t) {
+      const size_t at = (size_t)t * kMaxBins + d;
+      const uint32_t v = hist[at];
+      hist[at] = run;
+      run += v;
+    }
+  }
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
 
+// Exclusive scan of a[2 t], a[2 t + 1] over the block (kSortThreads threads, 2 values per
+// thread): returns the prefixes of both values; s_wsum holds kSortWarps words of scratch.
+__device__ __forceinline__ void block_scan2(uint32_t v0, uint32_t v1, uint32_t* s_wsum, uint32_t& e0, uint32_t& e1) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v0 + v1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_wsum[warp] = x;
+  __syncthreads();
+  uint32_t wpre = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) wpre += (w < warp) ? s_wsum[w] : 0u;
+  e0 = wpre + x - (v0 + v1);
+  e1 = e0 + v0;
+  __syncthreads();  // s_wsum may be reused
+}
+
 // One LSD pass over a tile of kSortTile keys.  hist holds, for this pass, the exclusive
 // prefix over tiles per digit (k_sort_scan); totals the per-digit totals.
+// The tile's keys are ranked stably (warp w owns a contiguous chunk, items in index order),
+// placed in shared memory in tile-local digit order, and written out from there, so that
+// consecutive threads write consecutive addresses of each digit's run.
 template <bool LAST>
 __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ idx_in, uint32_t n, int shift, int bits,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ idx_out, uint32_t* __restrict__ hist_next, int next_shift, int next_bits, GatherList g) {
-  __shared__ uint32_t s_base[kMaxBins];
+  __shared__ uint32_t s_base[kMaxBins];    // global start of (this tile, digit)
+  __shared__ uint32_t s_lstart[kMaxBins];  // tile-local start of each digit
   __shared__ uint32_t s_wc[kSortWarps][kMaxBins];
   __shared__ uint32_t s_wsum[kSortWarps];
+  __shared__ uint32_t s_key[kSortTile];
+  __shared__ uint32_t s_src[kSortTile];
   const int bins = 1 << bits;
+  const uint32_t mask = (uint32_t)(bins - 1);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t tile = blockIdx.x;
 
@@ -142,21 +249,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const int d0 = 2 * tid, d1 = 2 * tid + 1;
     const uint32_t v0 = d0 < bins ? __ldg(totals + d0) : 0u;
     const uint32_t v1 = d1 < bins ? __ldg(totals + d1) : 0u;
-    uint32_t x = v0 + v1;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) s_wsum[warp] = x;
-    __syncthreads();
-    uint32_t wpre = 0;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) wpre += (w < warp) ? s_wsum[w] : 0u;
-    const uint32_t excl = wpre + x - (v0 + v1);
+    uint32_t e0, e1;
+    block_scan2(v0, v1, s_wsum, e0, e1);
     const uint32_t* tp = hist + (size_t)tile * kMaxBins;
-    if (d0 < bins) s_base[d0] = excl + __ldg(tp + d0);
-    if (d1 < bins) s_base[d1] = excl + v0 + __ldg(tp + d1);
+    if (d0 < bins) s_base[d0] = e0 + __ldg(tp + d0);
+    if (d1 < bins) s_base[d1] = e1 + __ldg(tp + d1);
   }
   for (int i = tid; i < kSortWarps * bins; i += kSortThreads) s_wc[i / bins][i % bins] = 0;
   __syncthreads();
@@ -170,7 +267,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const uint32_t e = wbase + k * 32 + lane;
     const bool valid = e < n;
     key[k] = valid ? __ldg(keys_in + e) : 0u;
-    dig[k] = valid ? ((key[k] >> shift) & (uint32_t)(bins - 1)) : 0xFFFFFFFFu;
+    dig[k] = valid ? ((key[k] >> shift) & mask) : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(0xffffffffu, dig[k]);
     uint32_t old = 0;
     if (valid) old = s_wc[warp][dig[k]];
@@ -180,33 +277,60 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     rank[k] = old + __popc(peers & ltmask);
   }
   __syncthreads();
-  for (int d = tid; d < bins; d += kSortThreads) {
-    uint32_t run = 0;
+  // Per digit: exclusive offsets over warps, then the tile-local digit starts.
+  {
+    uint32_t c[2] = {0u, 0u};
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-      const uint32_t t = s_wc[w][d];
-      s_wc[w][d] = run;
-      run += t;
+    for (int q = 0; q < 2; ++q) {
+      const int d = 2 * tid + q;
+      if (d < bins) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+          const uint32_t t = s_wc[w][d];
+          s_wc[w][d] = run;
+          run += t;
+        }
+        c[q] = run;
+      }
+    }
+    uint32_t e0, e1;
+    block_scan2(c[0], c[1], s_wsum, e0, e1);
+    if (2 * tid < bins) s_lstart[2 * tid] = e0;
+    if (2 * tid + 1 < bins) s_lstart[2 * tid + 1] = e1;
+  }
+  __syncthreads();
+  // Place each key (and its source index) at its tile-local sorted slot.
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t e = wbase + k * 32 + lane;
+    if (e < n) {
+      const uint32_t d = dig[k];
+      const uint32_t lp = s_lstart[d] + s_wc[warp][d] + rank[k];
+      s_key[lp] = key[k];
+      s_src[lp] = idx_in ? __ldg(idx_in + e) : e;
     }
   }
   __syncthreads();
 
+  const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
   const uint32_t nmask = (1u << next_bits) - 1u;
-#pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    const uint32_t e = wbase + k * 32 + lane;
-    const bool valid = e < n;
-    uint32_t pos = 0;
+#pragma unroll 2
+  for (int it = 0; it < kSortItems; ++it) {
+    const uint32_t j = it * kSortThreads + tid;
+    const bool valid = j < count;
+    uint32_t kk = 0, pos = 0;
     if (valid) {
-      const uint32_t d = dig[k];
-      pos = s_base[d] + s_wc[warp][d] + rank[k];
+      kk = s_key[j];
+      const uint32_t d = (kk >> shift) & mask;
+      pos = s_base[d] + (j - s_lstart[d]);
     }
     // A consistent histogram gives pos < n; the guard keeps an inconsistent one (a bug)
     // from writing out of bounds: the element is dropped and the parity tests fail.
     const bool ok = valid && pos < n;
     if (ok) {
-      keys_out[pos] = key[k];
-      const uint32_t src = idx_in ? __ldg(idx_in + e) : e;
+      keys_out[pos] = kk;
+      const uint32_t src = s_src[j];
       if (!LAST) {
         idx_out[pos] = src;
       } else {
@@ -217,7 +341,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     }
     if (!LAST) {
       // Next pass's tile histogram, aggregated over lanes hitting the same (tile, digit).
-      const uint32_t slot = ok ? (pos / kSortTile) * kMaxBins + ((key[k] >> next_shift) & nmask) : 0xFFFFFFFFu;
+      const uint32_t slot = ok ? (pos / kSortTile) * kMaxBins + ((kk >> next_shift) & nmask) : 0xFFFFFFFFu;
       const uint32_t peers = __match_any_sync(0xffffffffu, slot);
       if (ok && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
     }
@@ -263,15 +387,17 @@ int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t
 
 int launch_sort_histogram(const SortPlan& p, const uint32_t* keys, const SortScratch& s, Launcher& L) {
   L.begin("sort_hist0");
-  k_sort_hist0<<<p.tiles, kSortThreads, 0, L.stream>>>(keys, p.n, p.bits[0], s.hist);
+  k_sort_hist<<<p.tiles, kSortThreads, 0, L.stream>>>(keys, p.n, 0, p.bits[0], s.hist);
   L.end("sort_hist0");
-  return check_launch("k_sort_hist0");
+  return check_launch("k_sort_hist");
 }
 
 int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L) {
   if (p.passes <= 1) return RTP_OK;
   const size_t per = (size_t)p.tiles * kMaxBins;
+  L.begin("sort_clear");
   RTP_CUDA(cudaMemsetAsync(s.hist + per, 0, sizeof(uint32_t) * per * (p.passes - 1), L.stream));
+  L.end("sort_clear");
   return RTP_OK;
 }
 
@@ -286,8 +412,15 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
     uint32_t* hist = s.hist + per * pass;
     uint32_t* totals = s.totals + (size_t)kMaxBins * pass;
     const int bins = 1 << p.bits[pass];
+    const uint32_t groups = scan_groups(p.tiles);
     L.begin("sort_scan");
-    k_sort_scan<<<(bins + 31) / 32, 256, 0, L.stream>>>(hist, p.tiles, bins, totals);
+    if (groups <= 1) {
+      k_sort_scan<<<(bins + 31) / 32, 256, 0, L.stream>>>(hist, p.tiles, bins, totals);
+    } else {
+      const dim3 grid((bins + 31) / 32, groups);
+      k_sort_scan_part<<<grid, 256, 0, L.stream>>>(hist, p.tiles, bins, s.scanPart);
+      k_sort_scan_final<<<grid, 256, 0, L.stream>>>(hist, p.tiles, bins, s.scanPart, totals);
+    }
     L.end("sort_scan");
     int rc = check_launch("k_sort_scan");
     if (rc) return rc;
@@ -315,7 +448,9 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
 }
 
 int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L) {
+  L.begin("cellTableClear");
   RTP_CUDA(cudaMemsetAsync(table, 0, sizeof(uint2) * g.nc, L.stream));
+  L.end("cellTableClear");
   if (n == 0) return RTP_OK;
   L.begin("cellTable");
   k_cell_table_fill<<<(n + 255) / 256, 256, 0, L.stream>>>(sorted_keys, n, g.nc, table);

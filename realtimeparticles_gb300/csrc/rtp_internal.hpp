@@ -47,9 +47,14 @@ struct SortScratch {
   uint32_t* keysB = nullptr;
   uint32_t* idxA = nullptr;
   uint32_t* idxB = nullptr;
-  uint32_t* hist = nullptr;    // passes x tiles x kMaxBins
-  uint32_t* totals = nullptr;  // passes x kMaxBins
+  uint32_t* hist = nullptr;      // passes x tiles x kMaxBins
+  uint32_t* totals = nullptr;    // passes x kMaxBins
+  uint32_t* scanPart = nullptr;  // tile groups x kMaxBins (two-kernel digit scan)
 };
+// Tile groups of the digit scan: one block column per kScanTilesPerGroup tiles, at most
+// kScanGroupsMax (beyond that the groups grow).
+constexpr uint32_t kScanTilesPerGroup = 128;
+constexpr uint32_t kScanGroupsMax = 64;
 size_t sort_scratch_bytes(const SortPlan& p);
 void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s);
 

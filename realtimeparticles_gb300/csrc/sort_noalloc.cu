@@ -24,10 +24,13 @@ constexpr size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr uint32_t kMaxKeys = RTP_NOALLOC_SORT_MAX_KEYS;
 constexpr uint32_t kMaxTiles = (kMaxKeys + kSortTile - 1) / kSortTile;
 constexpr int kMaxPasses = (32 + kMaxRadixBits - 1) / kMaxRadixBits;
-// Same layout as sort_scratch_bytes(): 4 key/index arrays, per-pass tile histograms, totals.
+// Same layout as sort_scratch_bytes(): 4 key/index arrays, per-pass tile histograms, totals,
+// digit-scan group sums (one group: kMaxTiles <= kScanTilesPerGroup).
+static_assert(kMaxTiles <= kScanTilesPerGroup, "one digit-scan group");
 constexpr size_t kScratchBytes = 4 * al256(sizeof(uint32_t) * (size_t)kMaxKeys) +
                                  al256(sizeof(uint32_t) * (size_t)kMaxPasses * kMaxTiles * kMaxBins) +
-                                 al256(sizeof(uint32_t) * (size_t)kMaxPasses * kMaxBins);
+                                 al256(sizeof(uint32_t) * (size_t)kMaxPasses * kMaxBins) +
+                                 al256(sizeof(uint32_t) * (size_t)kMaxBins);
 static_assert(kScratchBytes == RTP_NOALLOC_SORT_SCRATCH_BYTES, "keep rtp.h in step with the scratch layout");
 
 // The scratch itself: file scope, one copy per device that loads the library.

@@ -48,6 +48,19 @@ def test_radix_sort_is_a_stable_sort(torch, n, bits):
     assert np.array_equal(sk, keys[ref])
 
 
+@pytest.mark.parametrize("n,bits", [(262145, 25), (4194403, 24), (20000003, 25)])
+def test_radix_sort_large_tile_counts(torch, n, bits):
+    """Tile counts that take the grouped digit scan (above 128 tiles), up to more tiles than
+    the 64 groups x 128 tiles the groups start from (20M keys = 9766 tiles)."""
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+    keys[rng.integers(0, n, n // 4)] = keys[1]
+    sk, perm = _sort_gpu(torch, keys, bits)
+    ref = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm, ref)
+    assert np.array_equal(sk, keys[ref])
+
+
 def test_radix_sort_nearly_sorted_cell_keys(torch, oracle_mod):
     # The step's real input: keys of the previous order, slightly perturbed.
     rng = np.random.default_rng(7)
@@ -92,7 +105,7 @@ def test_fill_cell_ids_bit_exact(torch, oracle_mod):
     assert got.max() == c.keyBound - 1
 
 
-@pytest.mark.parametrize("case", ["random", "quirk_first_cell", "capped", "aliased", "single"])
+@pytest.mark.parametrize("case", ["random", "quirk_first_cell", "capped", "aliased", "single", "runs"])
 def test_cell_table_bit_exact(torch, oracle_mod, case):
     c = _consts(res=8)  # 512 cells, cap 100
     rng = np.random.default_rng(5)
@@ -104,6 +117,8 @@ def test_cell_table_bit_exact(torch, oracle_mod, case):
         sk = np.sort(np.concatenate([np.full(350, 17), np.full(101, 40), np.full(102, 41), [0]])).astype(np.uint32)
     elif case == "aliased":
         sk = np.sort(rng.integers(500, c.keyBound, 300)).astype(np.uint32)
+    elif case == "runs":  # runs around the table kernel's 32-particle look-ahead, first and last
+        sk = np.concatenate([np.full(33, 5), np.full(32, 6), np.full(34, 7), [8], np.full(40, 9)]).astype(np.uint32)
     else:
         sk = np.array([77], np.uint32)
     d = torch.from_numpy(sk.view(np.int32)).cuda()
