@@ -400,6 +400,51 @@ int rtp_mlp_loss_grad(const rtp_mlp* net, const float* lossWeights, const float*
 /* Inference kernel of the warm start on stand-alone features: d_out[s][o] = y_so * outScale[o]. */
 int rtp_mlp_forward(const rtp_mlp* net, const float* d_features, uint64_t n, float* d_out, void* stream);
 
+/* ---- Batched scenes and tuning (new: no counterpart in the reference) --------------------
+ * Many independent fluids scenes of uneven sizes stepped together.  Their particles share one
+ * set of device buffers (scene s occupies slots [offset_s, offset_s + nbParticles_s) of every
+ * buffer; rtp_batch_scene_range) and every stage of the step is a single launch over all scenes.
+ * Each scene has its own box (float extents, any aspect) and grid of cells cellFactor * h wide
+ * (rtp_tuning); all share the effect radius h, the fluid parameters, the Jacobi iteration count
+ * and the warm start.  Every scene evolves as the same scene on its own handle would: the
+ * stable sort keeps each scene in its slot range, and each scene's first sorted particle is
+ * left out of its cell as the reference's fillStartCell does.  On a batch handle rtp_reset,
+ * rtp_set_nb_particles and sample recording return RTP_ERR_NOT_SUPPORTED; everything else,
+ * including rtp_upload / rtp_download of whole buffers, works as on a fluids handle. */
+typedef struct rtp_batch_scene {
+  uint64_t nbParticles;
+  float boxSize[3];
+} rtp_batch_scene;
+
+int rtp_create_batch(uint32_t nscenes, const rtp_batch_scene* scenes, float effectRadius,
+                     uint32_t maxNbPartsInCell, void** out_handle);
+int rtp_batch_scene_range(void* handle, uint32_t scene, uint64_t* offset, uint64_t* count);
+/* The scene's own grid constants (cell keys counted from 0 within the scene) and the offset
+ * of its keys in the batch's cell-key space (RTP_BUF_CELL_ID, RTP_BUF_CELL_TABLE). */
+int rtp_batch_scene_constants(void* handle, uint32_t scene, rtp_grid_constants* out);
+int rtp_batch_scene_key_base(void* handle, uint32_t scene, uint32_t* base);
+
+/* Launch shape of a fluids handle: lanes per particle in the sweeps that walk recorded pair
+ * lists (2, 4 or 8; default 4) and, for a batch, the cell size as a multiple of h (>= 1;
+ * default 1; a single scene keeps the reference's grid).  rtp_autotune times every candidate
+ * (lanes x {1, 1.25, 1.5, 2} cell factors for a batch) over `steps` steps, L2 flushed before
+ * each, and keeps the fastest; the simulation advances meanwhile. */
+typedef struct rtp_tuning {
+  uint32_t lanes;
+  float cellFactor;
+} rtp_tuning;
+#define RTP_TUNE_MAX_CANDIDATES 32
+typedef struct rtp_tune_result {
+  rtp_tuning best;
+  double bestMsPerStep;
+  uint32_t tried;
+  rtp_tuning candidates[RTP_TUNE_MAX_CANDIDATES];
+  double msPerStep[RTP_TUNE_MAX_CANDIDATES];
+} rtp_tune_result;
+int rtp_set_tuning(void* handle, const rtp_tuning* t);
+int rtp_get_tuning(void* handle, rtp_tuning* t);
+int rtp_autotune(void* handle, uint32_t steps, rtp_tune_result* out);
+
 #ifdef __cplusplus
 }
 #endif

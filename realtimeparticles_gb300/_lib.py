@@ -78,6 +78,13 @@ _SIGS = {
     "rtp_train_warm_start": [P, P, U64, C.POINTER(abi.TrainConfig), C.POINTER(abi.Mlp), P, P],
     "rtp_mlp_loss_grad": [C.POINTER(abi.Mlp), P, P, P, U64, C.POINTER(C.c_double), C.POINTER(abi.Mlp), P],
     "rtp_mlp_forward": [C.POINTER(abi.Mlp), P, U64, P, P],
+    "rtp_create_batch": [U32, C.POINTER(abi.BatchScene), C.c_float, U32, PP],
+    "rtp_batch_scene_range": [P, U32, C.POINTER(U64), C.POINTER(U64)],
+    "rtp_batch_scene_constants": [P, U32, C.POINTER(abi.GridConstants)],
+    "rtp_batch_scene_key_base": [P, U32, C.POINTER(U32)],
+    "rtp_set_tuning": [P, C.POINTER(abi.Tuning)],
+    "rtp_get_tuning": [P, C.POINTER(abi.Tuning)],
+    "rtp_autotune": [P, U32, C.POINTER(abi.TuneResult)],
 }
 _RESTYPES = {"rtp_last_error": C.c_char_p}
 

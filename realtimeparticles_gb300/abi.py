@@ -162,6 +162,27 @@ class Metrics(C.Structure):
     ]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("nbParticles", C.c_uint64), ("boxSize", C.c_float * 3)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("lanes", C.c_uint32), ("cellFactor", C.c_float)]
+
+
+TUNE_MAX_CANDIDATES = 32
+
+
+class TuneResult(C.Structure):
+    _fields_ = [
+        ("best", Tuning),
+        ("bestMsPerStep", C.c_double),
+        ("tried", C.c_uint32),
+        ("candidates", Tuning * TUNE_MAX_CANDIDATES),
+        ("msPerStep", C.c_double * TUNE_MAX_CANDIDATES),
+    ]
+
+
 MLP_IN = 12
 MLP_HIDDEN = 64
 MLP_OUT = 4

@@ -25,20 +25,24 @@ namespace rtp {
 
 // fld_predictPosition (fluids.cl:62-74) + fillCellIDs (grid.cl:76-86) + digit-0 histogram.
 // Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
-__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK p, const float4* __restrict__ pos,
+template <bool BATCH>
+__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK p0, const float4* __restrict__ pos,
                                                                 const float4* __restrict__ vel, uint32_t n,
                                                                 float4* __restrict__ pred, uint32_t* __restrict__ keys,
                                                                 int bits0, uint32_t* __restrict__ hist0, int clampOut) {
   __shared__ uint32_t s_hist[kMaxBins];
   TileHistogram th;
   th.init(s_hist, bits0);
-  const float dt = p.dt;
+  const float dt = p0.dt;
   const float gx = __fmul_rn(0.0f, dt), gy = __fmul_rn(-kAbsGravityY, dt);
   const uint32_t base = blockIdx.x * kSortTile;
 #pragma unroll 2
   for (int k = 0; k < kSortItems; ++k) {
     const uint32_t i = base + k * kSortThreads + threadIdx.x;
     if (i < n) {
+      GridK g = g0;
+      FluidK p = p0;
+      scene_of<BATCH>(i, g, p);
       const float4 x = ld4(pos + i), v = ld4(vel + i);
       const float4 nv = f4(__fadd_rn(v.x, gx), __fadd_rn(v.y, gy), __fadd_rn(v.z, gx), __fadd_rn(v.w, gx));
       const float4 pp = f4(__fadd_rn(x.x, __fmul_rn(nv.x, dt)), __fadd_rn(x.y, __fmul_rn(nv.y, dt)),
@@ -59,6 +63,7 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g, FluidK 
 // the pairs within h for k_fluid_deltap.  One thread per particle: a filter pass over the
 // 27 cells writes the pairs within h to the device list (kept for k_fluid_deltap), then
 // the SPH terms are summed over that list.
+template <bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
@@ -66,6 +71,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, Flu
                                                                 float* __restrict__ lamTot, int totMode) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  scene_of<BATCH>(i, g, p);
   const Sph k(g);
   const float4 xi = ld4(pred + i);
   uint32_t cnt = 0;
@@ -107,25 +113,26 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, Flu
 }
 
 // fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
-// LAST adds fld_updateVel (fluids.cl:263-273).  kQuad lanes per particle.  Input positions
+// LAST adds fld_updateVel (fluids.cl:263-273).  LANES lanes per particle.  Input positions
 // are already clamped by fld_applyBoundaryCondition (done by their producer).
-template <bool LAST>
+template <bool LAST, bool BATCH, int LANES>
 __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut,
                                                       const float4* __restrict__ posS, float4* __restrict__ velS,
                                                       PairList pl, const float4* __restrict__ res) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t i = t / kQuad, q = t % kQuad;
+  const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
   float cx = 0.0f, cy = 0.0f, cz = 0.0f;
   float4 xi = f4(0.f, 0.f, 0.f, 0.f);
   if (active) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     xi = ld4(pred + i);  // clamped by the producer
     const float li = __ldg(lambda + i);
     auto ld = [&](uint32_t j) { return Pair4{ld4(pred + j), __ldg(lambda + j)}; };
-    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair4 a) {
+    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair4 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
@@ -141,9 +148,9 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
       }
     });
   }
-  cx = quad_sum(cx);
-  cy = quad_sum(cy);
-  cz = quad_sum(cz);
+  cx = quad_sum<LANES>(cx);
+  cy = quad_sum<LANES>(cy);
+  cz = quad_sum<LANES>(cz);
   if (!active || q != 0) return;
   float4 out = f4(xi.x + cx * p.invRho0, xi.y + cy * p.invRho0, xi.z + cz * p.invRho0, xi.w);
   if (res) {  // warm start: the network's residual displacement
@@ -165,10 +172,12 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
 }
 
 // fld_updateVel alone (only used when the solver runs zero iterations).
+template <bool BATCH>
 __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ posS,
                                    uint32_t n, float4* __restrict__ velS) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  scene_of<BATCH>(i, g, p);
   const float4 a = ld4(pred + i), b = ld4(posS + i);
   const float d = p.dt + kFloatEps;
   velS[i] = clamp4s(f4(__fdiv_rn(a.x - b.x, d), __fdiv_rn(a.y - b.y, d), __fdiv_rn(a.z - b.z, d), __fdiv_rn(a.w - b.w, d)),
@@ -179,7 +188,7 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
 // positions for confinement and XSPH (same two-phase scheme as k_fluid_lambda).
 // GUARD also evaluates fld_computeDensity at those positions and writes each block's sum
 // of |rho_i / rho0 - 1| to errPartial[blockIdx.x] (warm-start guard, solver statistics).
-template <bool GUARD>
+template <bool GUARD, bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                     const float4* __restrict__ velS,
                                                                     const uint2* __restrict__ table, uint32_t n,
@@ -188,6 +197,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, 
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
   if (i < n) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     const float4 xi = ld4(pred + i), vi = ld4(velS + i);
     uint32_t cnt = 0;
@@ -220,19 +230,21 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, 
   if (GUARD) block_error_partial(err, errPartial);
 }
 
-// fld_applyVorticityConfinement (fluids.cl:329-377), kQuad lanes per particle.
+// fld_applyVorticityConfinement (fluids.cl:329-377), LANES lanes per particle.
+template <bool BATCH, int LANES>
 __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
                                                        uint32_t n, float4* __restrict__ velS, PairList pl) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t i = t / kQuad, q = t % kQuad;
+  const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
   float ex = 0.0f, ey = 0.0f, ez = 0.0f;
   if (active) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     const float4 xi = ld4(pred + i);
     auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(vort + j)}; };
-    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
@@ -247,9 +259,9 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
       }
     });
   }
-  ex = quad_sum(ex);
-  ey = quad_sum(ey);
-  ez = quad_sum(ez);
+  ex = quad_sum<LANES>(ex);
+  ey = quad_sum<LANES>(ey);
+  ez = quad_sum<LANES>(ez);
   if (!active || q != 0) return;
   const float4 c = cross4(normalize0(f4(ex, ey, ez, 0.0f)), ld4(vort + i));
   const float s = p.vortCoeff * p.dt;
@@ -261,7 +273,8 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
 }
 
 // fld_applyXsphViscosityCorrection (fluids.cl:383-430) + fld_updatePosition (:444-450),
-// writing the canonical state buffers.  kQuad lanes per particle.
+// writing the canonical state buffers.  LANES lanes per particle.
+template <bool BATCH, int LANES>
 __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, const float4* __restrict__ pred,
                                                           const float4* __restrict__ velS,
                                                           const uint2* __restrict__ table, uint32_t n,
@@ -269,16 +282,17 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
                                                           float4* __restrict__ vel, uint32_t* __restrict__ ids,
                                                           PairList pl) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t i = t / kQuad, q = t % kQuad;
+  const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
   float ax = 0.0f, ay = 0.0f, az = 0.0f, aw = 0.0f;
   float4 xi = f4(0.f, 0.f, 0.f, 0.f), vi = xi;
   if (active) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     xi = ld4(pred + i);
     vi = ld4(velS + i);
     auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
-    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
@@ -292,10 +306,10 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
       }
     });
   }
-  ax = quad_sum(ax);
-  ay = quad_sum(ay);
-  az = quad_sum(az);
-  aw = quad_sum(aw);
+  ax = quad_sum<LANES>(ax);
+  ay = quad_sum<LANES>(ay);
+  az = quad_sum<LANES>(az);
+  aw = quad_sum<LANES>(aw);
   if (!active || q != 0) return;
   vel[i] = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
   pos[i] = xi;
@@ -315,6 +329,7 @@ __global__ void k_fluid_final(const float4* __restrict__ pred, const float4* __r
 
 // Step metrics: density (as fld_computeDensity) at the current positions with the step's
 // table, neighbour counts, kinetic energy.
+template <bool BATCH>
 __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const float4* __restrict__ pos,
                                                        const float4* __restrict__ vel, const uint2* __restrict__ table,
                                                        uint32_t n, double* __restrict__ acc, uint32_t* __restrict__ hist) {
@@ -324,6 +339,7 @@ __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const 
   double err = 0.0, ke = 0.0, nb = 0.0, comp = 0.0;
   float mx = 0.0f;
   if (i < n) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     const float4 xi = ld4(pos + i);
     float rho = 0.0f;
@@ -383,8 +399,12 @@ static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; 
 int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L) {
   L.begin("fld_predict");
-  k_fluid_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
-                                                                  clampOut ? 1 : 0);
+  if (p.bt.scenes)
+    k_fluid_predict<true><<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
+                                                                     clampOut ? 1 : 0);
+  else
+    k_fluid_predict<false><<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0],
+                                                                      hist0, clampOut ? 1 : 0);
   L.end("fld_predict");
   return check("k_fluid_predict");
 }
@@ -393,8 +413,12 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
                     float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
                     Launcher& L, float* lamTot, int totMode) {
   L.begin("fld_lambda");
-  k_fluid_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl,
-                                                                           lamTot, totMode);
+  if (p.bt.scenes)
+    k_fluid_lambda<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda,
+                                                                                   density, pl, lamTot, totMode);
+  else
+    k_fluid_lambda<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda,
+                                                                                    density, pl, lamTot, totMode);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
   if (rc) return rc;
@@ -404,24 +428,28 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
 int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
                  const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
                  const float4* res, Launcher& L) {
-  if (last) {
-    L.begin("fld_deltap_vel");
-    k_fluid_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS,
-                                                                        velS, pl, res);
-    L.end("fld_deltap_vel");
-  } else {
-    L.begin("fld_deltap");
-    k_fluid_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, posS,
-                                                                         velS, pl, res);
-    L.end("fld_deltap");
-  }
+  L.begin(last ? "fld_deltap_vel" : "fld_deltap");
+  dispatch_fluid(p, [&](auto B, auto LN) {
+    constexpr bool BATCH = decltype(B)::value;
+    constexpr int LANES = decltype(LN)::value;
+    if (last)
+      k_fluid_deltap<true, BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(
+          g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
+    else
+      k_fluid_deltap<false, BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(
+          g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
+  });
+  L.end(last ? "fld_deltap_vel" : "fld_deltap");
   return check("k_fluid_deltap");
 }
 
 int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const float4* posS, uint32_t n, float4* velS,
                      Launcher& L) {
   L.begin("fld_updateVel");
-  k_fluid_update_vel<<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
+  if (p.bt.scenes)
+    k_fluid_update_vel<true><<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
+  else
+    k_fluid_update_vel<false><<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
   L.end("fld_updateVel");
   return check("k_fluid_update_vel");
 }
@@ -429,12 +457,20 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
 int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
                     const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L) {
   L.begin("fld_vorticity");
-  if (errPartial)
-    k_fluid_vorticity<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort,
-                                                                                      pl, errPartial);
-  else
-    k_fluid_vorticity<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort,
-                                                                                       pl, nullptr);
+  const uint32_t nb = blocks(n, kSweepThreads);
+  if (p.bt.scenes) {
+    if (errPartial)
+      k_fluid_vorticity<true, true><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl, errPartial);
+    else
+      k_fluid_vorticity<false, true><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl, nullptr);
+  } else {
+    if (errPartial)
+      k_fluid_vorticity<true, false><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl,
+                                                                         errPartial);
+    else
+      k_fluid_vorticity<false, false><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl,
+                                                                          nullptr);
+  }
   L.end("fld_vorticity");
   return check("k_fluid_vorticity");
 }
@@ -449,12 +485,21 @@ int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS
       if (rc) return rc;
     }
     L.begin("fld_confine");
-    k_fluid_confine<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
+    dispatch_fluid(p, [&](auto B, auto LN) {
+      constexpr bool BATCH = decltype(B)::value;
+      constexpr int LANES = decltype(LN)::value;
+      k_fluid_confine<BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
+    });
     L.end("fld_confine");
     rc = check("k_fluid_confine");
     if (rc) return rc;
     L.begin("fld_xsph_final");
-    k_fluid_xsph_final<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS, pos, vel, ids, pl);
+    dispatch_fluid(p, [&](auto B, auto LN) {
+      constexpr bool BATCH = decltype(B)::value;
+      constexpr int LANES = decltype(LN)::value;
+      k_fluid_xsph_final<BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS,
+                                                                                      pos, vel, ids, pl);
+    });
     L.end("fld_xsph_final");
     return check("k_fluid_xsph_final");
   }
@@ -468,7 +513,10 @@ int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const floa
                   double* acc, uint32_t* hist, Launcher& L) {
   if (n == 0) return RTP_OK;
   L.begin("fld_metrics");
-  k_fluid_metrics<<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
+  if (p.bt.scenes)
+    k_fluid_metrics<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
+  else
+    k_fluid_metrics<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
   L.end("fld_metrics");
   return check("k_fluid_metrics");
 }

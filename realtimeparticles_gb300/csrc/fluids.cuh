@@ -4,6 +4,8 @@
 #include "rtp_internal.hpp"
 #include "sweep.cuh"
 
+#include <type_traits>
+
 namespace rtp {
 
 // FluidParams (kernels/define.cl:13-25) with the derived values the kernels use.
@@ -17,12 +19,44 @@ struct FluidK {
   int vorticity;
   float vortCoeff;
   float xsph;
+  BatchK bt;        // batched scenes (bt.scenes == nullptr: one scene, the fields above)
+  int lanes = 4;    // lanes per particle of the list sweeps: 2, 4 or 8
 };
 
 FluidK make_fluidk(const rtp_grid_constants& c, const rtp_fluid_params& p);
 
 #ifdef __CUDACC__
 __device__ __forceinline__ float4 bc_clamp(const FluidK& p, float4 x) { return clamp4(x, p.lo, p.hi); }
+
+// Parameters of particle slot i: the kernel's own (one scene) or its scene's (batch).
+template <bool BATCH>
+__device__ __forceinline__ void scene_of(uint32_t i, GridK& g, FluidK& p) {
+  if constexpr (BATCH) {
+    const SceneK* sc = p.bt.scenes + __ldg(p.bt.sceneOf + i);
+    g = sc->g;
+    p.lo = sc->lo;
+    p.hi = sc->hi;
+  }
+}
+
+// Calls f(std::integral_constant<bool, batch>, std::integral_constant<int, lanes>) for the
+// batch mode and lane count of p.
+template <class F>
+inline void dispatch_fluid(const FluidK& p, F&& f) {
+  using T = std::true_type;
+  using N = std::false_type;
+  const bool b = p.bt.scenes != nullptr;
+  switch (p.lanes) {
+    case 2:
+      b ? f(T{}, std::integral_constant<int, 2>{}) : f(N{}, std::integral_constant<int, 2>{});
+      break;
+    case 8:
+      b ? f(T{}, std::integral_constant<int, 8>{}) : f(N{}, std::integral_constant<int, 8>{});
+      break;
+    default:
+      b ? f(T{}, std::integral_constant<int, 4>{}) : f(N{}, std::integral_constant<int, 4>{});
+  }
+}
 
 // Operands of one pair loaded ahead of use: a position and a scalar, or two float4.
 struct Pair4 {

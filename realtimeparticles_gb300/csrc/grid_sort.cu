@@ -349,13 +349,18 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
 }
 
 // Cell table fill (grid.cl:91-138) in the [begin, endExcl) encoding; the table was zeroed.
-__global__ void k_cell_table_fill(const uint32_t* __restrict__ sk, uint32_t n, uint32_t nc, uint2* __restrict__ table) {
+// fillStartCell skips ID 0, so the reset value start = 1 stays for that cell: the first
+// sorted particle begins its cell at index 1.  In a batch (sceneOf != nullptr) that holds
+// for the first slot of every scene.
+__global__ void k_cell_table_fill(const uint32_t* __restrict__ sk, uint32_t n, uint32_t nc, uint2* __restrict__ table,
+                                  const uint16_t* __restrict__ sceneOf) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t k = __ldg(sk + i);
   if (k >= nc) return;
   uint32_t* t = reinterpret_cast<uint32_t*>(table + k);
-  if (i == 0) t[0] = 1u;  // fillStartCell skips ID 0: the reset value start = 1 stays
+  const bool sceneFirst = i == 0 || (sceneOf && __ldg(sceneOf + i - 1) != __ldg(sceneOf + i));
+  if (sceneFirst) t[0] = i + 1u;
   else if (__ldg(sk + i - 1) != k) t[0] = i;
   const uint32_t right = (i + 1 < n) ? __ldg(sk + i + 1) : 0xFFFFFFFFu;
   if (right != k) t[1] = i + 1;
@@ -447,13 +452,14 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
   return RTP_OK;
 }
 
-int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L) {
+int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L,
+                      const uint16_t* sceneOf) {
   L.begin("cellTableClear");
   RTP_CUDA(cudaMemsetAsync(table, 0, sizeof(uint2) * g.nc, L.stream));
   L.end("cellTableClear");
   if (n == 0) return RTP_OK;
   L.begin("cellTable");
-  k_cell_table_fill<<<(n + 255) / 256, 256, 0, L.stream>>>(sorted_keys, n, g.nc, table);
+  k_cell_table_fill<<<(n + 255) / 256, 256, 0, L.stream>>>(sorted_keys, n, g.nc, table, sceneOf);
   L.end("cellTable");
   return check_launch("k_cell_table_fill");
 }

@@ -29,6 +29,7 @@ struct GridK {
   float poly6;     // POLY6_COEFF
   float spiky;     // SPIKY_COEFF
   float maxVel;    // MAX_VEL
+  uint32_t base;   // first key / table entry of this grid (0; scene offset in a batch)
 };
 
 inline GridK make_gridk(const rtp_grid_constants& c) {
@@ -45,6 +46,7 @@ inline GridK make_gridk(const rtp_grid_constants& c) {
   g.poly6 = c.poly6Coeff;
   g.spiky = c.spikyCoeff;
   g.maxVel = c.maxVel;
+  g.base = 0;
   return g;
 }
 
@@ -59,12 +61,24 @@ __device__ __forceinline__ void cell3(const GridK& g, float4 p, int& cx, int& cy
   cz = (int)(uint32_t)floorf(__fdiv_rn(qz, g.cell));
 }
 
-// getCell1DIndexFromPos (grid.cl:29-38).
+// getCell1DIndexFromPos (grid.cl:29-38), offset by the grid's base key.
 __device__ __forceinline__ uint32_t cell_key(const GridK& g, float4 p) {
   int cx, cy, cz;
   cell3(g, p, cx, cy, cz);
-  return (uint32_t)cx * (uint32_t)g.R[2] * (uint32_t)g.R[1] + (uint32_t)cy * (uint32_t)g.R[2] + (uint32_t)cz;
+  return g.base + ((uint32_t)cx * (uint32_t)g.R[2] * (uint32_t)g.R[1] + (uint32_t)cy * (uint32_t)g.R[2] + (uint32_t)cz);
 }
+
+// Batched scenes: each scene's own grid and wall-clamp bounds, and the scene of every
+// particle slot (scenes occupy fixed contiguous slot ranges; the global sort keeps them so,
+// because scene s's keys lie in [base_s, base_s + keyBound_s), below scene s + 1's).
+struct SceneK {
+  GridK g;
+  float4 lo, hi;  // fld_applyBoundaryCondition bounds of the scene
+};
+struct BatchK {
+  const SceneK* scenes = nullptr;  // nullptr: a single scene, parameters from the kernel arguments
+  const uint16_t* sceneOf = nullptr;
+};
 
 // Cell table entry as stored on the device: [begin, endExcl).  Empty cells are (0, 0) so a
 // memset clears the table.  The reference stores (start, end) inclusive with (1, 0) for

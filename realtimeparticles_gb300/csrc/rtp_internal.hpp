@@ -80,8 +80,10 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
 // Zero the histogram area (the first pass reads it after the producer kernel filled it).
 int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L);
 
-// Cell table in the internal [begin, endExcl) encoding from sorted keys.
-int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L);
+// Cell table in the internal [begin, endExcl) encoding from sorted keys (sceneOf: the scene
+// of every slot of a batch, or nullptr).
+int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L,
+                      const uint16_t* sceneOf = nullptr);
 // Internal encoding -> the reference's inclusive (start, end) with (1, 0) for empty cells.
 int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L);
 int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L);

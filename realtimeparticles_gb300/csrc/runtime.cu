@@ -188,7 +188,34 @@ struct Handle {
   SolverStatsDev* solverStats = nullptr;
   PairList pairsRec{};         // pairs at the predicted positions while recording samples
   cudaStream_t stream2 = nullptr;  // captures the guard's rerun body
+
+  // Tuning (fluids): lanes per particle of the list sweeps; batch cell size = cellFactor * h.
+  uint32_t lanes = 4;
+  float cellFactor = 1.0f;
+
+  // Batched scenes (fluids): scene s owns slots [sceneOff[s], sceneOff[s] + desc[s].nbParticles).
+  bool isBatch = false;
+  float batchH = 0.0f;
+  std::vector<rtp_batch_scene> sceneDesc;
+  std::vector<uint64_t> sceneOff;
+  std::vector<SceneK> hScenes;
+  std::vector<rtp_grid_constants> sceneConst;  // each scene's own grid (keys without the base)
+  SceneK* dScenes = nullptr;
+  uint16_t* dSceneOf = nullptr;
+  uint32_t tableCells = 0;  // cells the table was allocated for
+  uint32_t sortKeyBits = 0; // key bits the sort scratch was allocated for
 };
+
+// The fluids parameters a step's kernels get: shared values, tuning and the batch tables.
+static FluidK fluidk_of(const Handle* h) {
+  FluidK k = make_fluidk(h->gc, h->fp);
+  k.lanes = (int)h->lanes;
+  if (h->isBatch) {
+    k.bt.scenes = h->dScenes;
+    k.bt.sceneOf = h->dSceneOf;
+  }
+  return k;
+}
 
 int Launcher::begin(const char* name) {
   if (!profiling || !owner) return RTP_OK;
@@ -272,6 +299,8 @@ static int alloc_buffers(Handle* h) {
     RTP_TRY(dalloc(h, &h->lapT, M));
     RTP_TRY(dalloc(h, &h->lamT, M));
   }
+  h->tableCells = h->gc.numCells;
+  h->sortKeyBits = h->gc.keyBits;
   const SortPlan full = make_sort_plan((uint32_t)M, h->gc.keyBits);
   const size_t sb = sort_scratch_bytes(full);
   RTP_CUDA(cudaMalloc(&h->sortMem, sb));
@@ -353,7 +382,7 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
   gl.dst1[0] = h->idsS;
   gl.n1 = 1;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
-  return launch_cell_table(g, h->cellId, n, h->table, L);
+  return launch_cell_table(g, h->cellId, n, h->table, L, h->isBatch ? h->dSceneOf : nullptr);
 }
 
 // `count` plain Jacobi iterations from `in`; the outputs alternate between dest and spare
@@ -393,7 +422,7 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   if (n == 0) return RTP_OK;
   if (h->wsOn) return record_fluids_ws_step(h, L);
   const GridK& g = h->g;
-  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const FluidK fk = fluidk_of(h);
   RTP_TRY(fluids_presort(h, L, fk, h->iters > 0));
   // Fluids.cpp:427-442.
   float4* cur = h->predA;
@@ -421,7 +450,7 @@ static int record_fluids_step(Handle* h, Launcher& L) {
 static int record_fluids_ws_step(Handle* h, Launcher& L) {
   const uint32_t n = (uint32_t)h->curN;
   const GridK& g = h->g;
-  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const FluidK fk = fluidk_of(h);
   RTP_TRY(fluids_presort(h, L, fk, true));
   RTP_TRY(ws_lambda_infer(g, fk, h->predA, h->velS, h->table, n, h->lambda, h->density, h->lamTot,
                           h->pairs, h->mlpBlock, h->wsRes, L));
@@ -490,7 +519,7 @@ static int record_sample_step(Handle* h, uint32_t iters, uint32_t stride, uint32
                               uint32_t count) {
   const uint32_t n = (uint32_t)h->curN;
   const GridK& g = h->g;
-  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const FluidK fk = fluidk_of(h);
   Launcher L;
   L.stream = h->stream;
   RTP_TRY(fluids_presort(h, L, fk, true));
@@ -568,7 +597,7 @@ int record_clouds_step(Handle* h, Launcher& L) {
   const uint32_t n = (uint32_t)h->curN;
   if (n == 0) return RTP_OK;
   const GridK& g = h->g;
-  const FluidK fk = make_fluidk(h->gc, h->fp);
+  const FluidK fk = fluidk_of(h);
   const CloudK ck = make_cloudk(h);
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   RTP_TRY(launch_sort_clear(plan, h->ss, L));
@@ -750,6 +779,83 @@ static int init_case(Handle* h) {
   }
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   h->hasStep = false;
+  return RTP_OK;
+}
+
+// ---- batched scenes ----------------------------------------------------------------------
+// Scene grids for cell size cellFactor * h: R_a = ceil(box_a / cell) (at least 3, so the 27
+// cells around a particle are distinct), keys as getCell1DIndexFromPos (grid.cl:29-38) offset
+// by base_s = sum of the key bounds of the scenes before s (the +W alias keys stay inside a
+// scene's own range).  Fills h->hScenes, h->sceneConst and the handle's global constants.
+static int batch_grids(Handle* h, float cellFactor) {
+  const float H = h->batchH;
+  const float cell = round_trip(H * cellFactor);
+  rtp_grid_constants base{};
+  {
+    rtp_model_params mp{};
+    mp.currNbParticles = mp.maxNbParticles = 1;
+    for (int a = 0; a < 3; ++a) {
+      mp.boxSize[a] = H * 4.0f;
+      mp.gridRes[a] = 4;
+    }
+    mp.dimension = 3;
+    mp.maxNbPartsInCell = h->mp.maxNbPartsInCell;
+    RTP_TRY(derive_constants(RTP_MODEL_FLUIDS, &mp, &base));  // h-derived constants (poly6, spiky, ...)
+  }
+  uint64_t keyBase = 0;
+  h->hScenes.assign(h->sceneDesc.size(), SceneK{});
+  h->sceneConst.assign(h->sceneDesc.size(), rtp_grid_constants{});
+  for (size_t s = 0; s < h->sceneDesc.size(); ++s) {
+    rtp_grid_constants c = base;
+    for (int a = 0; a < 3; ++a) {
+      const float L = h->sceneDesc[s].boxSize[a];
+      c.absWall[a] = round_trip(L / 2.0f);
+      const double r = std::ceil((double)L / (double)cell - 1e-6);
+      c.gridRes[a] = (uint32_t)std::max(3.0, r);
+    }
+    c.cellSize = cell;
+    c.effectRadius = base.effectRadius;
+    const uint64_t nc = (uint64_t)c.gridRes[0] * c.gridRes[1] * c.gridRes[2];
+    uint32_t top[3];
+    for (int a = 0; a < 3; ++a) {
+      const float q = std::fmin(std::fmax(c.absWall[a], -c.absWall[a]), c.absWall[a]) + c.absWall[a];
+      top[a] = (uint32_t)std::floor(q / c.cellSize);
+    }
+    const uint64_t kb = (uint64_t)top[0] * c.gridRes[2] * c.gridRes[1] + (uint64_t)top[1] * c.gridRes[2] + top[2] + 1;
+    if (nc > (1ull << 30) || kb > (1ull << 30)) return fail(RTP_ERR_INVALID_ARGUMENT, "batch scene grid too large");
+    c.numCells = (uint32_t)nc;
+    c.keyBound = (uint32_t)kb;
+    uint32_t bits = 0;
+    while (bits < 32 && ((uint64_t)1 << bits) < kb) ++bits;
+    c.keyBits = bits;
+    h->sceneConst[s] = c;
+    SceneK& sk = h->hScenes[s];
+    sk.g = make_gridk(c);
+    sk.g.base = (uint32_t)keyBase;
+    sk.lo = make_float4(-c.absWall[0] + 0.01f, -c.absWall[1] + 0.01f, -c.absWall[2] + 0.01f, 0.0f);
+    sk.hi = make_float4(c.absWall[0] - 0.1f, c.absWall[1] - 0.1f, c.absWall[2] - 0.1f, 0.0f);
+    keyBase += kb;
+    if (keyBase > (1ull << 31)) return fail(RTP_ERR_INVALID_ARGUMENT, "batch: too many cells");
+  }
+  rtp_grid_constants g = base;
+  g.absWall[0] = g.absWall[1] = g.absWall[2] = 0.0f;
+  g.gridRes[0] = g.gridRes[1] = g.gridRes[2] = 0;
+  g.cellSize = cell;
+  g.numCells = (uint32_t)keyBase;  // the global table: every scene's key range
+  g.keyBound = (uint32_t)keyBase;
+  uint32_t bits = 0;
+  while (bits < 32 && ((uint64_t)1 << bits) < keyBase) ++bits;
+  g.keyBits = bits;
+  h->gc = g;
+  h->g = make_gridk(g);
+  h->cellFactor = cellFactor;
+  return RTP_OK;
+}
+
+static int batch_upload_scenes(Handle* h) {
+  RTP_CUDA(cudaMemcpyAsync(h->dScenes, h->hScenes.data(), sizeof(SceneK) * h->hScenes.size(), cudaMemcpyHostToDevice,
+                           h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
   return RTP_OK;
 }
 
@@ -979,6 +1085,7 @@ int rtp_reset(void* handle) {
   RTP_GUARD_BEGIN
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: null handle");
   Handle* h = H(handle);
+  if (h->isBatch) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_reset: a batch has no preset cases (upload positions)");
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   rtp_fluid_params_default(&h->fp);
   rtp_boids_params_default(&h->bp);
@@ -1072,6 +1179,7 @@ int rtp_set_cloud_environment(void* handle, const rtp_cloud_env* env, const floa
 
 int rtp_set_nb_particles(void* handle, uint64_t n) {
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  if (H(handle)->isBatch) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_nb_particles: scene sizes of a batch are fixed");
   if (n > H(handle)->maxN) return fail(RTP_ERR_CAPACITY, "rtp_set_nb_particles: n > maxNbParticles");
   H(handle)->curN = n;
   invalidate(H(handle));
@@ -1276,9 +1384,7 @@ int rtp_get_metrics(void* handle, rtp_metrics* out) {
   RTP_CUDA(cudaMemsetAsync(h->mHist, 0, sizeof(uint32_t) * 80, h->stream));
   Launcher L;
   L.stream = h->stream;
-  rtp_fluid_params fp = h->fp;
-  if (h->model == RTP_MODEL_CLOUDS) fp.restDensity = h->fp.restDensity;
-  RTP_TRY(fluid_metrics(h->g, make_fluidk(h->gc, fp), h->predFinal, h->vel, h->table, n, h->mAcc, h->mHist, L));
+  RTP_TRY(fluid_metrics(h->g, fluidk_of(h), h->predFinal, h->vel, h->table, n, h->mAcc, h->mHist, L));
   if (h->pairs.count) RTP_TRY(pair_list_stats(h->pairs, n, h->mHist + 70, L));
   double acc[4];
   uint32_t hist[80];
@@ -1372,7 +1478,8 @@ int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, ui
   if (!handle || !written) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: null argument");
   *written = 0;
   Handle* h = H(handle);
-  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_record_warm_start_samples: fluids only");
+  if (h->model != RTP_MODEL_FLUIDS || h->isBatch)
+    return fail(RTP_ERR_NOT_SUPPORTED, "rtp_record_warm_start_samples: single fluids scenes only");
   if (referenceIterations == 0 || referenceIterations > 64)
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: referenceIterations must be in [1, 64]");
   if (stride == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_record_warm_start_samples: stride must be > 0");
@@ -1387,6 +1494,184 @@ int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, ui
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   h->hasStep = true;
   *written = count;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_create_batch(uint32_t nscenes, const rtp_batch_scene* scenes, float effectRadius, uint32_t maxNbPartsInCell,
+                     void** out_handle) {
+  RTP_GUARD_BEGIN
+  if (!scenes || !out_handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: null argument");
+  *out_handle = nullptr;
+  if (nscenes == 0 || nscenes > 65535) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: 1 to 65535 scenes");
+  if (!(effectRadius > 0.0f)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: effectRadius must be > 0");
+  uint64_t total = 0;
+  for (uint32_t s = 0; s < nscenes; ++s) {
+    if (scenes[s].nbParticles == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: empty scene");
+    for (int a = 0; a < 3; ++a)
+      if (!(scenes[s].boxSize[a] > 0.0f)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: empty box");
+    total += scenes[s].nbParticles;
+  }
+  if (total > (1ull << 28)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create_batch: more than 2^28 particles");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(RTP_ERR_NO_DEVICE, "rtp_create_batch: no CUDA device");
+  }
+  Handle* h = new Handle();
+  h->model = RTP_MODEL_FLUIDS;
+  h->isBatch = true;
+  h->batchH = effectRadius;
+  h->sceneDesc.assign(scenes, scenes + nscenes);
+  h->sceneOff.resize(nscenes);
+  uint64_t off = 0;
+  for (uint32_t s = 0; s < nscenes; ++s) {
+    h->sceneOff[s] = off;
+    off += scenes[s].nbParticles;
+  }
+  h->mp.currNbParticles = h->mp.maxNbParticles = total;
+  for (int a = 0; a < 3; ++a) h->mp.boxSize[a] = scenes[0].boxSize[a];
+  h->mp.dimension = 3;
+  h->mp.pCase = RTP_CASE_INVALID;
+  h->mp.maxNbPartsInCell = maxNbPartsInCell;
+  h->maxN = h->curN = total;
+  int rc = batch_grids(h, 1.0f);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  rtp_fluid_params_default(&h->fp);
+  rtp_boids_params_default(&h->bp);
+  rtp_cloud_params_default(&h->cp);
+  rtp_cloud_env_reference(&h->env);
+  h->iters = 2u;
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  rc = alloc_buffers(h);
+  if (!rc) rc = dalloc(h, &h->dScenes, nscenes);
+  if (!rc) rc = dalloc(h, &h->dSceneOf, total);
+  if (!rc) {
+    std::vector<uint16_t> so(total);
+    for (uint32_t s = 0; s < nscenes; ++s)
+      std::fill(so.begin() + h->sceneOff[s], so.begin() + h->sceneOff[s] + scenes[s].nbParticles, (uint16_t)s);
+    e = cudaMemcpy(h->dSceneOf, so.data(), sizeof(uint16_t) * total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy(sceneOf)");
+  }
+  if (!rc) rc = batch_upload_scenes(h);
+  if (!rc) {
+    e = cudaEventCreate(&h->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->t1);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate");
+  }
+  if (rc) {
+    free_handle(h);
+    return rc;
+  }
+  *out_handle = h;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_batch_scene_range(void* handle, uint32_t scene, uint64_t* offset, uint64_t* count) {
+  if (!handle || !offset || !count) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  if (!h->isBatch) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_batch_scene_range: not a batch");
+  if (scene >= h->sceneDesc.size()) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_batch_scene_range: no such scene");
+  *offset = h->sceneOff[scene];
+  *count = h->sceneDesc[scene].nbParticles;
+  return RTP_OK;
+}
+
+int rtp_batch_scene_constants(void* handle, uint32_t scene, rtp_grid_constants* out) {
+  if (!handle || !out) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  if (!h->isBatch) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_batch_scene_constants: not a batch");
+  if (scene >= h->sceneDesc.size()) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_batch_scene_constants: no such scene");
+  *out = h->sceneConst[scene];
+  return RTP_OK;
+}
+
+int rtp_batch_scene_key_base(void* handle, uint32_t scene, uint32_t* base) {
+  if (!handle || !base) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  if (!h->isBatch || scene >= h->hScenes.size()) return fail(RTP_ERR_INVALID_ARGUMENT, "no such batch scene");
+  *base = h->hScenes[scene].g.base;
+  return RTP_OK;
+}
+
+int rtp_set_tuning(void* handle, const rtp_tuning* t) {
+  RTP_GUARD_BEGIN
+  if (!handle || !t) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_tuning: fluids only");
+  if (t->lanes != 2 && t->lanes != 4 && t->lanes != 8) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: lanes 2, 4 or 8");
+  if (!h->isBatch && t->cellFactor != 1.0f)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: a single scene keeps the reference's grid (cellFactor 1)");
+  if (!(t->cellFactor >= 1.0f && t->cellFactor <= 4.0f))
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: cellFactor in [1, 4]");
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->isBatch && t->cellFactor != h->cellFactor) {
+    const float old = h->cellFactor;
+    int rc = batch_grids(h, t->cellFactor);
+    if (!rc && (h->gc.numCells > h->tableCells || h->gc.keyBits > h->sortKeyBits))
+      rc = fail(RTP_ERR_CAPACITY, "rtp_set_tuning: grid larger than allocated");
+    if (rc) {
+      batch_grids(h, old);
+      return rc;
+    }
+    RTP_TRY(batch_upload_scenes(h));
+    h->hasStep = false;
+  }
+  h->lanes = t->lanes;
+  invalidate(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_get_tuning(void* handle, rtp_tuning* t) {
+  if (!handle || !t) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  t->lanes = H(handle)->lanes;
+  t->cellFactor = H(handle)->cellFactor;
+  return RTP_OK;
+}
+
+int rtp_autotune(void* handle, uint32_t steps, rtp_tune_result* out) {
+  RTP_GUARD_BEGIN
+  if (!handle || !out) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_autotune: fluids only");
+  if (steps == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_autotune: steps must be > 0");
+  std::memset(out, 0, sizeof *out);
+  const uint32_t lanes[3] = {2, 4, 8};
+  const float factors[4] = {1.0f, 1.25f, 1.5f, 2.0f};
+  const int nf = h->isBatch ? 4 : 1;
+  double best = 1e300;
+  rtp_tuning bestT{4, 1.0f};
+  for (int f = 0; f < nf; ++f)
+    for (int l = 0; l < 3; ++l) {
+      rtp_tuning t{lanes[l], factors[f]};
+      if (rtp_set_tuning(handle, &t) != RTP_OK) continue;
+      RTP_TRY(run_steps(h, 2));
+      double ms = 0.0;
+      RTP_TRY(rtp_time_steps(handle, steps, 256ull << 20, &ms));
+      ms /= steps;
+      if (out->tried < RTP_TUNE_MAX_CANDIDATES) {
+        out->candidates[out->tried] = t;
+        out->msPerStep[out->tried] = ms;
+        out->tried += 1;
+      }
+      if (ms < best) {
+        best = ms;
+        bestT = t;
+      }
+    }
+  RTP_TRY(rtp_set_tuning(handle, &bestT));
+  out->best = bestT;
+  out->bestMsPerStep = best;
   return RTP_OK;
   RTP_GUARD_END
 }

@@ -24,7 +24,7 @@ struct PairList {
 constexpr uint32_t kListOverflow = 0xFFFFFFFFu;
 constexpr uint32_t kPairListK = 64;        // entries per particle in the device list
 constexpr uint32_t kSweepThreads = 64;     // block size of the two-phase sweeps (one wave at 131k)
-constexpr uint32_t kQuad = 4;              // lanes per particle in the list sweeps
+constexpr uint32_t kQuad = 4;              // default lanes per particle in the list sweeps
 
 // Visits [b0,e0) [b1,e1) [b2,e2) in that order, joining ranges that touch so that the
 // usual case (three consecutive non-empty cells of one z column) is a single loop.
@@ -98,7 +98,7 @@ __device__ __forceinline__ void for_each_fluid_row(const GridK& g, const uint2* 
 #pragma unroll 1
     for (int b = 0; b < 3; ++b) {
       const int y = (cy + b - 1 + g.R[1]) % g.R[1];
-      const uint32_t row = ((uint32_t)x * g.R[1] + (uint32_t)y) * g.R[2];
+      const uint32_t row = g.base + ((uint32_t)x * g.R[1] + (uint32_t)y) * g.R[2];
       uint32_t b0, e0, b1, e1, b2, e2;
       cell_range(table, row + (uint32_t)z0, g.cap, b0, e0);
       cell_range(table, row + (uint32_t)z1, g.cap, b1, e1);
@@ -146,24 +146,25 @@ __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const
   });
 }
 
-// Visits the pairs recorded for particle i, one in kQuad per lane (lane q takes entries
-// q, q + kQuad, ...); an overflowed particle searches its 27 cells on lane 0.
-template <class G, class F>
+// Visits the pairs recorded for particle i, one in LANES per lane (lane q takes entries
+// q, q + LANES, ...); an overflowed particle searches its 27 cells on lane 0.
+template <int LANES = kQuad, class G, class F>
 __device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restrict__ table, const PairList& L,
                                            uint32_t i, uint32_t q, float4 xi, G&& ld, F&& f) {
   const uint32_t c = __ldg(L.count + i);
   if (c != kListOverflow) {
     const uint32_t* base = L.idx + i;
-    visit_list_x4(q, c, kQuad, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
+    visit_list_x4(q, c, LANES, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
   } else if (q == 0) {
     for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
   }
 }
 
-// Sum of v over the kQuad lanes of a particle (all 32 lanes of the warp must call).
+// Sum of v over the LANES lanes of a particle (all 32 lanes of the warp must call).
+template <int LANES = kQuad>
 __device__ __forceinline__ float quad_sum(float v) {
-  v += __shfl_xor_sync(0xffffffffu, v, 1);
-  v += __shfl_xor_sync(0xffffffffu, v, 2);
+#pragma unroll
+  for (int o = 1; o < LANES; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 

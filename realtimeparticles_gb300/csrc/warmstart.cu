@@ -71,7 +71,7 @@ __device__ __forceinline__ float wall_proximity(float x, float lo, float hi, flo
 
 // Inference holds the network's fragments after the sweep: 14 blocks of 64 threads per SM
 // (73 registers) still keep 131,072 particles in one wave on 152 SMs.
-template <int MODE>
+template <int MODE, bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
     k_ws_lambda(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ velS,
                 const uint2* __restrict__ table, uint32_t n,
@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
   for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
   float lam = 0.0f;
   if (active) {
+    scene_of<BATCH>(i, g, p);
     const float4 xi = ld4(pred + i), vi = ld4(velS + i);
     WsSums S;
     ws_sweep(g, table, pred, velS, i, xi, vi, pl, S);
@@ -183,12 +184,14 @@ __global__ void __launch_bounds__(128) k_ws_record_targets(GridK g, FluidK p, co
   o[3] = xf.z - (xi.z + cz * p.invRho0);
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads) k_ws_density_error(GridK g, FluidK p, const float4* __restrict__ pos,
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float* __restrict__ errPartial) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
   if (i < n) {
+    scene_of<BATCH>(i, g, p);
     const Sph k(g);
     const float4 xi = ld4(pos + i);
     float rho = 0.0f;
@@ -248,7 +251,8 @@ int ws_lambda_record(const GridK& g, const FluidK& p, const float4* pred, const 
   if (stride == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "sample stride must be > 0");
   MlpDev m{};
   L.begin("ws_lambda_record");
-  k_ws_lambda<kRecord><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+  if (p.bt.scenes) return fail(RTP_ERR_NOT_SUPPORTED, "sample recording runs on single scenes");
+  k_ws_lambda<kRecord, false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
       g, p, pred, velS, table, n, lambda, density, lamTot, pl, stride, phase, feats, capacity, m, nullptr);
   L.end("ws_lambda_record");
   return check("k_ws_lambda<record>");
@@ -258,8 +262,12 @@ int ws_lambda_infer(const GridK& g, const FluidK& p, const float4* pred, const f
                     const void* mlpBlock, float4* res, Launcher& L) {
   const MlpDev m = mlp_dev(mlpBlock);
   L.begin("ws_lambda_mlp");
-  k_ws_lambda<kInfer><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
-      g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
+  if (p.bt.scenes)
+    k_ws_lambda<kInfer, true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
+  else
+    k_ws_lambda<kInfer, false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
   L.end("ws_lambda_mlp");
   return check("k_ws_lambda<infer>");
 }
@@ -278,7 +286,10 @@ int ws_record_targets(const GridK& g, const FluidK& p, const float4* x0, const f
 int ws_density_error(const GridK& g, const FluidK& p, const float4* pos, const uint2* table, uint32_t n,
                      float* errPartial, Launcher& L) {
   L.begin("ws_density_error");
-  k_ws_density_error<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
+  if (p.bt.scenes)
+    k_ws_density_error<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
+  else
+    k_ws_density_error<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
   L.end("ws_density_error");
   return check("k_ws_density_error");
 }

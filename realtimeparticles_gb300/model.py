@@ -279,6 +279,27 @@ class Fluids(Model):
     def setJacobiIterations(self, it):
         call("rtp_set_jacobi_iterations", self._h, int(it))
 
+    # launch shape (new; rtp.h rtp_set_tuning) --------------------------------------------
+    def setTuning(self, lanes=4, cell_factor=1.0):
+        t = abi.Tuning()
+        t.lanes = int(lanes)
+        t.cellFactor = float(cell_factor)
+        call("rtp_set_tuning", self._h, C.byref(t))
+
+    def tuning(self):
+        t = abi.Tuning()
+        call("rtp_get_tuning", self._h, C.byref(t))
+        return int(t.lanes), float(t.cellFactor)
+
+    def autotune(self, steps=5):
+        """Times every launch-shape candidate over `steps` steps and keeps the fastest.
+        Returns (best (lanes, cell factor), {(lanes, cell factor): ms per step})."""
+        r = abi.TuneResult()
+        call("rtp_autotune", self._h, int(steps), C.byref(r))
+        cands = {(int(r.candidates[i].lanes), round(float(r.candidates[i].cellFactor), 3)): float(r.msPerStep[i])
+                 for i in range(r.tried)}
+        return (int(r.best.lanes), float(r.best.cellFactor)), cands
+
     # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
     def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):
         """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off."""
@@ -330,6 +351,49 @@ class Fluids(Model):
         self.setJacobiIterations(iters)
 
 
+class FluidsBatch(Fluids):
+    """Many independent fluids scenes stepped together (rtp.h rtp_create_batch).  Buffers
+    are the scenes' particles concatenated; sceneRange(s) gives scene s's slots."""
+
+    def __init__(self, scenes, effect_radius, max_parts_in_cell=0):
+        arr = (abi.BatchScene * len(scenes))()
+        for i, (n, box) in enumerate(scenes):
+            arr[i].nbParticles = int(n)
+            for a in range(3):
+                arr[i].boxSize[a] = float(box[a])
+        self._h = C.c_void_p()
+        call("rtp_create_batch", len(scenes), arr, float(effect_radius), int(max_parts_in_cell), C.byref(self._h))
+        total = sum(int(n) for n, _ in scenes)
+        self._params = abi.model_params(total, total, scenes[0][1], (1, 1, 1), 3)
+        self._input_json = copy.deepcopy(self._DEFAULT_JSON)
+        self._boundary = abi.BOUNCING_WALL
+        self._pause = False
+        self._dimension = 3
+        self._case = abi.CASE_INVALID
+        self._nscenes = len(scenes)
+
+    def numScenes(self):
+        return self._nscenes
+
+    def sceneRange(self, s):
+        off, cnt = C.c_uint64(), C.c_uint64()
+        call("rtp_batch_scene_range", self._h, int(s), C.byref(off), C.byref(cnt))
+        return int(off.value), int(cnt.value)
+
+    def sceneConstants(self, s):
+        c = abi.GridConstants()
+        call("rtp_batch_scene_constants", self._h, int(s), C.byref(c))
+        return c
+
+    def sceneKeyBase(self, s):
+        b = C.c_uint32()
+        call("rtp_batch_scene_key_base", self._h, int(s), C.byref(b))
+        return int(b.value)
+
+    def constants(self):
+        raise NotImplementedError("a batch has one grid per scene: sceneConstants(s)")
+
+
 class Boids(Model):
     """Physics::CL::Boids (physics/ocl/Boids.hpp) on the GB300 path."""
 
@@ -368,6 +432,27 @@ class Clouds(Model):
 
     def setJacobiIterations(self, it):
         call("rtp_set_jacobi_iterations", self._h, int(it))
+
+    # launch shape (new; rtp.h rtp_set_tuning) --------------------------------------------
+    def setTuning(self, lanes=4, cell_factor=1.0):
+        t = abi.Tuning()
+        t.lanes = int(lanes)
+        t.cellFactor = float(cell_factor)
+        call("rtp_set_tuning", self._h, C.byref(t))
+
+    def tuning(self):
+        t = abi.Tuning()
+        call("rtp_get_tuning", self._h, C.byref(t))
+        return int(t.lanes), float(t.cellFactor)
+
+    def autotune(self, steps=5):
+        """Times every launch-shape candidate over `steps` steps and keeps the fastest.
+        Returns (best (lanes, cell factor), {(lanes, cell factor): ms per step})."""
+        r = abi.TuneResult()
+        call("rtp_autotune", self._h, int(steps), C.byref(r))
+        cands = {(int(r.candidates[i].lanes), round(float(r.candidates[i].cellFactor), 3)): float(r.msPerStep[i])
+                 for i in range(r.tried)}
+        return (int(r.best.lanes), float(r.best.cellFactor)), cands
 
     # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
     def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):

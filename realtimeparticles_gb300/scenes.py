@@ -231,3 +231,41 @@ def clouds_cumulus(n=131072, res=(30, 60, 30), width=1.0, seed=0, noise=True, no
     cp.windCoeff = 1.0 * scale
     return {"pos": pos, "vel": vel, "model_params": mp, "fluid_params": fp, "cloud_params": cp,
             "env": env, "ground": ground}
+
+
+def batched_dam_breaks(count=48, seed=0, n_range=(4096, 65536), aspect_range=(0.5, 2.0), d=0.0125, jitter=0.01):
+    """Independent dam-break scenes for one batch: particle counts log-uniform in n_range,
+    box aspect ratios (x extent over the unit y, z extents) uniform in aspect_range, seeded.
+
+    Scene box = (round(40 a) h, 40 h, 40 h) with h = 2d; its fluid is a jittered lattice of
+    spacing d filling x in [lo, lo + 0.4 L_x), z in [lo, lo + 0.8 L_z), layer by layer from
+    the floor until the scene's count is reached (lo = -W + 0.01, the clamp floor).  Returns
+    dict(scenes=[(n, (bx, by, bz))], pos, vel (concatenated in scene order), offsets,
+    fluid_params, h, d)."""
+    rng = np.random.default_rng(seed)
+    h = 2.0 * d
+    lo_n, hi_n = n_range
+    ns = np.round(np.exp(rng.uniform(np.log(lo_n), np.log(hi_n), count))).astype(np.int64)
+    aspects = rng.uniform(aspect_range[0], aspect_range[1], count)
+    descs, poss, offs = [], [], []
+    off = 0
+    for n, a in zip(ns, aspects):
+        rx = max(3, int(round(40 * a)))
+        box = (rx * h, 40 * h, 40 * h)
+        W = [b / 2.0 for b in box]
+        nx = int(np.floor(0.4 * box[0] / d))
+        nz = int(np.floor(0.8 * box[2] / d))
+        ny = int(np.ceil(n / (nx * nz)))
+        iy, ix, iz = np.meshgrid(np.arange(ny), np.arange(nx), np.arange(nz), indexing="ij")
+        idx = np.stack([ix.ravel(), iy.ravel(), iz.ravel()], axis=1)[:n].astype(np.float64)
+        lo = np.array([-W[0] + 0.01, -W[1] + 0.01, -W[2] + 0.01])
+        xyz = lo + (idx + 0.5) * d + rng.uniform(-jitter * d, jitter * d, size=(n, 3))
+        p = np.zeros((n, 4), np.float32)
+        p[:, :3] = xyz.astype(np.float32)
+        descs.append((int(n), tuple(float(b) for b in box)))
+        poss.append(p)
+        offs.append(off)
+        off += int(n)
+    pos = np.concatenate(poss)
+    return {"scenes": descs, "pos": pos, "vel": np.zeros_like(pos), "offsets": offs,
+            "fluid_params": fluid_params(lattice_rest_density(d, h)), "h": h, "d": d}

@@ -33,7 +33,8 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
                "rtp_cloud_env": abi.CloudEnv, "rtp_grid_constants": abi.GridConstants,
                "rtp_kernel_time": abi.KernelTime, "rtp_metrics": abi.Metrics, "rtp_mlp": abi.Mlp,
                "rtp_warm_start_config": abi.WarmStartConfig, "rtp_solver_stats": abi.SolverStats,
-               "rtp_train_config": abi.TrainConfig}
+               "rtp_train_config": abi.TrainConfig, "rtp_batch_scene": abi.BatchScene, "rtp_tuning": abi.Tuning,
+               "rtp_tune_result": abi.TuneResult}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s/include/rtp.h"' % ROOT, "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
