@@ -8,6 +8,8 @@ Metric: particle-steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+* autotune (fluids workloads): the launch shape (list-sweep lanes; for a batch also the cell
+  factor) is picked by the library's autotuner before warm-up; candidates and times reported.
 * value: K device-timed steps (CUDA events around each graph replay on the model's
   stream), inputs resident in HBM, L2 flushed before every step by a 256 MiB write.
 * e2e: K steps through the public API with host buffers: upload pos/vel from pinned
@@ -61,6 +63,9 @@ WORKLOADS = {
     "pbf_dam_break_16m": dict(kind="fluids", lattice=(256, 256, 256), box=6.4, iters=3, max_steps=10,
                               metric="PBF particle-steps/s @16.7M (plain, 3 Jacobi iterations)"),
     "boids_131k": dict(kind="boids", n=131072, metric="boids particle-steps/s @131k"),
+    # 48 independent dam breaks (4,096-65,536 particles, box aspect 0.5-2, seed 0) in one batch.
+    "pbf_batched_48": dict(kind="batch", count=48, seed=0, iters=3, max_steps=300,
+                           metric="batched PBF particle-steps/s (48 dam-break scenes, 3 Jacobi iterations)"),
     "clouds_131k": dict(kind="clouds", n=131072, iters=1, metric="clouds particle-steps/s @131k"),
 }
 
@@ -68,6 +73,15 @@ WORKLOADS = {
 def make_model(w):
     """The model of workload w with its seeded inputs uploaded."""
     from realtimeparticles_gb300 import model
+    if w["kind"] == "batch":
+        sc = scenes.batched_dam_breaks(count=w["count"], seed=w["seed"])
+        m = model.FluidsBatch(sc["scenes"], sc["h"])
+        m.setFluidParams(sc["fluid_params"])
+        m.setJacobiIterations(w["iters"])
+        m.upload(abi.BUF_POS, sc["pos"])
+        m.upload(abi.BUF_VEL, sc["vel"])
+        m._scene_set = sc
+        return m, sc["pos"].shape[0]
     if w["kind"] == "fluids":
         sc = scenes.dam_break(lattice=w["lattice"], box=w.get("box", 1.0))
         m = model.Fluids(sc["model_params"])
@@ -389,6 +403,51 @@ def grid_sort_summary(kt, steps, n, c, nonempty, peak):
             "sort_passes": passes, "cells": int(c.numCells), "nonempty_cells": nonempty}
 
 
+def batch_study(m, w, steps, warmup):
+    """The batch against the same scenes on separate handles stepped one after another, and
+    plain against warm-started solver error on the batch."""
+    from realtimeparticles_gb300 import model, warmstart
+    sc = m._scene_set
+    lanes, factor = m.tuning()
+    n_total = sc["pos"].shape[0]
+    ms_sum = 0.0
+    for s, (n, box) in enumerate(sc["scenes"]):
+        off = sc["offsets"][s]
+        res = tuple(int(round(b / sc["h"])) for b in box)
+        with model.Fluids(abi.model_params(n, n, box, res, 3)) as one:
+            one.setFluidParams(sc["fluid_params"])
+            one.setJacobiIterations(w["iters"])
+            one.setTuning(lanes, 1.0)
+            one.upload(abi.BUF_POS, sc["pos"][off:off + n])
+            one.upload(abi.BUF_VEL, sc["vel"][off:off + n])
+            one.update(warmup)
+            ms_sum += one.timeSteps(steps, flush_bytes=L2_FLUSH_BYTES) / steps
+    separate = n_total / (ms_sum / 1000.0)
+    # Plain and warm-started solver error on the batch (network trained on the 131k dam break).
+    feats, targets = warmstart.generate_samples(seeds=range(1, 9), lattice=(32, 64, 64), steps=400,
+                                                record_every=25, stride=8, reference_iterations=8)
+    net, hist = warmstart.train(feats, targets, epochs=16, batch=8192, seed=0)
+    del feats, targets
+    errs = {}
+    for name, use in (("plain", False), ("learned_extra1", True)):
+        mb, _ = make_model(w)
+        with mb:
+            mb.setTuning(lanes, factor)
+            mb.enableSolverStats(True)
+            if use:
+                mb.setWarmStart(net, extra_iterations=1, guard_tolerance=0.0)
+            mb.update(warmup)
+            mb.resetSolverStats()
+            ms = mb.timeSteps(steps, flush_bytes=L2_FLUSH_BYTES) / steps
+            errs[name] = {"particle_steps_per_s": n_total / (ms / 1000.0), "ms_per_step": ms,
+                          "mean_density_error": mb.solverStats()["mean"]}
+    return {"scenes": len(sc["scenes"]), "particles": n_total,
+            "scene_particles_min": min(n for n, _ in sc["scenes"]),
+            "scene_particles_max": max(n for n, _ in sc["scenes"]),
+            "separate_handles_particle_steps_per_s": separate,
+            "separate_handles_ms_per_step": ms_sum, "solver": errs}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -405,6 +464,11 @@ def run_ours(args):
     if "max_steps" in w:
         args.steps = min(args.steps, w["max_steps"])
     m, n = make_model(w)
+    tune = None
+    if w["kind"] in ("batch", "fluids"):
+        best, cands = m.autotune(steps=5)
+        tune = {"best": {"lanes": best[0], "cell_factor": best[1]},
+                "candidates_ms_per_step": {"%d/%.2f" % k: v for k, v in sorted(cands.items())}}
 
     # Warm-up (graph capture happens here).
     m.update(max(3, args.warmup))
@@ -435,7 +499,7 @@ def run_ours(args):
     achieved = alg / (dom_avg_ms / 1000.0) / 1e9
     share = {k: round(v[1] / sum(x[1] for x in kt.values()), 4) for k, v in kt.items()}
     grid_sort = None
-    if w["kind"] == "fluids":
+    if w["kind"] == "fluids":  # (a batch has one grid per scene)
         tab = m.download(abi.BUF_CELL_TABLE)
         nonempty = int(np.count_nonzero(tab[:, 1] >= tab[:, 0]))
         grid_sort = grid_sort_summary(kt, args.steps, n, m.constants(), nonempty, peak)
@@ -465,6 +529,7 @@ def run_ours(args):
     t_e2e = max_over_ranks(t_e2e, ws)
     e2e = n * args.steps * ws / t_e2e
     metrics = m.metrics() if w["kind"] != "boids" else None
+    batch = batch_study(m, w, args.steps, max(3, args.warmup)) if w["kind"] == "batch" and rank == 0 else None
     m.close()
 
     out = None
@@ -490,6 +555,10 @@ def run_ours(args):
         }
         if grid_sort:
             out["grid_sort"] = grid_sort
+        if tune:
+            out["autotune"] = tune
+        if batch:
+            out["batch"] = batch
         if metrics is not None:
             out["state_check"] = {"mean_density_error": metrics.meanDensityError,
                                   "kinetic_energy": metrics.kineticEnergy,

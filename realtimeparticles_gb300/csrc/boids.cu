@@ -13,8 +13,10 @@ namespace rtp {
 
 __global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, const float4* __restrict__ pos, uint32_t n,
                                                              uint32_t* __restrict__ keys, int bits0,
-                                                             uint32_t* __restrict__ hist0) {
+                                                             uint32_t* __restrict__ hist0, ZeroJob zero) {
+  pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
+  zero_job(zero);
   TileHistogram th;
   th.init(s_hist, bits0);
   const uint32_t base = blockIdx.x * kSortTile;
@@ -43,6 +45,7 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
                                                             const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
                                                             float4* __restrict__ vel, float4* __restrict__ acc,
                                                             uint32_t* __restrict__ ids) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = ld4(posS + i);
@@ -113,9 +116,9 @@ static int check(const char* what) {
 }
 
 int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
-                  Launcher& L) {
+                  Launcher& L, const ZeroJob& zero) {
   L.begin("bd_keys");
-  k_boids_keys<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, pos, n, keys, plan.bits[0], hist0);
+  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, n, keys, plan.bits[0], hist0, zero);
   L.end("bd_keys");
   return check("k_boids_keys");
 }
@@ -126,9 +129,9 @@ int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, const flo
   const uint32_t b = (n + 127) / 128;
   L.begin("bd_rules_update");
   if (periodic)
-    k_boids_rules_update<true><<<b, 128, 0, L.stream>>>(g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
   else
-    k_boids_rules_update<false><<<b, 128, 0, L.stream>>>(g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
   L.end("bd_rules_update");
   return check("k_boids_rules_update");
 }

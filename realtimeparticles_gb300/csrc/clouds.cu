@@ -155,8 +155,10 @@ __global__ void __launch_bounds__(kSortThreads) k_cloud_thermo_predict(
     GridK g, CloudK c, const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
     float* __restrict__ temp, float* __restrict__ vapor, float* __restrict__ cloud, float* __restrict__ buoy,
     float4* __restrict__ pred, float4* __restrict__ tot, uint32_t* __restrict__ keys, int bits0,
-    uint32_t* __restrict__ hist0) {
+    uint32_t* __restrict__ hist0, ZeroJob zero) {
+  pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
+  zero_job(zero);
   TileHistogram th;
   th.init(s_hist, bits0);
   const float dt = c.dt;
@@ -199,6 +201,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g
                                                                          const float* __restrict__ temp,
                                                                          const uint2* __restrict__ table, uint32_t n,
                                                                          float* __restrict__ lamT, PairList pl) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
@@ -243,6 +246,7 @@ __global__ void __launch_bounds__(128) k_cloud_temp_correct(GridK g, CloudK c, c
                                                             const float* __restrict__ lamT,
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             float* __restrict__ temp, PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -272,6 +276,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float* __restrict__ lambda,
                                                                     float* __restrict__ density, PairList pl) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
@@ -319,6 +324,7 @@ __global__ void __launch_bounds__(128) k_cloud_deltap(GridK g, FluidK p, const f
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut, float4* __restrict__ tot,
                                                       float4* __restrict__ velS, PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -361,6 +367,7 @@ __global__ void __launch_bounds__(128) k_cloud_deltap(GridK g, FluidK p, const f
 
 __global__ void k_cloud_update_vel(GridK g, FluidK p, const float4* __restrict__ tot, uint32_t n,
                                    float4* __restrict__ velS) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 t = ld4(tot + i);
@@ -374,6 +381,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, 
                                                                        const float4* __restrict__ velS,
                                                                        const uint2* __restrict__ table, uint32_t n,
                                                                        float4* __restrict__ vort, PairList pl) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Sph k(g);
@@ -409,6 +417,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, 
 __global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
                                                        uint32_t n, float4* __restrict__ velS, PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -449,6 +458,7 @@ __global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const 
 __global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
                                                      const float4* __restrict__ velS, const uint2* __restrict__ table,
                                                      uint32_t n, CloudState s, PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -495,6 +505,7 @@ __global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c
 // cld_initTemperature + cld_initVaporDensity (clouds.cl:116-135); cloud = 0.
 __global__ void k_cloud_init(GridK g, CloudK c, const float4* __restrict__ pos, uint32_t n, float* __restrict__ temp,
                              float* __restrict__ vapor, float* __restrict__ cloud, float* __restrict__ buoy) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float t = env_temp(c, g, ld4(pos + i));
@@ -512,10 +523,10 @@ static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; 
 
 int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const float4* vel, uint32_t n, float* temp,
                   float* vapor, float* cloud, float* buoy, float4* pred, float4* tot, uint32_t* keys,
-                  const SortPlan& plan, uint32_t* hist0, Launcher& L) {
+                  const SortPlan& plan, uint32_t* hist0, Launcher& L, const ZeroJob& zero) {
   L.begin("cld_thermo_predict");
-  k_cloud_thermo_predict<<<plan.tiles, kSortThreads, 0, L.stream>>>(g, c, pos, vel, n, temp, vapor, cloud, buoy, pred,
-                                                                    tot, keys, plan.bits[0], hist0);
+  launch(L, k_cloud_thermo_predict, dim3(plan.tiles), dim3(kSortThreads), g, c, pos, vel, n, temp, vapor, cloud, buoy, pred,
+                                                                    tot, keys, plan.bits[0], hist0, zero);
   L.end("cld_thermo_predict");
   return check("k_cloud_thermo_predict");
 }
@@ -523,12 +534,12 @@ int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const floa
 int cloud_temperature(const GridK& g, const CloudK& c, const float4* posS, float* tempS, float* lamT, const uint2* table,
                       uint32_t n, const PairList& pl, Launcher& L) {
   L.begin("cld_temp_lambda");
-  k_cloud_temp_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, c, posS, tempS, table, n, lamT, pl);
+  launch(L, k_cloud_temp_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, c, posS, tempS, table, n, lamT, pl);
   L.end("cld_temp_lambda");
   int rc = check("k_cloud_temp_lambda");
   if (rc) return rc;
   L.begin("cld_temp_correct");
-  k_cloud_temp_correct<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, c, posS, lamT, table, n, tempS, pl);
+  launch(L, k_cloud_temp_correct, dim3(blocks(n * kQuad, 128)), dim3(128), g, c, posS, lamT, table, n, tempS, pl);
   L.end("cld_temp_correct");
   return check("k_cloud_temp_correct");
 }
@@ -537,16 +548,16 @@ int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
                     const uint2* table, uint32_t n, float* lambda, float* density, bool last, float4* velS,
                     const PairList& pl, Launcher& L) {
   L.begin("cld_lambda");
-  k_cloud_lambda<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda, density, pl);
+  launch(L, k_cloud_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda, density, pl);
   L.end("cld_lambda");
   int rc = check("k_cloud_lambda");
   if (rc) return rc;
   L.begin(last ? "cld_deltap_vel" : "cld_deltap");
   if (last)
-    k_cloud_deltap<true><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS, velS,
+    launch(L, k_cloud_deltap<true>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut, totS, velS,
                                                                         pl);
   else
-    k_cloud_deltap<false><<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, predIn, lambda, table, n, predOut, totS,
+    launch(L, k_cloud_deltap<false>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut, totS,
                                                                          velS, pl);
   L.end(last ? "cld_deltap_vel" : "cld_deltap");
   return check("k_cloud_deltap");
@@ -554,7 +565,7 @@ int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
 
 int cloud_update_vel(const GridK& g, const FluidK& p, const float4* totS, uint32_t n, float4* velS, Launcher& L) {
   L.begin("cld_updateVel");
-  k_cloud_update_vel<<<blocks(n, 256), 256, 0, L.stream>>>(g, p, totS, n, velS);
+  launch(L, k_cloud_update_vel, dim3(blocks(n, 256)), dim3(256), g, p, totS, n, velS);
   L.end("cld_updateVel");
   return check("k_cloud_update_vel");
 }
@@ -563,18 +574,18 @@ int cloud_post(const GridK& g, const FluidK& p, const CloudK& c, const float4* p
                const uint2* table, uint32_t n, const CloudState& s, const PairList& pl, Launcher& L) {
   if (p.vorticity) {
     L.begin("cld_vorticity");
-    k_cloud_vorticity<<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, pred, velS, table, n, vort, pl);
+    launch(L, k_cloud_vorticity, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, pred, velS, table, n, vort, pl);
     L.end("cld_vorticity");
     int rc = check("k_cloud_vorticity");
     if (rc) return rc;
     L.begin("cld_confine");
-    k_cloud_confine<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
+    launch(L, k_cloud_confine, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, pred, vort, table, n, velS, pl);
     L.end("cld_confine");
     rc = check("k_cloud_confine");
     if (rc) return rc;
   }
   L.begin("cld_xsph_final");
-  k_cloud_final<<<blocks(n * kQuad, 128), 128, 0, L.stream>>>(g, p, c, pred, velS, table, n, s, pl);
+  launch(L, k_cloud_final, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, c, pred, velS, table, n, s, pl);
   L.end("cld_xsph_final");
   return check("k_cloud_final");
 }
@@ -583,7 +594,7 @@ int cloud_init(const GridK& g, const CloudK& c, const float4* pos, uint32_t n, f
                float* buoy, Launcher& L) {
   if (n == 0) return RTP_OK;
   L.begin("cld_init");
-  k_cloud_init<<<blocks(n, 256), 256, 0, L.stream>>>(g, c, pos, n, temp, vapor, cloud, buoy);
+  launch(L, k_cloud_init, dim3(blocks(n, 256)), dim3(256), g, c, pos, n, temp, vapor, cloud, buoy);
   L.end("cld_init");
   return check("k_cloud_init");
 }

@@ -31,7 +31,7 @@ struct CloudState {
 
 int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const float4* vel, uint32_t n, float* temp,
                   float* vapor, float* cloud, float* buoy, float4* pred, float4* tot, uint32_t* keys,
-                  const SortPlan& plan, uint32_t* hist0, Launcher& L);
+                  const SortPlan& plan, uint32_t* hist0, Launcher& L, const ZeroJob& zero = ZeroJob{});
 int cloud_temperature(const GridK& g, const CloudK& c, const float4* posS, float* tempS, float* lamT, const uint2* table,
                       uint32_t n, const PairList& pl, Launcher& L);
 int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, float4* totS,

@@ -29,8 +29,11 @@ template <bool BATCH>
 __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK p0, const float4* __restrict__ pos,
                                                                 const float4* __restrict__ vel, uint32_t n,
                                                                 float4* __restrict__ pred, uint32_t* __restrict__ keys,
-                                                                int bits0, uint32_t* __restrict__ hist0, int clampOut) {
+                                                                int bits0, uint32_t* __restrict__ hist0, int clampOut,
+                                                                ZeroJob zero) {
+  pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
+  zero_job(zero);
   TileHistogram th;
   th.init(s_hist, bits0);
   const float dt = p0.dt;
@@ -69,6 +72,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, Flu
                                                                 float* __restrict__ lambda,
                                                                 float* __restrict__ density, PairList pl,
                                                                 float* __restrict__ lamTot, int totMode) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   scene_of<BATCH>(i, g, p);
@@ -121,6 +125,7 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
                                                       uint32_t n, float4* __restrict__ predOut,
                                                       const float4* __restrict__ posS, float4* __restrict__ velS,
                                                       PairList pl, const float4* __restrict__ res) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
@@ -175,6 +180,7 @@ __global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const f
 template <bool BATCH>
 __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ posS,
                                    uint32_t n, float4* __restrict__ velS) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   scene_of<BATCH>(i, g, p);
@@ -194,6 +200,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, 
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float4* __restrict__ vort, PairList pl,
                                                                     float* __restrict__ errPartial) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
   if (i < n) {
@@ -235,6 +242,7 @@ template <bool BATCH, int LANES>
 __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
                                                        uint32_t n, float4* __restrict__ velS, PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
@@ -281,6 +289,7 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
                                                           const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
                                                           float4* __restrict__ vel, uint32_t* __restrict__ ids,
                                                           PairList pl) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
@@ -320,6 +329,7 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
 __global__ void k_fluid_final(const float4* __restrict__ pred, const float4* __restrict__ velS, uint32_t n,
                               const uint32_t* __restrict__ idsS, float4* __restrict__ pos, float4* __restrict__ vel,
                               uint32_t* __restrict__ ids) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   pos[i] = ld4(pred + i);
@@ -333,6 +343,7 @@ template <bool BATCH>
 __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const float4* __restrict__ pos,
                                                        const float4* __restrict__ vel, const uint2* __restrict__ table,
                                                        uint32_t n, double* __restrict__ acc, uint32_t* __restrict__ hist) {
+  pdl_enter();
   // acc: [0] sum |rho/rho0 - 1|, [1] kinetic energy, [2] neighbour count, [3] sum max(rho/rho0 - 1, 0);
   // hist[64] = max error bits.
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -382,6 +393,7 @@ __global__ void __launch_bounds__(128) k_fluid_metrics(GridK g, FluidK p, const 
 
 // Pair-list statistics: overflowed particles and the longest list (diagnostics).
 __global__ void k_pair_list_stats(const uint32_t* __restrict__ count, uint32_t n, uint32_t* __restrict__ out) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t c = __ldg(count + i);
@@ -397,14 +409,14 @@ static int check(const char* what) {
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
 int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
-                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L) {
+                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L, const ZeroJob& zero) {
   L.begin("fld_predict");
   if (p.bt.scenes)
-    k_fluid_predict<true><<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
-                                                                     clampOut ? 1 : 0);
+    launch(L, k_fluid_predict<true>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
+                                                                     clampOut ? 1 : 0, zero);
   else
-    k_fluid_predict<false><<<plan.tiles, kSortThreads, 0, L.stream>>>(g, p, pos, vel, n, pred, keys, plan.bits[0],
-                                                                      hist0, clampOut ? 1 : 0);
+    launch(L, k_fluid_predict<false>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0],
+                                                                      hist0, clampOut ? 1 : 0, zero);
   L.end("fld_predict");
   return check("k_fluid_predict");
 }
@@ -414,10 +426,10 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
                     Launcher& L, float* lamTot, int totMode) {
   L.begin("fld_lambda");
   if (p.bt.scenes)
-    k_fluid_lambda<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda,
+    launch(L, k_fluid_lambda<true>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda,
                                                                                    density, pl, lamTot, totMode);
   else
-    k_fluid_lambda<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, predIn, table, n, lambda,
+    launch(L, k_fluid_lambda<false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda,
                                                                                     density, pl, lamTot, totMode);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
@@ -433,10 +445,10 @@ int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* 
     constexpr bool BATCH = decltype(B)::value;
     constexpr int LANES = decltype(LN)::value;
     if (last)
-      k_fluid_deltap<true, BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(
+      launch(L, k_fluid_deltap<true, BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128),
           g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
     else
-      k_fluid_deltap<false, BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(
+      launch(L, k_fluid_deltap<false, BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128),
           g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
   });
   L.end(last ? "fld_deltap_vel" : "fld_deltap");
@@ -447,9 +459,9 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
                      Launcher& L) {
   L.begin("fld_updateVel");
   if (p.bt.scenes)
-    k_fluid_update_vel<true><<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
+    launch(L, k_fluid_update_vel<true>, dim3(blocks(n, 256)), dim3(256), g, p, pred, posS, n, velS);
   else
-    k_fluid_update_vel<false><<<blocks(n, 256), 256, 0, L.stream>>>(g, p, pred, posS, n, velS);
+    launch(L, k_fluid_update_vel<false>, dim3(blocks(n, 256)), dim3(256), g, p, pred, posS, n, velS);
   L.end("fld_updateVel");
   return check("k_fluid_update_vel");
 }
@@ -460,15 +472,15 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
   const uint32_t nb = blocks(n, kSweepThreads);
   if (p.bt.scenes) {
     if (errPartial)
-      k_fluid_vorticity<true, true><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl, errPartial);
+      launch(L, k_fluid_vorticity<true, true>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, errPartial);
     else
-      k_fluid_vorticity<false, true><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl, nullptr);
+      launch(L, k_fluid_vorticity<false, true>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, nullptr);
   } else {
     if (errPartial)
-      k_fluid_vorticity<true, false><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl,
+      launch(L, k_fluid_vorticity<true, false>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl,
                                                                          errPartial);
     else
-      k_fluid_vorticity<false, false><<<nb, kSweepThreads, 0, L.stream>>>(g, p, pred, velS, table, n, vort, pl,
+      launch(L, k_fluid_vorticity<false, false>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl,
                                                                           nullptr);
   }
   L.end("fld_vorticity");
@@ -488,7 +500,7 @@ int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS
     dispatch_fluid(p, [&](auto B, auto LN) {
       constexpr bool BATCH = decltype(B)::value;
       constexpr int LANES = decltype(LN)::value;
-      k_fluid_confine<BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(g, p, pred, vort, table, n, velS, pl);
+      launch(L, k_fluid_confine<BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128), g, p, pred, vort, table, n, velS, pl);
     });
     L.end("fld_confine");
     rc = check("k_fluid_confine");
@@ -497,14 +509,14 @@ int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS
     dispatch_fluid(p, [&](auto B, auto LN) {
       constexpr bool BATCH = decltype(B)::value;
       constexpr int LANES = decltype(LN)::value;
-      k_fluid_xsph_final<BATCH, LANES><<<blocks(n * LANES, 128), 128, 0, L.stream>>>(g, p, pred, velS, table, n, idsS,
+      launch(L, k_fluid_xsph_final<BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128), g, p, pred, velS, table, n, idsS,
                                                                                       pos, vel, ids, pl);
     });
     L.end("fld_xsph_final");
     return check("k_fluid_xsph_final");
   }
   L.begin("fld_final");
-  k_fluid_final<<<blocks(n, 256), 256, 0, L.stream>>>(pred, velS, n, idsS, pos, vel, ids);
+  launch(L, k_fluid_final, dim3(blocks(n, 256)), dim3(256), pred, velS, n, idsS, pos, vel, ids);
   L.end("fld_final");
   return check("k_fluid_final");
 }
@@ -514,9 +526,9 @@ int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const floa
   if (n == 0) return RTP_OK;
   L.begin("fld_metrics");
   if (p.bt.scenes)
-    k_fluid_metrics<true><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
+    launch(L, k_fluid_metrics<true>, dim3(blocks(n, 128)), dim3(128), g, p, pos, vel, table, n, acc, hist);
   else
-    k_fluid_metrics<false><<<blocks(n, 128), 128, 0, L.stream>>>(g, p, pos, vel, table, n, acc, hist);
+    launch(L, k_fluid_metrics<false>, dim3(blocks(n, 128)), dim3(128), g, p, pos, vel, table, n, acc, hist);
   L.end("fld_metrics");
   return check("k_fluid_metrics");
 }
@@ -526,7 +538,7 @@ int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const floa
 namespace rtp {
 int pair_list_stats(const PairList& pl, uint32_t n, uint32_t* out2, Launcher& L) {
   if (n == 0) return RTP_OK;
-  k_pair_list_stats<<<(n + 255) / 256, 256, 0, L.stream>>>(pl.count, n, out2);
+  launch(L, k_pair_list_stats, dim3((n + 255) / 256), dim3(256), pl.count, n, out2);
   return check("k_pair_list_stats");
 }
 }  // namespace rtp

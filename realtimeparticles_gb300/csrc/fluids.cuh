@@ -84,7 +84,8 @@ __device__ __forceinline__ void block_error_partial(float v, float* out) {
 constexpr int kTotNone = 0, kTotWrite = 1, kTotAdd = 2;
 
 int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
-                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L);
+                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L,
+                  const ZeroJob& zero = ZeroJob{});
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table,
                     uint32_t n, float* lambda, float* density, bool last, const float4* posS, float4* velS,
                     const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone);

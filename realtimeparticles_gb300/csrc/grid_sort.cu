@@ -70,6 +70,7 @@ void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s) {
 
 // fillCellIDs (grid.cl:76-86).
 __global__ void k_fill_cell_ids(GridK g, const float4* __restrict__ pos, uint32_t n, uint32_t* __restrict__ keys) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) keys[i] = cell_key(g, ld4(pos + i));
 }
@@ -77,6 +78,7 @@ __global__ void k_fill_cell_ids(GridK g, const float4* __restrict__ pos, uint32_
 // Per-tile histogram of the digit at `shift` (pass 0 of externally supplied keys).
 __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
                                                             int bits, uint32_t* __restrict__ hist) {
+  pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
   TileHistogram th;
   th.init(s_hist, bits);
@@ -94,6 +96,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __re
 // Used when the tiles fit one block per digit group (up to kScanTilesPerGroup tiles).
 __global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, uint32_t tiles, int bins,
                                                    uint32_t* __restrict__ totals) {
+  pdl_enter();
   __shared__ uint32_t s_part[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
@@ -138,6 +141,7 @@ __device__ __forceinline__ void scan_group_range(uint32_t tiles, uint32_t groups
 
 __global__ void __launch_bounds__(256) k_sort_scan_part(const uint32_t* __restrict__ hist, uint32_t tiles, int bins,
                                                         uint32_t* __restrict__ part) {
+  pdl_enter();
   __shared__ uint32_t s_part[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
@@ -161,6 +165,7 @@ __global__ void __launch_bounds__(256) k_sort_scan_part(const uint32_t* __restri
 __global__ void __launch_bounds__(256) k_sort_scan_final(uint32_t* __restrict__ hist, uint32_t tiles, int bins,
                                                          const uint32_t* __restrict__ part,
                                                          uint32_t* __restrict__ totals) {
+  pdl_enter();
   __shared__ uint32_t s_part[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
@@ -233,6 +238,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ idx_in, uint32_t n, int shift, int bits,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ idx_out, uint32_t* __restrict__ hist_next, int next_shift, int next_bits, GatherList g) {
+  pdl_enter();
   __shared__ uint32_t s_base[kMaxBins];    // global start of (this tile, digit)
   __shared__ uint32_t s_lstart[kMaxBins];  // tile-local start of each digit
   __shared__ uint32_t s_wc[kSortWarps][kMaxBins];
@@ -354,6 +360,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
 // for the first slot of every scene.
 __global__ void k_cell_table_fill(const uint32_t* __restrict__ sk, uint32_t n, uint32_t nc, uint2* __restrict__ table,
                                   const uint16_t* __restrict__ sceneOf) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t k = __ldg(sk + i);
@@ -369,6 +376,7 @@ __global__ void k_cell_table_fill(const uint32_t* __restrict__ sk, uint32_t n, u
 // Internal encoding -> reference format (start, end inclusive, capped; empty = (1, 0)).
 // In place is allowed: each thread reads and writes only its own cell.
 __global__ void k_cell_table_ref(const uint2* table, uint32_t nc, uint32_t cap, uint2* out) {
+  pdl_enter();
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const uint2 se = table[c];
@@ -385,16 +393,28 @@ static int check_launch(const char* what) {
 int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L) {
   if (n == 0) return RTP_OK;
   L.begin("fillCellIDs");
-  k_fill_cell_ids<<<(n + 255) / 256, 256, 0, L.stream>>>(g, pos, n, keys);
+  launch(L, k_fill_cell_ids, dim3((n + 255) / 256), dim3(256), g, pos, n, keys);
   L.end("fillCellIDs");
   return check_launch("k_fill_cell_ids");
 }
 
 int launch_sort_histogram(const SortPlan& p, const uint32_t* keys, const SortScratch& s, Launcher& L) {
   L.begin("sort_hist0");
-  k_sort_hist<<<p.tiles, kSortThreads, 0, L.stream>>>(keys, p.n, 0, p.bits[0], s.hist);
+  launch(L, k_sort_hist, dim3(p.tiles), dim3(kSortThreads), keys, p.n, 0, p.bits[0], s.hist);
   L.end("sort_hist0");
   return check_launch("k_sort_hist");
+}
+
+ZeroJob step_zero_job(const SortPlan& p, const SortScratch& s, uint2* table, uint32_t nc) {
+  ZeroJob z;
+  if (p.passes > 1) {
+    const size_t per = (size_t)p.tiles * kMaxBins;
+    z.p[0] = s.hist + per;
+    z.n[0] = (uint32_t)(per * (p.passes - 1));
+  }
+  z.p[1] = reinterpret_cast<uint32_t*>(table);
+  z.n[1] = 2u * nc;
+  return z;
 }
 
 int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L) {
@@ -420,11 +440,11 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
     const uint32_t groups = scan_groups(p.tiles);
     L.begin("sort_scan");
     if (groups <= 1) {
-      k_sort_scan<<<(bins + 31) / 32, 256, 0, L.stream>>>(hist, p.tiles, bins, totals);
+      launch(L, k_sort_scan, dim3((bins + 31) / 32), dim3(256), hist, p.tiles, bins, totals);
     } else {
       const dim3 grid((bins + 31) / 32, groups);
-      k_sort_scan_part<<<grid, 256, 0, L.stream>>>(hist, p.tiles, bins, s.scanPart);
-      k_sort_scan_final<<<grid, 256, 0, L.stream>>>(hist, p.tiles, bins, s.scanPart, totals);
+      launch(L, k_sort_scan_part, dim3(grid), dim3(256), hist, p.tiles, bins, s.scanPart);
+      launch(L, k_sort_scan_final, dim3(grid), dim3(256), hist, p.tiles, bins, s.scanPart, totals);
     }
     L.end("sort_scan");
     int rc = check_launch("k_sort_scan");
@@ -434,12 +454,12 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
     if (!last && kout == kin) kout = (kout == s.keysA) ? s.keysB : s.keysA;
     if (last) {
       L.begin("sort_pass_gather");
-      k_sort_pass<true><<<p.tiles, kSortThreads, 0, L.stream>>>(kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+      launch(L, k_sort_pass<true>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
                                                                 totals, kout, nullptr, nullptr, 0, 1, g);
       L.end("sort_pass_gather");
     } else {
       L.begin("sort_pass");
-      k_sort_pass<false><<<p.tiles, kSortThreads, 0, L.stream>>>(kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+      launch(L, k_sort_pass<false>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
                                                                  totals, kout, iout, hist + per, p.shift[pass + 1],
                                                                  p.bits[pass + 1], g);
       L.end("sort_pass");
@@ -453,20 +473,22 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
 }
 
 int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L,
-                      const uint16_t* sceneOf) {
-  L.begin("cellTableClear");
-  RTP_CUDA(cudaMemsetAsync(table, 0, sizeof(uint2) * g.nc, L.stream));
-  L.end("cellTableClear");
+                      const uint16_t* sceneOf, bool cleared) {
+  if (!cleared) {
+    L.begin("cellTableClear");
+    RTP_CUDA(cudaMemsetAsync(table, 0, sizeof(uint2) * g.nc, L.stream));
+    L.end("cellTableClear");
+  }
   if (n == 0) return RTP_OK;
   L.begin("cellTable");
-  k_cell_table_fill<<<(n + 255) / 256, 256, 0, L.stream>>>(sorted_keys, n, g.nc, table, sceneOf);
+  launch(L, k_cell_table_fill, dim3((n + 255) / 256), dim3(256), sorted_keys, n, g.nc, table, sceneOf);
   L.end("cellTable");
   return check_launch("k_cell_table_fill");
 }
 
 int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L) {
   L.begin("cellTableRef");
-  k_cell_table_ref<<<(g.nc + 255) / 256, 256, 0, L.stream>>>(table, g.nc, g.cap, out);
+  launch(L, k_cell_table_ref, dim3((g.nc + 255) / 256), dim3(256), table, g.nc, g.cap, out);
   L.end("cellTableRef");
   return check_launch("k_cell_table_ref");
 }

@@ -27,9 +27,28 @@ struct Launcher {
   cudaStream_t stream = nullptr;
   bool profiling = false;
   void* owner = nullptr;  // Handle* when profiling
+  bool pdl = false;       // launch with programmatic dependent launch allowed
   int begin(const char* name);
   int end(const char* name);
 };
+
+// Launches kernel k on L's stream (errors are reported by cudaGetLastError, as for <<< >>>).
+// With L.pdl the launch allows programmatic dependent launch; every kernel launched here calls
+// pdl_enter() before it reads anything, so it never reads a predecessor's output early.
+template <class... P, class... A>
+inline void launch(const Launcher& L, void (*k)(P...), dim3 grid, dim3 block, A&&... a) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = L.pdl ? 1u : 0u;
+  (void)cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(a)...);
+}
 
 // ---- Radix sort ---------------------------------------------------------------------
 struct SortPlan {
@@ -82,8 +101,12 @@ int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L);
 
 // Cell table in the internal [begin, endExcl) encoding from sorted keys (sceneOf: the scene
 // of every slot of a batch, or nullptr).
+// cleared: the table was zeroed already (by the key-producing kernel's ZeroJob).
 int launch_cell_table(const GridK& g, const uint32_t* sorted_keys, uint32_t n, uint2* table, Launcher& L,
-                      const uint16_t* sceneOf = nullptr);
+                      const uint16_t* sceneOf = nullptr, bool cleared = false);
+// What the key-producing kernel of a model step clears: the histograms of sort passes >= 1
+// (instead of launch_sort_clear) and the cell table (instead of its memset).
+ZeroJob step_zero_job(const SortPlan& p, const SortScratch& s, uint2* table, uint32_t nc);
 // Internal encoding -> the reference's inclusive (start, end) with (1, 0) for empty cells.
 int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L);
 int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L);

@@ -368,8 +368,8 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
   const uint32_t n = (uint32_t)h->curN;
   const GridK& g = h->g;
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
-  RTP_TRY(launch_sort_clear(plan, h->ss, L));
-  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L));
+  const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
+  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L, zero));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -382,7 +382,7 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
   gl.dst1[0] = h->idsS;
   gl.n1 = 1;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
-  return launch_cell_table(g, h->cellId, n, h->table, L, h->isBatch ? h->dSceneOf : nullptr);
+  return launch_cell_table(g, h->cellId, n, h->table, L, h->isBatch ? h->dSceneOf : nullptr, true);
 }
 
 // `count` plain Jacobi iterations from `in`; the outputs alternate between dest and spare
@@ -540,9 +540,9 @@ static int record_boids_step(Handle* h, Launcher& L) {
   if (n == 0) return RTP_OK;
   const GridK& g = h->g;
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
-  RTP_TRY(launch_sort_clear(plan, h->ss, L));
+  const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
   // Boids.cpp:335-344.
-  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L));
+  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L, zero));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -553,7 +553,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
   gl.dst1[0] = h->idsS;
   gl.n1 = 1;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
-  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L, nullptr, true));
   // Boids.cpp:346-373.
   BoidsK bk;
   bk.velocityScale = h->bp.velocityScale;
@@ -600,10 +600,10 @@ int record_clouds_step(Handle* h, Launcher& L) {
   const FluidK fk = fluidk_of(h);
   const CloudK ck = make_cloudk(h);
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
-  RTP_TRY(launch_sort_clear(plan, h->ss, L));
+  const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
   // Clouds.cpp:516-541: thermodynamics, predict, mixed boundary, cell ids.
   RTP_TRY(cloud_presort(g, ck, h->pos, h->vel, n, h->temp, h->vapor, h->cloud, h->buoy, h->predTmp, h->totCorr,
-                        h->ss.keysA, plan, h->ss.hist, L));
+                        h->ss.keysA, plan, h->ss.hist, L, zero));
   // Clouds.cpp:543.
   GatherList gl;
   gl.src4[0] = h->pos;
@@ -627,7 +627,7 @@ int record_clouds_step(Handle* h, Launcher& L) {
   gl.dst1[4] = h->idsS;
   gl.n1 = 5;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
-  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L));
+  RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L, nullptr, true));
   // Clouds.cpp:554-567.
   if (ck.smoothing) RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, h->pairs, L));
   // Clouds.cpp:570-590.

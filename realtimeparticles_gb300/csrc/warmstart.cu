@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
                 float* __restrict__ lambda, float* __restrict__ density, float* __restrict__ lamTot, PairList pl,
                 uint32_t stride, uint32_t phase, float* __restrict__ feats, uint32_t capacity, MlpDev m,
                 float4* __restrict__ res) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n;
   float f[kMlpIn];
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(128) k_ws_record_targets(GridK g, FluidK p, co
                                                            const float4* __restrict__ xFinal, PairList pl0,
                                                            uint32_t stride, uint32_t phase, uint32_t count,
                                                            float* __restrict__ targets) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t s = t / kQuad, q = t % kQuad;
   const uint32_t i = phase + s * stride;
@@ -188,6 +190,7 @@ template <bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads) k_ws_density_error(GridK g, FluidK p, const float4* __restrict__ pos,
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float* __restrict__ errPartial) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
   if (i < n) {
@@ -211,6 +214,7 @@ constexpr int kGuardThreads = 256;
 __global__ void __launch_bounds__(kGuardThreads) k_ws_guard(const float* __restrict__ part, uint32_t nblk, uint32_t n,
                                                            float tol, SolverStatsDev* st,
                                                            cudaGraphConditionalHandle hnd, int hasCond, int accept) {
+  pdl_enter();
   __shared__ double s_sum[kGuardThreads];
   double v = 0.0;
   for (uint32_t b = threadIdx.x; b < nblk; b += kGuardThreads) v += (double)part[b];
@@ -252,7 +256,7 @@ int ws_lambda_record(const GridK& g, const FluidK& p, const float4* pred, const 
   MlpDev m{};
   L.begin("ws_lambda_record");
   if (p.bt.scenes) return fail(RTP_ERR_NOT_SUPPORTED, "sample recording runs on single scenes");
-  k_ws_lambda<kRecord, false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+  launch(L, k_ws_lambda<kRecord, false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
       g, p, pred, velS, table, n, lambda, density, lamTot, pl, stride, phase, feats, capacity, m, nullptr);
   L.end("ws_lambda_record");
   return check("k_ws_lambda<record>");
@@ -263,10 +267,10 @@ int ws_lambda_infer(const GridK& g, const FluidK& p, const float4* pred, const f
   const MlpDev m = mlp_dev(mlpBlock);
   L.begin("ws_lambda_mlp");
   if (p.bt.scenes)
-    k_ws_lambda<kInfer, true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+    launch(L, k_ws_lambda<kInfer, true>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
         g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
   else
-    k_ws_lambda<kInfer, false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(
+    launch(L, k_ws_lambda<kInfer, false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
         g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
   L.end("ws_lambda_mlp");
   return check("k_ws_lambda<infer>");
@@ -277,7 +281,7 @@ int ws_record_targets(const GridK& g, const FluidK& p, const float4* x0, const f
                       uint32_t count, float* targets, Launcher& L) {
   if (count == 0) return RTP_OK;
   L.begin("ws_record_targets");
-  k_ws_record_targets<<<blocks(count * kQuad, 128), 128, 0, L.stream>>>(g, p, x0, lamTot, table, n, xFinal, pl0, stride,
+  launch(L, k_ws_record_targets, dim3(blocks(count * kQuad, 128)), dim3(128), g, p, x0, lamTot, table, n, xFinal, pl0, stride,
                                                                          phase, count, targets);
   L.end("ws_record_targets");
   return check("k_ws_record_targets");
@@ -287,9 +291,9 @@ int ws_density_error(const GridK& g, const FluidK& p, const float4* pos, const u
                      float* errPartial, Launcher& L) {
   L.begin("ws_density_error");
   if (p.bt.scenes)
-    k_ws_density_error<true><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
+    launch(L, k_ws_density_error<true>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, pos, table, n, errPartial);
   else
-    k_ws_density_error<false><<<blocks(n, kSweepThreads), kSweepThreads, 0, L.stream>>>(g, p, pos, table, n, errPartial);
+    launch(L, k_ws_density_error<false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, pos, table, n, errPartial);
   L.end("ws_density_error");
   return check("k_ws_density_error");
 }
@@ -297,7 +301,7 @@ int ws_density_error(const GridK& g, const FluidK& p, const float4* pos, const u
 int ws_guard(const float* errPartial, uint32_t n, float tol, SolverStatsDev* st, cudaGraphConditionalHandle hnd,
              bool hasCond, bool accept, Launcher& L) {
   L.begin(accept ? "ws_accept" : "ws_guard");
-  k_ws_guard<<<1, kGuardThreads, 0, L.stream>>>(errPartial, ws_error_blocks(n), n, tol, st, hnd, hasCond ? 1 : 0,
+  launch(L, k_ws_guard, dim3(1), dim3(kGuardThreads), errPartial, ws_error_blocks(n), n, tol, st, hnd, hasCond ? 1 : 0,
                                                 accept ? 1 : 0);
   L.end(accept ? "ws_accept" : "ws_guard");
   return check("k_ws_guard");
