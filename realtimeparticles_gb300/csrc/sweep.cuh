@@ -65,6 +65,26 @@ __device__ __forceinline__ void visit_range_x4(uint32_t b, uint32_t e, G&& g, F&
   for (; j < e; ++j) f(j, g(j));
 }
 
+// As visit_range_x4 with eight loads in flight first (the distance-only filter passes, whose
+// per-candidate work is small enough to keep eight positions in registers).
+template <class G, class F>
+__device__ __forceinline__ void visit_range_x8(uint32_t b, uint32_t e, G&& g, F&& f) {
+  uint32_t j = b;
+  for (; j + 8 <= e; j += 8) {
+    const auto a0 = g(j), a1 = g(j + 1), a2 = g(j + 2), a3 = g(j + 3);
+    const auto a4 = g(j + 4), a5 = g(j + 5), a6 = g(j + 6), a7 = g(j + 7);
+    f(j, a0);
+    f(j + 1, a1);
+    f(j + 2, a2);
+    f(j + 3, a3);
+    f(j + 4, a4);
+    f(j + 5, a5);
+    f(j + 6, a6);
+    f(j + 7, a7);
+  }
+  visit_range_x4(j, e, g, f);
+}
+
 // Walks list entries begin, begin + step, ... < end in order, four at a time: the four
 // indices idx(kk) are loaded, then g(j) loads each pair's operands, then f(j, loaded)
 // consumes them, so a lane keeps several dependent load chains in flight.
@@ -137,12 +157,12 @@ __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const
       } else if (ce == rb[r]) {
         ce = re[r];
       } else {
-        visit_range_x4(cb, ce, ld, test);
+        visit_range_x8(cb, ce, ld, test);
         cb = rb[r];
         ce = re[r];
       }
     }
-    visit_range_x4(cb, ce, ld, test);
+    visit_range_x8(cb, ce, ld, test);
   });
 }
 
