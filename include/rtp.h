@@ -243,7 +243,11 @@ int rtp_clouds_init(void* handle);
 int rtp_set_nb_particles(void* handle, uint64_t n);
 int rtp_get_nb_particles(void* handle, uint64_t* n);
 int rtp_set_boundary(void* handle, int boundary);
-int rtp_set_dimension(void* handle, uint32_t dim); /* triggers reset, Model.hpp:109-113 */
+/* Model::setDimension (Model.hpp:109-113): stores the dimension and resets.  A 2D model keeps
+ * its particles in the x = 0 plane (the reference's YZ cases, Fluids.cpp:287-333,
+ * Boids.cpp:291-299, Clouds.cpp:417-446); boids use the 9-cell 2D rules (boids.cl:137-221),
+ * fluids and clouds the same kernels as in 3D with dim = 2 in their parameters. */
+int rtp_set_dimension(void* handle, uint32_t dim);
 int rtp_set_case(void* handle, int pcase);
 int rtp_pause(void* handle, int pause);
 

@@ -42,6 +42,8 @@ def lib():
                                      C.c_uint32, P]
         L.or_boids_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.BoidsParams), C.c_float,
                                     C.c_int, C.c_uint32, P]
+        L.or_boids_step_dim.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.BoidsParams), C.c_float,
+                                        C.c_int, C.c_int, C.c_uint32, P]
         L.or_clouds_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
                                      C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P, C.c_uint32,
                                      C.c_uint32, P]
@@ -159,10 +161,10 @@ def fluids_step(c, fp, iters, st):
         raise ValueError("or_fluids_step failed: %d" % rc)
 
 
-def boids_step(c, bp, dt, boundary, st):
+def boids_step(c, bp, dt, boundary, st, dim=3):
     n = st["pos"].shape[0]
     s = _state(st)
-    rc = lib().or_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), n, C.byref(s))
+    rc = lib().or_boids_step_dim(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), n, C.byref(s))
     if rc != 0:
         raise ValueError("or_boids_step failed: %d" % rc)
 
@@ -298,7 +300,7 @@ def ref_lib():
         L.ref_fill_cell_ids.argtypes = [G, P, C.c_uint32, P]
         L.ref_cell_table.argtypes = [G, P, C.c_uint32, P]
         L.ref_fluids_step.argtypes = [G, C.POINTER(abi.FluidParams), C.c_uint32, C.c_uint32, P]
-        L.ref_boids_step.argtypes = [G, C.POINTER(abi.BoidsParams), C.c_float, C.c_int, C.c_uint32, P]
+        L.ref_boids_step.argtypes = [G, C.POINTER(abi.BoidsParams), C.c_float, C.c_int, C.c_int, C.c_uint32, P]
         L.ref_clouds_step.argtypes = [G, C.POINTER(abi.FluidParams), C.POINTER(abi.CloudParams), C.c_uint32,
                                       C.c_uint32, P]
         L.ref_clouds_init.argtypes = [G, C.POINTER(abi.CloudParams), C.c_uint32, P]
@@ -325,9 +327,10 @@ def ref_fluids_step(c, fp, iters, st):
     ref_lib().ref_fluids_step(C.byref(c), C.byref(fp), int(iters), st["pos"].shape[0], C.byref(s))
 
 
-def ref_boids_step(c, bp, dt, boundary, st):
+def ref_boids_step(c, bp, dt, boundary, st, dim=3):
     s = _state(st)
-    ref_lib().ref_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), st["pos"].shape[0], C.byref(s))
+    ref_lib().ref_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), st["pos"].shape[0],
+                             C.byref(s))
 
 
 def ref_clouds_step(c, fp, cp, iters, st):

@@ -179,6 +179,23 @@ inline void boid_neighbours(const Grid& g, const uint32_t* table, f4 pos, F&& f)
       }
 }
 
+// Neighbour loop of the 2D boids kernel (boids.cl:167-212): the 9 cells (0, iY, iZ) around the
+// particle's cell, all three indices range-checked against GRID_RES_X, and the cell index
+// taken in the x = GRID_RES_X / 2 plane: (GRID_RES_X / 2 * GRID_RES_X + y) * GRID_RES_Y + z.
+template <class F>
+inline void boid_neighbours_2d(const Grid& g, const uint32_t* table, f4 pos, F&& f) {
+  uint32_t c3[3];
+  g.cell3(pos, c3);
+  for (int iY = -1; iY <= 1; ++iY)
+    for (int iZ = -1; iZ <= 1; ++iZ) {
+      const int nx = (int)c3[0], ny = (int)c3[1] + iY, nz = (int)c3[2] + iZ;
+      if (nx < 0 || ny < 0 || nz < 0 || nx >= g.R[0] || ny >= g.R[0] || nz >= g.R[0]) continue;
+      const uint32_t c1 = (uint32_t)((g.R[0] / 2 * g.R[0] + ny) * g.R[1] + nz);
+      const uint32_t s = table[2 * c1], e = table[2 * c1 + 1];
+      for (uint32_t k = s; k <= e; ++k) f(k);
+    }
+}
+
 struct Sph {
   float h, poly6c, spikyc;
   explicit Sph(const rtp_grid_constants* c) : h(c->effectRadius), poly6c(c->poly6Coeff), spikyc(c->spikyCoeff) {}
@@ -806,7 +823,12 @@ void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, co
 
 int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary,
                   uint32_t n, or_state* s) {
-  if (!c || !p || !s || !s->pos || !s->vel) return RTP_ERR_INVALID_ARGUMENT;
+  return or_boids_step_dim(c, p, dt, boundary, 3, n, s);
+}
+
+int or_boids_step_dim(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary, int dim,
+                      uint32_t n, or_state* s) {
+  if (!c || !p || !s || !s->pos || !s->vel || (dim != 2 && dim != 3)) return RTP_ERR_INVALID_ARGUMENT;
   const Grid g(c);
   float* pos = s->pos;
   float* vel = s->vel;
@@ -822,13 +844,14 @@ int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float 
 
   std::vector<float> acc(4 * (size_t)n);
   const float R2 = c->effectRadiusSquared;
-  // bd_applyBoidsRulesWithGrid3D, boids.cl:46-132.
+  // bd_applyBoidsRulesWithGrid3D, boids.cl:46-132 (2D: bd_applyBoidsRulesWithGrid2D, :137-221;
+  // Boids.cpp:346-349 picks it when the model is 2D).
   OR_PARALLEL_FOR
   for (int64_t i = 0; i < (int64_t)n; ++i) {
     const f4 x = ld4(pos, i);
     int count = 0;
     f4 newAcc = splat(0.0f), avgPos = splat(0.0f), avgVel = splat(0.0f), repulse = splat(0.0f);
-    boid_neighbours(g, table.data(), x, [&](uint32_t e) {
+    auto rule = [&](uint32_t e) {
       const f4 posN = ld4(pos, e);
       const f4 vec = x - posN;
       const float sq = dot(vec, vec);
@@ -838,7 +861,11 @@ int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float 
         repulse = repulse + vec / sq;
         ++count;
       }
-    });
+    };
+    if (dim == 2)
+      boid_neighbours_2d(g, table.data(), x, rule);
+    else
+      boid_neighbours(g, table.data(), x, rule);
     if (count != 0) {
       avgPos = avgPos / (float)count;
       avgPos = avgPos - x;

@@ -63,6 +63,9 @@ int or_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* p, uint3
 /* One Boids::update (Boids.cpp:323-377, target rule off, dt a parameter). */
 int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt,
                   int boundary, uint32_t n, or_state* s);
+/* The same for a 2D (dim = 2) or 3D model. */
+int or_boids_step_dim(const rtp_grid_constants* c, const rtp_boids_params* p, float dt,
+                      int boundary, int dim, uint32_t n, or_state* s);
 /* One Clouds::update (Clouds.cpp:503-610). `ground` may be NULL (constant groundTemp0). */
 int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp,
                    const rtp_cloud_params* cp, const rtp_cloud_env* env, const float* ground,

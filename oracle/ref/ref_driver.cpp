@@ -173,7 +173,7 @@ int ref_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, uin
 }
 
 // Boids::update (Boids.cpp:335-373), target rule off, dt a parameter.
-int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, float dt, int boundary, uint32_t n,
+int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, float dt, int boundary, int dim, uint32_t n,
                    or_state* s) {
   ref_consts = *c;
   const ref_boids::BoidsRuleParams P = as<ref_boids::BoidsRuleParams>(*bp);
@@ -190,7 +190,10 @@ int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, floa
   const uint2* T = reinterpret_cast<const uint2*>(table.data());
   std::vector<float> acc(4 * (size_t)n);
   float4* A = F4(acc.data());
-  run(n, [&] { ref_boids::bd_applyBoidsRulesWithGrid3D(pos, vel, T, P, A); });
+  if (dim == 2)  // Boids.cpp:346-349
+    run(n, [&] { ref_boids::bd_applyBoidsRulesWithGrid2D(pos, vel, T, P, A); });
+  else
+    run(n, [&] { ref_boids::bd_applyBoidsRulesWithGrid3D(pos, vel, T, P, A); });
   const float vmax = bp->velocityScale;
   run(n, [&] { ref_boids::bd_updateVel(A, dt, vmax, vel); });
   if (boundary == RTP_BOUNDARY_CYCLIC_WALL)

@@ -4,7 +4,7 @@
 //   k_boids_keys          fillCellIDs(pos) + sort-tile histogram
 //   sort passes           RadixSort::sort of {pos, vel} (+ ids); acc is recomputed each step
 //   cell table            start/end (cap 3000, Boids.cpp:78)
-//   k_boids_rules_update  bd_applyBoidsRulesWithGrid3D + bd_updateVel + the boundary
+//   k_boids_rules_update  bd_applyBoidsRulesWithGrid3D (2D models: ...Grid2D) + bd_updateVel + the boundary
 //                         condition (bd_updatePosAndApplyPeriodicBC / ...WallBC), reading
 //                         the sorted copies and writing the canonical pos/vel buffers.
 #include "boids.cuh"
@@ -38,7 +38,7 @@ __device__ __forceinline__ float4 fnorm(float4 a) {
   return a * rsqrtf(d);
 }
 
-template <bool PERIODIC>
+template <bool PERIODIC, bool DIM2>
 __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, const float4* __restrict__ posS,
                                                             const float4* __restrict__ velS,
                                                             const uint2* __restrict__ table, uint32_t n,
@@ -53,29 +53,51 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
   cell3(g, xi, cx, cy, cz);
   int count = 0;
   float4 sp = f4(0.f, 0.f, 0.f, 0.f), sv = sp, sr = sp;
-  // bd_applyBoidsRulesWithGrid3D (boids.cl:78-113): 27 cells, no wrap.
-  for (int dx = -1; dx <= 1; ++dx) {
-    const int nx = cx + dx;
-    if (nx < 0 || nx >= g.R[0]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int ny = cy + dy;
-      if (ny < 0 || ny >= g.R[1]) continue;
-      const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
-      for (int dz = -1; dz <= 1; ++dz) {
-        const int nz = cz + dz;
-        if (nz < 0 || nz >= g.R[2]) continue;
-        uint32_t j0, j1;
-        cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
-        for (uint32_t j = j0; j < j1; ++j) {
-          const float4 xj = ld4(posS + j);
-          const float4 v = xi - xj;
-          const float sq = dot4(v, v);
-          if (sq < g.boidsR2 && sq > kFloatEps) {
-            sp = sp + xj;
-            sv = sv + fnorm(ld4(velS + j));
-            sr = sr + v * (1.0f / sq);
-            ++count;
-          }
+  auto rule = [&](uint32_t j0, uint32_t j1) {
+    for (uint32_t j = j0; j < j1; ++j) {
+      const float4 xj = ld4(posS + j);
+      const float4 v = xi - xj;
+      const float sq = dot4(v, v);
+      if (sq < g.boidsR2 && sq > kFloatEps) {
+        sp = sp + xj;
+        sv = sv + fnorm(ld4(velS + j));
+        sr = sr + v * (1.0f / sq);
+        ++count;
+      }
+    }
+  };
+  if (DIM2) {
+    // bd_applyBoidsRulesWithGrid2D (boids.cl:167-212): the 9 cells (0, dy, dz), every index
+    // checked against GRID_RES_X, cells taken in the x = GRID_RES_X / 2 plane.
+    const int R = g.R[0];
+    if (cx >= 0 && cx < R) {
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int ny = cy + dy;
+        if (ny < 0 || ny >= R) continue;
+        for (int dz = -1; dz <= 1; ++dz) {
+          const int nz = cz + dz;
+          if (nz < 0 || nz >= R) continue;
+          uint32_t j0, j1;
+          cell_range(table, (uint32_t)((R / 2 * R + ny) * g.R[1] + nz), g.cap, j0, j1);
+          rule(j0, j1);
+        }
+      }
+    }
+  } else {
+    // bd_applyBoidsRulesWithGrid3D (boids.cl:78-113): 27 cells, no wrap.
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int nx = cx + dx;
+      if (nx < 0 || nx >= g.R[0]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int ny = cy + dy;
+        if (ny < 0 || ny >= g.R[1]) continue;
+        const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
+        for (int dz = -1; dz <= 1; ++dz) {
+          const int nz = cz + dz;
+          if (nz < 0 || nz >= g.R[2]) continue;
+          uint32_t j0, j1;
+          cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
+          rule(j0, j1);
         }
       }
     }
@@ -123,15 +145,20 @@ int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys,
   return check("k_boids_keys");
 }
 
-int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, const float4* posS, const float4* velS,
-                       const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, float4* acc,
-                       uint32_t* ids, Launcher& L) {
+int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, bool dim2, const float4* posS,
+                       const float4* velS, const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos,
+                       float4* vel, float4* acc, uint32_t* ids, Launcher& L) {
   const uint32_t b = (n + 127) / 128;
   L.begin("bd_rules_update");
-  if (periodic)
-    launch(L, k_boids_rules_update<true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+  if (periodic && dim2)
+    launch(L, k_boids_rules_update<true, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+  else if (periodic)
+    launch(L, k_boids_rules_update<true, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+  else if (dim2)
+    launch(L, k_boids_rules_update<false, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
   else
-    launch(L, k_boids_rules_update<false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<false, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc,
+           ids);
   L.end("bd_rules_update");
   return check("k_boids_rules_update");
 }

@@ -14,7 +14,7 @@ struct BoidsK {
 
 int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
                   Launcher& L, const ZeroJob& zero = ZeroJob{});
-int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, const float4* posS, const float4* velS,
+int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, bool dim2, const float4* posS, const float4* velS,
                        const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, float4* acc,
                        uint32_t* ids, Launcher& L);
 

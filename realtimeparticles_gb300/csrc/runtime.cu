@@ -562,7 +562,9 @@ static int record_boids_step(Handle* h, Launcher& L) {
   bk.cohesionScale = h->bp.cohesionScale;
   bk.dt = h->boidsDt;
   bk.maxVelocity = h->bp.velocityScale;
-  return boids_rules_update(g, bk, h->boundary == RTP_BOUNDARY_CYCLIC_WALL, h->posS, h->velS, h->table, n, h->idsS,
+  // Boids.cpp:346-349: the 2D rules kernel for a 2D model.
+  return boids_rules_update(g, bk, h->boundary == RTP_BOUNDARY_CYCLIC_WALL, h->mp.dimension == 2, h->posS, h->velS,
+                            h->table, n, h->idsS,
                             h->pos, h->vel, h->acc, h->ids, L);
 }
 
@@ -701,6 +703,89 @@ static void sphere_grid(std::vector<V3>& out, const int res[3], V3 s, V3 e) {
       }
 }
 
+// Geometry::GenerateRectangularGrid in the YZ plane, uniform (utils/Geometry.cpp:70-126):
+// res2 = (count along y, count along z), spacing (0, dy / res2[0], dz / res2[1]).
+static void rect_grid_yz(std::vector<V3>& out, const int res2[2], V3 s, V3 e) {
+  const V3 sp = {0.0f, (e.y - s.y) / res2[0], (e.z - s.z) / res2[1]};
+  for (int iy = 0; iy < res2[0]; ++iy)
+    for (int iz = 0; iz < res2[1]; ++iz) out.push_back({s.x + 0 * sp.x, s.y + iy * sp.y, s.z + iz * sp.z});
+}
+
+// Geometry::GenerateCircularGrid in the YZ plane (utils/Geometry.cpp:128-185): res2 =
+// (angles, radii); radius = |end - start| / 2 around the midpoint.
+static void circle_grid_yz(std::vector<V3>& out, const int res2[2], V3 s, V3 e) {
+  const V3 v = {e.x - s.x, e.y - s.y, e.z - s.z};
+  const V3 c = {s.x + v.x / 2.0f, s.y + v.y / 2.0f, s.z + v.z / 2.0f};
+  const float radius = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z) / 2.0f;
+  const float da = 2.0f * PI_F / res2[0], dr = radius / res2[1];
+  for (int io = 0; io < res2[0]; ++io)
+    for (int ir = 0; ir < res2[1]; ++ir)
+      out.push_back({c.x, c.y + ((ir + 1) * dr) * std::cos(io * da), c.z + ((ir + 1) * dr) * std::sin(io * da)});
+}
+
+// Utils::ALL_NB_PARTICLES subdiv2D (utils/Parameters.hpp:89-98).
+static bool subdiv2(uint64_t n, int out[2]) {
+  static const struct {
+    uint64_t n;
+    int s[2];
+  } T[] = {{512, {32, 16}},    {1024, {32, 32}},   {4096, {64, 64}},   {8192, {128, 64}},
+           {16384, {128, 128}}, {32768, {128, 256}}, {65536, {256, 256}}, {131072, {256, 512}}};
+  for (const auto& e : T)
+    if (e.n == n) {
+      out[0] = e.s[0];
+      out[1] = e.s[1];
+      return true;
+    }
+  return false;
+}
+
+// The 2D cases (particles in the x = 0 plane): Fluids.cpp:287-333, Boids.cpp:291-299,
+// Clouds.cpp:417-446.
+static int case_2d(const Handle* h, std::vector<V3>& verts, uint64_t& n) {
+  const float by = h->mp.boxSize[1], bz = h->mp.boxSize[2];
+  const int pc = h->mp.pCase;
+  int res2[2];
+  if (h->model == RTP_MODEL_FLUIDS) {
+    if (pc == RTP_CASE_FLUIDS_DAM) {
+      n = 4096;
+      subdiv2(n, res2);
+      rect_grid_yz(verts, res2, {0.0f, by / -2.0f, bz / -2.0f}, {0.0f, 0.0f, 0.0f});
+    } else if (pc == RTP_CASE_FLUIDS_BOMB) {
+      n = 4096;
+      subdiv2(n, res2);
+      rect_grid_yz(verts, res2, {0.0f, by / -6.0f, bz / -6.0f}, {0.0f, by / 6.0f, bz / 6.0f});
+    } else if (pc == RTP_CASE_FLUIDS_DROP) {
+      n = 512;
+      subdiv2(n, res2);
+      rect_grid_yz(verts, res2, {0.0f, 2.0f * by / 10.0f, bz / -10.0f}, {0.0f, 4.0f * by / 10.0f, bz / 10.0f});
+      const int bottom[2] = {64, 128};
+      rect_grid_yz(verts, bottom, {0.0f, by / -2.0f, bz / -2.0f}, {0.0f, 0.0f, bz / 2.0f});
+      n += 4096;
+    } else {
+      return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a fluids case");
+    }
+  } else if (h->model == RTP_MODEL_BOIDS) {
+    if (pc == RTP_CASE_BOIDS_SMALL) n = 512;
+    else if (pc == RTP_CASE_BOIDS_MEDIUM) n = 16384;
+    else if (pc == RTP_CASE_BOIDS_LARGE) n = 65536;
+    else if (pc == RTP_CASE_BOIDS_XLARGE) n = 131072;
+    else return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a boids case");
+    subdiv2(n, res2);
+    circle_grid_yz(verts, res2, {0.0f, by / -6.0f, bz / -6.0f}, {0.0f, by / 6.0f, bz / 6.0f});
+  } else {
+    n = 8192;
+    subdiv2(n, res2);
+    const int count = res2[0] * res2[1];
+    if (pc == RTP_CASE_CLOUDS_CUMULUS)
+      box_random(verts, count, {0.0f, by / -2.0f, bz / -2.0f}, {0.0f, 0.0f, bz / 2.0f}, 1);
+    else if (pc == RTP_CASE_CLOUDS_HOMOGENEOUS)
+      box_random(verts, count, {0.0f, by / -2.0f, bz / -2.0f}, {0.0f, by / 2.0f, bz / 2.0f}, 1);
+    else
+      return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_reset: not a clouds case");
+  }
+  return RTP_OK;
+}
+
 // Utils::ALL_NB_PARTICLES subdiv3D (utils/Parameters.hpp:89-98).
 static bool subdiv3(uint64_t n, int out[3]) {
   static const struct {
@@ -724,7 +809,9 @@ static int init_case(Handle* h) {
   int res[3];
   uint64_t n = 0;
   const int pc = h->mp.pCase;
-  if (h->model == RTP_MODEL_FLUIDS) {
+  if (h->mp.dimension == 2) {
+    RTP_TRY(case_2d(h, verts, n));
+  } else if (h->model == RTP_MODEL_FLUIDS) {
     if (pc == RTP_CASE_FLUIDS_DAM) {  // Fluids.cpp:341-346
       n = 131072;
       subdiv3(n, res);
@@ -1020,7 +1107,6 @@ int rtp_create(int model, const rtp_model_params* params, void** out_handle) {
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: currNbParticles > maxNbParticles");
   if (params->dimension != 3 && params->dimension != 2)
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_create: dimension must be 2 or 3");
-  if (params->dimension == 2) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_create: 2D models are not built yet");
   int ndev = 0;
   const cudaError_t de = cudaGetDeviceCount(&ndev);
   if (de != cudaSuccess || ndev == 0) {
@@ -1090,6 +1176,8 @@ int rtp_reset(void* handle) {
   rtp_fluid_params_default(&h->fp);
   rtp_boids_params_default(&h->bp);
   rtp_cloud_params_default(&h->cp);
+  // FluidKernelInputs.dim / CloudKernelInputs.dim follow the model (Fluids.cpp:234, Clouds.cpp:289).
+  h->fp.dim = h->cp.dim = h->mp.dimension == 2 ? 2u : 3u;
   h->iters = (h->model == RTP_MODEL_CLOUDS) ? 1u : 2u;
   h->boidsDt = 0.1f;
   invalidate(h);
@@ -1203,12 +1291,11 @@ int rtp_set_boundary(void* handle, int boundary) {
 
 int rtp_set_dimension(void* handle, uint32_t dim) {
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
-  if (dim == 3) {
-    H(handle)->mp.dimension = 3;
-    return rtp_reset(handle);
-  }
-  if (dim == 2) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_dimension: 2D models are not built yet");
-  return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_dimension: dimension must be 2 or 3");
+  if (dim != 2 && dim != 3) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_dimension: dimension must be 2 or 3");
+  if (H(handle)->isBatch) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_dimension: batches are 3D");
+  // Model::setDimension (Model.hpp:109-113): store, then reset.
+  H(handle)->mp.dimension = dim;
+  return rtp_reset(handle);
 }
 
 int rtp_set_case(void* handle, int pcase) {

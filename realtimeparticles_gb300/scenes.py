@@ -269,3 +269,30 @@ def batched_dam_breaks(count=48, seed=0, n_range=(4096, 65536), aspect_range=(0.
     pos = np.concatenate(poss)
     return {"scenes": descs, "pos": pos, "vel": np.zeros_like(pos), "offsets": offs,
             "fluid_params": fluid_params(lattice_rest_density(d, h)), "h": h, "d": d}
+
+
+def boids_plane(n=4096, box=2.0, res2=None):
+    """The reference's 2D boids start (Boids.cpp:291-299): a circular grid in the x = 0 plane
+    (Geometry::GenerateCircularGrid, utils/Geometry.cpp:128-185) between (0, -box/6, -box/6)
+    and (0, box/6, box/6), velocities = positions (Boids.cpp:317-318).  res2 = (angles, radii)
+    defaults to the reference's subdivision of n."""
+    sub = {512: (32, 16), 1024: (32, 32), 4096: (64, 64), 8192: (128, 64), 16384: (128, 128),
+           32768: (128, 256), 65536: (256, 256), 131072: (256, 512)}
+    na, nr = res2 or sub[n]
+    s = np.array([0.0, -box / 6.0, -box / 6.0], np.float32)
+    e = np.array([0.0, box / 6.0, box / 6.0], np.float32)
+    v = e - s
+    c = s + v / np.float32(2.0)
+    radius = np.float32(np.sqrt(np.float32(v @ v))) / np.float32(2.0)
+    da = np.float32(2.0 * np.pi) / np.float32(na)
+    dr = radius / np.float32(nr)
+    io, ir = np.meshgrid(np.arange(na), np.arange(nr), indexing="ij")
+    ang = (io.ravel().astype(np.float32) * da).astype(np.float32)
+    rad = ((ir.ravel() + 1).astype(np.float32) * dr).astype(np.float32)
+    pos = np.zeros((na * nr, 4), np.float32)
+    pos[:, 0] = c[0]
+    pos[:, 1] = c[1] + rad * np.cos(ang)
+    pos[:, 2] = c[2] + rad * np.sin(ang)
+    res = int(round(box / 0.05))
+    mp = abi.model_params(na * nr, na * nr, (box, box, box), (res, res, res), 2, abi.CASE_INVALID)
+    return {"pos": pos, "vel": pos.copy(), "model_params": mp, "boids_params": boids_params()}

@@ -62,8 +62,12 @@ def test_errors_and_capacity():
         with pytest.raises(RtpError):
             m.setBoundary(7)
         with pytest.raises(RtpError) as e:
+            m.setDimension(4)
+        assert e.value.code == abi.ERR_INVALID_ARGUMENT
+        with pytest.raises(RtpError) as e:  # the 2D dam case needs 4,096 particles: more than the 512 here
+            m.setCase(abi.CASE_FLUIDS_DAM)
             m.setDimension(2)
-        assert e.value.code == abi.ERR_NOT_SUPPORTED
+        assert e.value.code == abi.ERR_CAPACITY
     with pytest.raises(RtpError):
         model.Fluids(abi.model_params(10, 5, (1, 1, 1), (4, 4, 4)))
 

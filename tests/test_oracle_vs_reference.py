@@ -69,11 +69,33 @@ def test_boids_matches_reference(boundary, dt):
             assert _same(a[k], b[k]), k
 
 
-@pytest.mark.parametrize("smoothing,iters", [(1, 1), (0, 2)])
-def test_clouds_matches_reference(smoothing, iters):
+@pytest.mark.parametrize("boundary", [abi.CYCLIC_WALL, abi.BOUNCING_WALL])
+def test_boids_2d_matches_reference(boundary):
+    """The 2D rules kernel (boids.cl:137-221) on the reference's 2D start (x = 0 plane)."""
+    sb = scenes.boids_plane(n=4096)
+    c = oracle.derive_constants(abi.BOIDS, sb["model_params"])
+    n = sb["pos"].shape[0]
+    a, b = _pair(n, c, abi.BOIDS)
+    for st in (a, b):
+        st["pos"][:] = sb["pos"]
+        st["vel"][:] = sb["vel"]
+    for _ in range(4):
+        oracle.boids_step(c, sb["boids_params"], 0.1, boundary, a, dim=2)
+        oracle.ref_boids_step(c, sb["boids_params"], 0.1, boundary, b, dim=2)
+        for k in ("pos", "vel", "acc", "id", "table"):
+            assert _same(a[k], b[k]), k
+    assert np.all(a["pos"][:, 0] == 0.0)  # the plane is kept
+
+
+@pytest.mark.parametrize("smoothing,iters,dim", [(1, 1, 3), (0, 2, 3), (1, 1, 2)])
+def test_clouds_matches_reference(smoothing, iters, dim):
     scc = scenes.clouds_cumulus(n=4000, noise=False, seed=smoothing + 3)
     cp = scc["cloud_params"]
     cp.isTempSmoothingEnabled = smoothing
+    if dim == 2:  # a 2D model: particles in the x = 0 plane, no x wind (clouds.cl:951)
+        cp.dim = 2
+        scc["fluid_params"].dim = 2
+        scc["pos"][:, 0] = 0.0
     c = oracle.derive_constants(abi.CLOUDS, scc["model_params"])
     env = scenes.cloud_env_reference()
     a, b = _pair(4000, c, abi.CLOUDS)
