@@ -179,9 +179,13 @@ typedef enum rtp_buffer {
   RTP_BUF_CELL_TABLE = 11,/* uint2  c_startEndPartID in the reference's inclusive format */
   RTP_BUF_VORTICITY = 12, /* float4 p_vort */
   RTP_BUF_ACC = 13,       /* float4 p_acc (boids) */
-  RTP_BUF_LAMBDA_TOTAL = 14 /* float: lambda summed over the iterations of the last warm-started
-                               or sample-recording step (fluids; the warm start's multiplier
-                               plus the extra iterations' lambdas).  Cleared by uploading POS. */
+  RTP_BUF_LAMBDA_TOTAL = 14, /* float: lambda summed over the iterations of the last warm-started
+                                or sample-recording step (fluids; the warm start's multiplier
+                                plus the extra iterations' lambdas).  Cleared by uploading POS. */
+  RTP_BUF_COLOR = 15,         /* float4 p_col (rtp_fill_fluid_color / rtp_fill_color_float) */
+  RTP_BUF_CAMERA_DIST = 16,   /* uint   p_cameraDist of every slot (rtp_fill_camera_order) */
+  RTP_BUF_DRAW_ORDER = 17,    /* uint   slots in the order the reference draws them */
+  RTP_BUF_GRID_DETECTOR = 18  /* float8 per cell: 1 where a particle is (rtp_fill_grid_detector) */
 } rtp_buffer;
 
 /* Per-kernel device time, collected when profiling is enabled (the reference's
@@ -309,6 +313,24 @@ int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_k
 #define RTP_NOALLOC_SORT_SCRATCH_BYTES 5253120u
 int rtp_radix_sort_noalloc(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint32_t* d_keys_out,
                            uint32_t* d_perm_out, void* stream);
+
+/* ---- Headless side outputs (render-only in the reference) -------------------------------
+ * Computed on demand from the current state into device buffers (rtp_device_ptr /
+ * rtp_download); nothing here changes the simulation state.  The first call allocates the
+ * buffer. */
+/* fld_fillFluidColor (fluids.cl:458-478, Fluids.cpp:459-463) from the last step's density. */
+int rtp_fill_fluid_color(void* handle);
+/* fillColorFloat (utils.cl, Clouds.cpp:612-619): a float buffer (RTP_BUF_DENSITY, _LAMBDA,
+ * _TEMP, _VAPOR, _CLOUD, _BUOYANCY, _LAMBDA_TOTAL) mapped to [0, 1] between minVal and maxVal,
+ * 0 outside, as grey levels. */
+int rtp_fill_color_float(void* handle, int buffer, float minVal, float maxVal);
+/* resetCameraDist + fillCameraDist (utils.cl) for a camera at cameraPos, then the stable
+ * ascending order of those keys (the reference sorts the whole state by them before drawing,
+ * Fluids.cpp:466-468; here the state stays and RTP_BUF_DRAW_ORDER holds the slot order). */
+#define RTP_FAR_DIST 1000000.0f
+int rtp_fill_camera_order(void* handle, const float cameraPos[3]);
+/* resetGridDetector + fillGridDetector (grid.cl:43-60) over the current positions. */
+int rtp_fill_grid_detector(void* handle);
 
 /* ---- Learned warm start of the fluids' constraint solve (new: no counterpart in the
  * reference, whose Jacobi loop starts every substep from a zero correction,

@@ -66,6 +66,10 @@ def lib():
                                  C.POINTER(C.c_int)]
         L.or_ws_record_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.c_uint32,
                                         C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, C.POINTER(C.c_uint32)]
+        L.or_fill_fluid_color.argtypes = [P, C.c_uint32, C.c_float, P]
+        L.or_fill_color_float.argtypes = [P, C.c_uint32, C.c_float, C.c_float, P]
+        L.or_fill_camera_dist.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
+        L.or_fill_grid_detector.argtypes = [C.POINTER(abi.GridConstants), P, C.c_uint32, P]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_threads.restype = C.c_int
         _LIB = L
@@ -213,6 +217,36 @@ def fluid_metrics(c, fp, pred, vel, table):
     return m
 
 
+# ---- side outputs -----------------------------------------------------------------------
+def fill_fluid_color(density, rest_density):
+    d = np.ascontiguousarray(density, dtype=np.float32)
+    out = np.empty((d.shape[0], 4), np.float32)
+    lib().or_fill_fluid_color(_p(d), d.shape[0], float(rest_density), _p(out))
+    return out
+
+
+def fill_color_float(q, vmin, vmax):
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    out = np.empty((q.shape[0], 4), np.float32)
+    lib().or_fill_color_float(_p(q), q.shape[0], float(vmin), float(vmax), _p(out))
+    return out
+
+
+def fill_camera_dist(pos, n, cam):
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    cam = np.ascontiguousarray(cam, dtype=np.float32)
+    out = np.empty(pos.shape[0], np.uint32)
+    lib().or_fill_camera_dist(_p(pos), int(n), pos.shape[0], _p(cam), _p(out))
+    return out
+
+
+def fill_grid_detector(c, pos):
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    out = np.empty((c.numCells, 8), np.float32)
+    lib().or_fill_grid_detector(C.byref(c), _p(pos), pos.shape[0], _p(out))
+    return out
+
+
 # ---- learned warm start (restates the GPU method) ---------------------------------------
 MLP_GRAD_SHAPES = (("w1", (64, 12)), ("b1", (64,)), ("w2", (64, 64)), ("b2", (64,)), ("w3", (4, 64)), ("b3", (4,)))
 
@@ -304,6 +338,10 @@ def ref_lib():
         L.ref_clouds_step.argtypes = [G, C.POINTER(abi.FluidParams), C.POINTER(abi.CloudParams), C.c_uint32,
                                       C.c_uint32, P]
         L.ref_clouds_init.argtypes = [G, C.POINTER(abi.CloudParams), C.c_uint32, P]
+        L.ref_fill_fluid_color.argtypes = [G, C.POINTER(abi.FluidParams), P, C.c_uint32, P]
+        L.ref_fill_color_float.argtypes = [G, P, C.c_uint32, C.c_float, C.c_float, P]
+        L.ref_fill_camera_dist.argtypes = [G, P, C.c_uint32, C.c_uint32, P, P]
+        L.ref_fill_grid_detector.argtypes = [G, P, C.c_uint32, P]
         _REF = L
     return _REF
 
@@ -341,3 +379,22 @@ def ref_clouds_step(c, fp, cp, iters, st):
 def ref_clouds_init(c, cp, st):
     s = _state(st)
     ref_lib().ref_clouds_init(C.byref(c), C.byref(cp), st["pos"].shape[0], C.byref(s))
+
+
+def ref_side_outputs(c, fp, density, q, vmin, vmax, pos, n, cam):
+    """The reference's side-output kernels: (fluid colours, float colours, camera distances,
+    grid detector)."""
+    L = ref_lib()
+    density = np.ascontiguousarray(density, dtype=np.float32)
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    cam = np.ascontiguousarray(cam, dtype=np.float32)
+    col = np.empty((density.shape[0], 4), np.float32)
+    L.ref_fill_fluid_color(C.byref(c), C.byref(fp), _p(density), density.shape[0], _p(col))
+    colf = np.empty((q.shape[0], 4), np.float32)
+    L.ref_fill_color_float(C.byref(c), _p(q), q.shape[0], float(vmin), float(vmax), _p(colf))
+    dist = np.empty(pos.shape[0], np.uint32)
+    L.ref_fill_camera_dist(C.byref(c), _p(pos), int(n), pos.shape[0], _p(cam), _p(dist))
+    det = np.empty((c.numCells, 8), np.float32)
+    L.ref_fill_grid_detector(C.byref(c), _p(pos), int(n), _p(det))
+    return col, colf, dist, det

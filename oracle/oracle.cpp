@@ -781,6 +781,54 @@ int or_ws_record_step(const rtp_grid_constants* c, const rtp_fluid_params* p, ui
   return RTP_OK;
 }
 
+// ---- side outputs (render-only in the reference) -------------------------------------------
+
+void or_fill_fluid_color(const float* density, uint32_t n, float restDensity, float* col) {
+  // fld_fillFluidColor, fluids.cl:458-478.
+  const f4 blue = mk(0.0f, 0.1f, 1.0f, 0.5f), lightBlue = mk(0.7f, 0.7f, 1.0f, 0.5f), darkBlue = mk(0.0f, 0.0f, 0.8f, 0.5f);
+  for (uint32_t i = 0; i < n; ++i) {
+    const float constraint = (1.0f - density[i] / restDensity);
+    f4 color = blue;
+    if (constraint > 0.0f) color = color + (constraint * (lightBlue - blue)) / 0.35f;
+    else if (constraint < 0.0f) color = color + (constraint * (blue - darkBlue)) / 0.35f;
+    st4(col, i, color);
+  }
+}
+
+void or_fill_color_float(const float* q, uint32_t n, float minVal, float maxVal, float* col) {
+  // fillColorFloat, utils.cl.
+  for (uint32_t i = 0; i < n; ++i) {
+    float val = (q[i] - minVal) / (maxVal - minVal);
+    val *= stepf(0.0f, val);
+    val *= stepf(val, 1.0f);
+    st4(col, i, mk(val, val, val, val));
+  }
+}
+
+void or_fill_camera_dist(const float* pos, uint32_t n, uint32_t maxN, const float cam[3], uint32_t* dist) {
+  // resetCameraDist + fillCameraDist, utils.cl.
+  const float FAR = 1000000.0f;  // FAR_DIST, define.cl:9
+  for (uint32_t i = 0; i < maxN; ++i) {
+    if (i >= n) {
+      dist[i] = (uint32_t)FAR;
+      continue;
+    }
+    const float dx = pos[4 * i] - cam[0], dy = pos[4 * i + 1] - cam[1], dz = pos[4 * i + 2] - cam[2];
+    const float len = std::sqrt(dx * dx + dy * dy + dz * dz);
+    dist[i] = (uint32_t)std::fmax(FAR - len * 100.0f, 0.0f);
+  }
+}
+
+void or_fill_grid_detector(const rtp_grid_constants* c, const float* pos, uint32_t n, float* det) {
+  // resetGridDetector + fillGridDetector, grid.cl:43-60.
+  const Grid g(c);
+  std::fill(det, det + 8 * (size_t)c->numCells, 0.0f);
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t k = g.cell1(ld4(pos, i));
+    if (k < c->numCells) std::fill(det + 8 * (size_t)k, det + 8 * (size_t)k + 8, 1.0f);
+  }
+}
+
 void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* pred,
                       const float* vel, const uint32_t* table, uint32_t n, rtp_metrics* m) {
   std::memset(m, 0, sizeof *m);

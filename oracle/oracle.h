@@ -87,6 +87,14 @@ void or_fld_correction(const rtp_grid_constants* c, const rtp_fluid_params* p,
 void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, const float* predPos,
                       const float* vel, const uint32_t* table, uint32_t n, rtp_metrics* m);
 
+/* Side outputs (render-only in the reference): fld_fillFluidColor (fluids.cl:458-478),
+ * fillColorFloat and resetCameraDist + fillCameraDist (utils.cl), resetGridDetector +
+ * fillGridDetector (grid.cl:43-60; 8 floats per cell). */
+void or_fill_fluid_color(const float* density, uint32_t n, float restDensity, float* col);
+void or_fill_color_float(const float* q, uint32_t n, float minVal, float maxVal, float* col);
+void or_fill_camera_dist(const float* pos, uint32_t n, uint32_t maxN, const float cam[3], uint32_t* dist);
+void or_fill_grid_detector(const rtp_grid_constants* c, const float* pos, uint32_t n, float* det);
+
 /* ---- learned warm start (new; restates the GPU method, not a reference kernel) ---------- */
 /* Raw features (rtp.h, RTP_MLP_IN per particle) at the clamped predicted positions x0 of a
  * sorted state: vel = the step's input velocities. */

@@ -285,3 +285,36 @@ void ref_clouds_init(const rtp_grid_constants* c, const rtp_cloud_params* cp, ui
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Side outputs through the reference's own kernels.
+void ref_fill_fluid_color(const rtp_grid_constants* c, const rtp_fluid_params* fp, const float* density, uint32_t n,
+                          float* col) {
+  ref_consts = *c;
+  const ref_fluids::FluidParams P = as<ref_fluids::FluidParams>(*fp);
+  run(n, [&] { ref_fluids::fld_fillFluidColor(density, P, F4(col)); });
+}
+
+void ref_fill_color_float(const rtp_grid_constants* c, const float* q, uint32_t n, float minVal, float maxVal,
+                          float* col) {
+  ref_consts = *c;
+  run(n, [&] { ref_clouds::fillColorFloat(q, minVal, maxVal, F4(col)); });
+}
+
+void ref_fill_camera_dist(const rtp_grid_constants* c, const float* pos, uint32_t n, uint32_t maxN, const float cam[3],
+                          uint32_t* dist) {
+  ref_consts = *c;
+  clshim::float3 cp{cam[0], cam[1], cam[2]};
+  run(maxN, [&] { ref_fluids::resetCameraDist(dist); });
+  run(n, [&] { ref_fluids::fillCameraDist(F4(const_cast<float*>(pos)), &cp, dist); });
+}
+
+void ref_fill_grid_detector(const rtp_grid_constants* c, const float* pos, uint32_t n, float* det) {
+  ref_consts = *c;
+  clshim::float8* d = reinterpret_cast<clshim::float8*>(det);
+  run(c->numCells, [&] { ref_fluids::resetGridDetector(d); });
+  run(n, [&] { ref_fluids::fillGridDetector(F4(const_cast<float*>(pos)), d); });
+}
+
+}  // extern "C"

@@ -78,6 +78,10 @@ _SIGS = {
     "rtp_train_warm_start": [P, P, U64, C.POINTER(abi.TrainConfig), C.POINTER(abi.Mlp), P, P],
     "rtp_mlp_loss_grad": [C.POINTER(abi.Mlp), P, P, P, U64, C.POINTER(C.c_double), C.POINTER(abi.Mlp), P],
     "rtp_mlp_forward": [C.POINTER(abi.Mlp), P, U64, P, P],
+    "rtp_fill_fluid_color": [P],
+    "rtp_fill_color_float": [P, C.c_int, C.c_float, C.c_float],
+    "rtp_fill_camera_order": [P, C.POINTER(C.c_float)],
+    "rtp_fill_grid_detector": [P],
     "rtp_create_batch": [U32, C.POINTER(abi.BatchScene), C.c_float, U32, PP],
     "rtp_batch_scene_range": [P, U32, C.POINTER(U64), C.POINTER(U64)],
     "rtp_batch_scene_constants": [P, U32, C.POINTER(abi.GridConstants)],

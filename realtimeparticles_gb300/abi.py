@@ -54,6 +54,10 @@ BUF_CELL_TABLE = 11
 BUF_VORTICITY = 12
 BUF_ACC = 13
 BUF_LAMBDA_TOTAL = 14
+BUF_COLOR = 15
+BUF_CAMERA_DIST = 16
+BUF_DRAW_ORDER = 17
+BUF_GRID_DETECTOR = 18
 
 
 class ModelParams(C.Structure):

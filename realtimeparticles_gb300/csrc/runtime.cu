@@ -21,6 +21,7 @@
 #include "clouds.cuh"
 #include "fluids.cuh"
 #include "rtp_internal.hpp"
+#include "side.cuh"
 #include "warmstart.cuh"
 
 namespace rtp {
@@ -202,6 +203,12 @@ struct Handle {
   std::vector<rtp_grid_constants> sceneConst;  // each scene's own grid (keys without the base)
   SceneK* dScenes = nullptr;
   uint16_t* dSceneOf = nullptr;
+  // Side outputs (allocated on first use).
+  float4* col = nullptr;
+  uint32_t *camDist = nullptr, *camSorted = nullptr, *drawOrder = nullptr;
+  float* gridDet = nullptr;
+  void* camSortMem = nullptr;
+  SortScratch camSS{};
   uint32_t tableCells = 0;  // cells the table was allocated for
   uint32_t sortKeyBits = 0; // key bits the sort scratch was allocated for
 };
@@ -1328,6 +1335,10 @@ static int buffer_info(Handle* h, int buf, void** dptr, size_t* elem, uint64_t* 
     case RTP_BUF_VORTICITY: *dptr = h->vort; *elem = 16; break;
     case RTP_BUF_ACC: *dptr = h->acc; *elem = 16; break;
     case RTP_BUF_LAMBDA_TOTAL: *dptr = h->lamTot; *elem = 4; break;
+    case RTP_BUF_COLOR: *dptr = h->col; *elem = 16; break;
+    case RTP_BUF_CAMERA_DIST: *dptr = h->camDist; *elem = 4; break;
+    case RTP_BUF_DRAW_ORDER: *dptr = h->drawOrder; *elem = 4; break;
+    case RTP_BUF_GRID_DETECTOR: *dptr = h->gridDet; *elem = 32; *cap = h->gc.numCells; break;
     default: return fail(RTP_ERR_INVALID_ARGUMENT, "unknown buffer");
   }
   if (!*dptr) return fail(RTP_ERR_INVALID_ARGUMENT, "buffer not used by this model");
@@ -1581,6 +1592,83 @@ int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, ui
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   h->hasStep = true;
   *written = count;
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_fill_fluid_color(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_fill_fluid_color: fluids only");
+  if (!h->hasStep) return fail(RTP_ERR_STATE, "rtp_fill_fluid_color: run a step first (density)");
+  if (!h->col) RTP_TRY(dalloc(h, &h->col, h->maxN));
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(side_fluid_color(h->density, (uint32_t)h->curN, h->fp.restDensity, h->col, L));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_fill_color_float(void* handle, int buffer, float minVal, float maxVal) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  Handle* h = H(handle);
+  if (buffer != RTP_BUF_DENSITY && buffer != RTP_BUF_LAMBDA && buffer != RTP_BUF_TEMP && buffer != RTP_BUF_VAPOR &&
+      buffer != RTP_BUF_CLOUD && buffer != RTP_BUF_BUOYANCY && buffer != RTP_BUF_LAMBDA_TOTAL)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_fill_color_float: not a per-particle float buffer");
+  void* q;
+  size_t elem;
+  uint64_t cap;
+  RTP_TRY(buffer_info(h, buffer, &q, &elem, &cap));
+  if (!h->col) RTP_TRY(dalloc(h, &h->col, h->maxN));
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(side_color_float((const float*)q, (uint32_t)h->curN, minVal, maxVal, h->col, L));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_fill_camera_order(void* handle, const float cameraPos[3]) {
+  RTP_GUARD_BEGIN
+  if (!handle || !cameraPos) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  Handle* h = H(handle);
+  const uint32_t M = (uint32_t)h->maxN;
+  if (!h->camDist) {
+    RTP_TRY(dalloc(h, &h->camDist, M));
+    RTP_TRY(dalloc(h, &h->camSorted, M));
+    RTP_TRY(dalloc(h, &h->drawOrder, M));
+    const SortPlan plan = make_sort_plan(M, 20);  // keys <= FAR_DIST < 2^20
+    RTP_CUDA(cudaMalloc(&h->camSortMem, sort_scratch_bytes(plan)));
+    h->allocs.push_back(h->camSortMem);
+    sort_scratch_carve(plan, h->camSortMem, h->camSS);
+  }
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(side_camera_dist(h->pos, (uint32_t)h->curN, M, cameraPos, h->camDist, L));
+  const SortPlan plan = make_sort_plan(M, 20);
+  RTP_TRY(launch_sort_clear(plan, h->camSS, L));
+  RTP_TRY(launch_sort_histogram(plan, h->camDist, h->camSS, L));
+  GatherList gl;
+  gl.perm = h->drawOrder;
+  RTP_TRY(launch_sort_passes(plan, h->camDist, h->camSorted, h->camSS, gl, L));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_fill_grid_detector(void* handle) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
+  Handle* h = H(handle);
+  if (h->isBatch) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_fill_grid_detector: one grid per scene in a batch");
+  if (!h->gridDet) RTP_TRY(dalloc(h, &h->gridDet, (size_t)h->gc.numCells * 8));
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(side_grid_detector(h->g, h->pos, (uint32_t)h->curN, h->gridDet, L));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
   return RTP_OK;
   RTP_GUARD_END
 }

@@ -59,8 +59,8 @@ _CLOUDS_JSON = {
 }
 _CLOUDS_JSON["Fluids"]["Nb Jacobi Iterations"] = [2, 1, 6]
 
-_F4 = {abi.BUF_POS, abi.BUF_VEL, abi.BUF_PRED_POS, abi.BUF_VORTICITY, abi.BUF_ACC}
-_U32 = {abi.BUF_ID, abi.BUF_CELL_ID}
+_F4 = {abi.BUF_POS, abi.BUF_VEL, abi.BUF_PRED_POS, abi.BUF_VORTICITY, abi.BUF_ACC, abi.BUF_COLOR}
+_U32 = {abi.BUF_ID, abi.BUF_CELL_ID, abi.BUF_CAMERA_DIST, abi.BUF_DRAW_ORDER}
 
 
 def _merge_patch(target, patch):
@@ -229,8 +229,15 @@ class Model:
 
     def download(self, buffer, count=None):
         if count is None:
-            count = self.nbParticles() if buffer != abi.BUF_CELL_TABLE else self.constants().numCells
-        if buffer in _F4:
+            if buffer in (abi.BUF_CELL_TABLE, abi.BUF_GRID_DETECTOR):
+                count = self.constants().numCells
+            elif buffer in (abi.BUF_CAMERA_DIST, abi.BUF_DRAW_ORDER):
+                count = self.maxNbParticles()
+            else:
+                count = self.nbParticles()
+        if buffer == abi.BUF_GRID_DETECTOR:
+            out = np.empty((count, 8), np.float32)
+        elif buffer in _F4:
             out = np.empty((count, 4), np.float32)
         elif buffer == abi.BUF_CELL_TABLE:
             out = np.empty((count, 2), np.uint32)
@@ -260,6 +267,20 @@ class Model:
         m = abi.Metrics()
         call("rtp_get_metrics", self._h, C.byref(m))
         return m
+
+    # headless side outputs (render-only in the reference) --------------------------------
+    def fillFluidColor(self):
+        call("rtp_fill_fluid_color", self._h)
+
+    def fillColorFloat(self, buffer, min_val, max_val):
+        call("rtp_fill_color_float", self._h, int(buffer), float(min_val), float(max_val))
+
+    def fillCameraOrder(self, camera_pos):
+        cam = (C.c_float * 3)(*[float(v) for v in camera_pos])
+        call("rtp_fill_camera_order", self._h, cam)
+
+    def fillGridDetector(self):
+        call("rtp_fill_grid_detector", self._h)
 
 
 class Fluids(Model):

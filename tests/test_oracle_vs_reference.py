@@ -109,3 +109,23 @@ def test_clouds_matches_reference(smoothing, iters, dim):
         oracle.ref_clouds_step(c, scc["fluid_params"], cp, iters, b)
         for k in ("pos", "vel", "predPos", "totCorrPos", "temp", "vapor", "cloud", "buoyancy", "id", "cellId"):
             assert _same(a[k], b[k]), k
+
+
+def test_side_outputs_match_reference():
+    """Render-only side outputs: colours, camera distances, grid detector."""
+    sc = scenes.dam_break(lattice=(8, 16, 16))
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    rng = np.random.default_rng(1)
+    n = sc["pos"].shape[0]
+    density = (sc["fluid_params"].restDensity * rng.uniform(0.5, 1.5, n)).astype(np.float32)
+    density[:5] = sc["fluid_params"].restDensity
+    q = rng.uniform(-1, 3, n).astype(np.float32)
+    pos = np.concatenate([sc["pos"], np.full((100, 4), np.inf, np.float32)])
+    pos[:, 3] = 0
+    cam = np.array([0.3, 2.0, -4.0], np.float32)
+    col_r, colf_r, dist_r, det_r = oracle.ref_side_outputs(c, sc["fluid_params"], density, q, 0.0, 2.0, pos, n, cam)
+    assert _same(oracle.fill_fluid_color(density, sc["fluid_params"].restDensity), col_r)
+    assert _same(oracle.fill_color_float(q, 0.0, 2.0), colf_r)
+    assert _same(oracle.fill_camera_dist(pos, n, cam), dist_r)
+    assert _same(oracle.fill_grid_detector(c, pos[:n]), det_r)
+    assert det_r.sum() > 0 and np.all(dist_r[n:] == 1000000)
