@@ -237,6 +237,23 @@ int rtp_get_fluid_params(void* handle, rtp_fluid_params* p);
 int rtp_set_jacobi_iterations(void* handle, uint32_t iters); /* "Nb Jacobi Iterations" */
 int rtp_set_boids_params(void* handle, const rtp_boids_params* p);
 int rtp_set_boids_time_step(void* handle, float dt);  /* Boids.cpp:334 hard-codes 0.1 */
+/* Boids target attractor: the JSON "Target" group (Boids.cpp:45-51, transferred at
+ * :193-202) with TargetKernelInputs (Boids.hpp:22-26).  While enabled, every step moves
+ * the target along its Perlin-noise trajectory (Target::updatePos, Target.cpp:27-50, with
+ * the velocity scale of the rules) and adds bd_addTargetRule (boids.cl:226-241) to the
+ * rules' acceleration before the velocity update (Boids.cpp:351-358).  The trajectory is
+ * a host state of the model: reset does not restart it, disabling pauses it. */
+typedef struct rtp_target_params {
+  int32_t enabled;    /* "Enable##Target" (default 0) */
+  int32_t visible;    /* "Show" (default 1); reported visible only while enabled (Target.hpp:25) */
+  float radiusEffect; /* "Radius"[0] (default 2.0) */
+  int32_t signEffect; /* (int)"Attract": 1 (default); Attract = false gives 0, no effect */
+} rtp_target_params;
+int rtp_target_params_default(rtp_target_params* out);
+int rtp_set_target(void* handle, const rtp_target_params* p);         /* boids only */
+/* Model::targetPos / isTargetActivated / isTargetVisible (physics/Model.hpp:130-132): the
+ * position after the last step taken (0, 0, 0 before the first). Other models: 0 and false. */
+int rtp_get_target(void* handle, float pos[3], int* activated, int* visible);
 int rtp_set_cloud_params(void* handle, const rtp_cloud_params* p);
 int rtp_set_cloud_environment(void* handle, const rtp_cloud_env* env, const float* groundTemp);
 /* cld_initTemperature + cld_initVaporDensity over the current positions, cloud = 0

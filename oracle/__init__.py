@@ -44,6 +44,12 @@ def lib():
                                     C.c_int, C.c_uint32, P]
         L.or_boids_step_dim.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.BoidsParams), C.c_float,
                                         C.c_int, C.c_int, C.c_uint32, P]
+        L.or_boids_step_target.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.BoidsParams), C.c_float,
+                                           C.c_int, C.c_int, P, C.c_float, C.c_int, C.c_uint32, P]
+        L.or_perlin_noise.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float]
+        L.or_perlin_noise.restype = C.c_float
+        L.or_target_trajectory.argtypes = [C.c_float, C.c_int, C.c_float, C.c_uint32, P]
+        L.or_target_trajectory.restype = None
         L.or_clouds_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
                                      C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P, C.c_uint32,
                                      C.c_uint32, P]
@@ -165,12 +171,26 @@ def fluids_step(c, fp, iters, st):
         raise ValueError("or_fluids_step failed: %d" % rc)
 
 
-def boids_step(c, bp, dt, boundary, st, dim=3):
+def boids_step(c, bp, dt, boundary, st, dim=3, target=None, target_radius=2.0, target_sign=1):
+    """One Boids::update; `target` (x, y, z) applies the target rule with that position."""
     n = st["pos"].shape[0]
     s = _state(st)
-    rc = lib().or_boids_step_dim(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), n, C.byref(s))
+    t = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+    rc = lib().or_boids_step_target(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), _p(t),
+                                    float(target_radius), int(target_sign), n, C.byref(s))
     if rc != 0:
         raise ValueError("or_boids_step failed: %d" % rc)
+
+
+def perlin_noise(seed, x, y, z):
+    return float(lib().or_perlin_noise(int(seed), float(x), float(y), float(z)))
+
+
+def target_trajectory(box_width, dim, particles_vel, nsteps):
+    """Target positions after each of nsteps Target::updatePos calls from a new Target: [nsteps, 3]."""
+    out = np.empty((int(nsteps), 3), np.float32)
+    lib().or_target_trajectory(float(box_width), int(dim), float(particles_vel), int(nsteps), _p(out))
+    return out
 
 
 def clouds_init(c, cp, env, ground, st):
@@ -335,6 +355,10 @@ def ref_lib():
         L.ref_cell_table.argtypes = [G, P, C.c_uint32, P]
         L.ref_fluids_step.argtypes = [G, C.POINTER(abi.FluidParams), C.c_uint32, C.c_uint32, P]
         L.ref_boids_step.argtypes = [G, C.POINTER(abi.BoidsParams), C.c_float, C.c_int, C.c_int, C.c_uint32, P]
+        L.ref_boids_step_target.argtypes = [G, C.POINTER(abi.BoidsParams), C.c_float, C.c_int, C.c_int, P,
+                                            C.c_float, C.c_int, C.c_uint32, P]
+        L.ref_perlin_noise.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float]
+        L.ref_perlin_noise.restype = C.c_float
         L.ref_clouds_step.argtypes = [G, C.POINTER(abi.FluidParams), C.POINTER(abi.CloudParams), C.c_uint32,
                                       C.c_uint32, P]
         L.ref_clouds_init.argtypes = [G, C.POINTER(abi.CloudParams), C.c_uint32, P]
@@ -365,10 +389,17 @@ def ref_fluids_step(c, fp, iters, st):
     ref_lib().ref_fluids_step(C.byref(c), C.byref(fp), int(iters), st["pos"].shape[0], C.byref(s))
 
 
-def ref_boids_step(c, bp, dt, boundary, st, dim=3):
+def ref_boids_step(c, bp, dt, boundary, st, dim=3, target=None, target_radius=2.0, target_sign=1):
     s = _state(st)
-    ref_lib().ref_boids_step(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), st["pos"].shape[0],
-                             C.byref(s))
+    t = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+    ref_lib().ref_boids_step_target(C.byref(c), C.byref(bp), float(dt), int(boundary), int(dim), _p(t),
+                                    float(target_radius), int(target_sign), st["pos"].shape[0], C.byref(s))
+
+
+def ref_perlin_noise(seed, x, y, z):
+    """The reference's PerlinNoise; None when its copy was not compiled in."""
+    v = float(ref_lib().ref_perlin_noise(int(seed), float(x), float(y), float(z)))
+    return None if v == -1.0 else v
 
 
 def ref_clouds_step(c, fp, cp, iters, st):

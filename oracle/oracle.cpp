@@ -20,6 +20,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
+#include <random>
 #include <vector>
 
 #ifdef _OPENMP
@@ -871,11 +873,67 @@ void or_fluid_metrics(const rtp_grid_constants* c, const rtp_fluid_params* p, co
 
 int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary,
                   uint32_t n, or_state* s) {
-  return or_boids_step_dim(c, p, dt, boundary, 3, n, s);
+  return or_boids_step_target(c, p, dt, boundary, 3, nullptr, 0.0f, 0, n, s);
 }
 
 int or_boids_step_dim(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary, int dim,
                       uint32_t n, or_state* s) {
+  return or_boids_step_target(c, p, dt, boundary, dim, nullptr, 0.0f, 0, n, s);
+}
+
+// Physics::PerlinNoise (PerlinNoise.cpp:10-85): Perlin's improved noise over the permutation
+// of 0..255 that std::shuffle draws with std::default_random_engine(seed), mapped to [0, 1].
+float or_perlin_noise(int seed, float x, float y, float z) {
+  std::vector<int> perm(256);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::default_random_engine engine(seed);
+  std::shuffle(perm.begin(), perm.end(), engine);
+  perm.insert(perm.end(), perm.begin(), perm.end());
+  auto fade = [](float t) { return t * t * t * (t * (t * 6 - 15) + 10); };
+  auto lerp = [](float t, float a, float b) { return a + t * (b - a); };
+  auto grad = [](int hash, float gx, float gy, float gz) {
+    const int h = hash & 15;
+    const float u = h < 8 ? gx : gy;
+    const float v = h < 4 ? gy : (h == 12 || h == 14) ? gx : gz;
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+  };
+  const int X = (int)std::floor(x) & 255, Y = (int)std::floor(y) & 255, Z = (int)std::floor(z) & 255;
+  x -= std::floor(x);
+  y -= std::floor(y);
+  z -= std::floor(z);
+  const float u = fade(x), v = fade(y), w = fade(z);
+  const int A = perm[X] + Y, AA = perm[A] + Z, AB = perm[A + 1] + Z;
+  const int B = perm[X + 1] + Y, BA = perm[B] + Z, BB = perm[B + 1] + Z;
+  const float z0 = lerp(v, lerp(u, grad(perm[AA], x, y, z), grad(perm[BA], x - 1, y, z)),
+                        lerp(u, grad(perm[AB], x, y - 1, z), grad(perm[BB], x - 1, y - 1, z)));
+  const float z1 = lerp(v, lerp(u, grad(perm[AA + 1], x, y, z - 1), grad(perm[BA + 1], x - 1, y, z - 1)),
+                        lerp(u, grad(perm[AB + 1], x, y - 1, z - 1), grad(perm[BB + 1], x - 1, y - 1, z - 1)));
+  return (lerp(w, z0, z1) + 1.0f) / 2.0f;
+}
+
+// Target::updatePos (Target.cpp:27-50) nsteps times from a new Target (Target.cpp:11-22,
+// box width boxWidth): out[3 * s + k] = coordinate k after step s.
+void or_target_trajectory(float boxWidth, int dim, float particlesVel, uint32_t nsteps, float* out) {
+  const float maxRadius = 0.48f * boxWidth;
+  float px = 0.0f, py = 0.0f, pz = 0.0f;
+  const float PI = 3.14f;
+  for (uint32_t s = 0; s < nsteps; ++s) {
+    px += 0.001f;
+    py += 0.002f;
+    pz += 0.01f;
+    const float nTheta = or_perlin_noise(1, px, py, pz);
+    const float nBeta = or_perlin_noise(29, px, py, pz);
+    const float nR = or_perlin_noise(246, px, py, pz);
+    const float velRatio = particlesVel / 9.5f;
+    const float radius = maxRadius * std::cos(12 * velRatio * PI * nR);
+    out[3 * s + 0] = dim == 3 ? radius * std::cos(5 * velRatio * PI * nBeta) : 0.0f;
+    out[3 * s + 1] = radius * std::sin(5 * velRatio * PI * nBeta) * std::cos(4 * velRatio * PI * nTheta);
+    out[3 * s + 2] = radius * std::sin(5 * velRatio * PI * nBeta) * std::sin(4 * velRatio * PI * nTheta);
+  }
+}
+
+int or_boids_step_target(const rtp_grid_constants* c, const rtp_boids_params* p, float dt, int boundary, int dim,
+                         const float* target, float targetRadius, int targetSign, uint32_t n, or_state* s) {
   if (!c || !p || !s || !s->pos || !s->vel || (dim != 2 && dim != 3)) return RTP_ERR_INVALID_ARGUMENT;
   const Grid g(c);
   float* pos = s->pos;
@@ -923,6 +981,17 @@ int or_boids_step_dim(const rtp_grid_constants* c, const rtp_boids_params* p, fl
       newAcc = avgVel * p->alignmentScale + repulse * p->separationScale + avgPos * p->cohesionScale;
     }
     st4(acc.data(), i, newAcc);
+  }
+  if (target) {
+    // bd_addTargetRule, boids.cl:226-241 (Boids.cpp:351-358): target w = 0.
+    const f4 tp = mk(target[0], target[1], target[2], 0.0f);
+    OR_PARALLEL_FOR
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const f4 vec = tp - ld4(pos, i);
+      const float dist = flen(vec);
+      if (dist < targetRadius)
+        st4(acc.data(), i, ld4(acc.data(), i) + ((float)targetSign * vec) * clampf(1.3f / dist, 0.0f, 1.4f * 0.5f));
+    }
   }
   // bd_updateVel, boids.cl:246-259 (maxVelocity = velocityScale, Boids.cpp:217).
   const float vmax = p->velocityScale;

@@ -66,6 +66,16 @@ int or_boids_step(const rtp_grid_constants* c, const rtp_boids_params* p, float 
 /* The same for a 2D (dim = 2) or 3D model. */
 int or_boids_step_dim(const rtp_grid_constants* c, const rtp_boids_params* p, float dt,
                       int boundary, int dim, uint32_t n, or_state* s);
+/* The same with the target rule (bd_addTargetRule, boids.cl:226-241) for a target at
+ * target[0..2] this step, or without it when target is NULL. */
+int or_boids_step_target(const rtp_grid_constants* c, const rtp_boids_params* p, float dt,
+                         int boundary, int dim, const float* target, float targetRadius,
+                         int targetSign, uint32_t n, or_state* s);
+/* Physics::PerlinNoise(seed).computeNoiseValue(x, y, z) (PerlinNoise.cpp:10-85). */
+float or_perlin_noise(int seed, float x, float y, float z);
+/* Target::updatePos (Target.cpp:27-50) nsteps times from a new Target of box width
+ * boxWidth: out[3 * step + k]. */
+void or_target_trajectory(float boxWidth, int dim, float particlesVel, uint32_t nsteps, float* out);
 /* One Clouds::update (Clouds.cpp:503-610). `ground` may be NULL (constant groundTemp0). */
 int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp,
                    const rtp_cloud_params* cp, const rtp_cloud_env* env, const float* ground,

@@ -1,6 +1,7 @@
 #!/usr/bin/env python3
 """Builds oracle/_ref/libref.so: the reference's own step kernels (physics/ocl/kernels/*.cl
-of axoloto/RealTimeParticles) compiled for the CPU, to check the oracle against them.
+of axoloto/RealTimeParticles) and its Perlin noise (physics/utils/PerlinNoise.cpp) compiled
+for the CPU, to check the oracle against them.
 
 TEST INFRASTRUCTURE ONLY.  When the reference checkout is present (REFERENCE_DIR, default
 /root/reference), each OpenCL program is assembled from its .cl files in the order the
@@ -68,6 +69,14 @@ def generate():
                 "namespace ref_%s {\nusing namespace clshim;\n%s\n%s\n%s\n}  // namespace ref_%s\n"
                 % (", ".join(files), prog, defs, "".join(body), undefs, prog))
         open(os.path.join(OUT, "ref_%s.cpp" % prog), "w").write(text)
+    # Physics::PerlinNoise (the boids target's noise) and the math header it includes, as
+    # they are: they compile alone.  Target.cpp needs spdlog and nlohmann/json (absent).
+    pdir = os.path.join(OUT, "perlin")
+    os.makedirs(pdir, exist_ok=True)
+    for src in (os.path.join(REF, "physics", "utils", "PerlinNoise.cpp"),
+                os.path.join(REF, "physics", "utils", "PerlinNoise.hpp"),
+                os.path.join(REF, "utils", "Math.hpp")):
+        open(os.path.join(pdir, os.path.basename(src)), "w").write(open(src).read())
 
 
 def compile_lib():

@@ -26,6 +26,13 @@ thread_local uint g_global_size = 0;
 #include "ref_clouds.cpp"
 #include "ref_fluids.cpp"
 
+// Physics::PerlinNoise (physics/utils/PerlinNoise.cpp, copied by build_ref.py with the
+// utils/Math.hpp it includes); Target.cpp itself needs spdlog and nlohmann/json, absent here.
+#if __has_include("perlin/PerlinNoise.cpp")
+#include "perlin/PerlinNoise.cpp"
+#define REF_HAS_PERLIN 1
+#endif
+
 namespace {
 
 using clshim::float4;
@@ -172,9 +179,10 @@ int ref_fluids_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, uin
   return RTP_OK;
 }
 
-// Boids::update (Boids.cpp:335-373), target rule off, dt a parameter.
-int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, float dt, int boundary, int dim, uint32_t n,
-                   or_state* s) {
+// Boids::update (Boids.cpp:335-373), dt a parameter; the target rule (:351-358) runs when
+// target is not NULL, with the target's position of this step.
+int ref_boids_step_target(const rtp_grid_constants* c, const rtp_boids_params* bp, float dt, int boundary, int dim,
+                          const float* target, float targetRadius, int targetSign, uint32_t n, or_state* s) {
   ref_consts = *c;
   const ref_boids::BoidsRuleParams P = as<ref_boids::BoidsRuleParams>(*bp);
   float4 *pos = F4(s->pos), *vel = F4(s->vel);
@@ -194,6 +202,13 @@ int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, floa
     run(n, [&] { ref_boids::bd_applyBoidsRulesWithGrid2D(pos, vel, T, P, A); });
   else
     run(n, [&] { ref_boids::bd_applyBoidsRulesWithGrid3D(pos, vel, T, P, A); });
+  if (target) {
+    const float4 tp = clshim::make_float4(target[0], target[1], target[2], 0.0f);
+    ref_boids::TargetParams TP;
+    TP.targetRadiusEffect = targetRadius;
+    TP.targetSignEffect = targetSign;
+    run(n, [&] { ref_boids::bd_addTargetRule(pos, tp, TP, A); });
+  }
   const float vmax = bp->velocityScale;
   run(n, [&] { ref_boids::bd_updateVel(A, dt, vmax, vel); });
   if (boundary == RTP_BOUNDARY_CYCLIC_WALL)
@@ -315,6 +330,22 @@ void ref_fill_grid_detector(const rtp_grid_constants* c, const float* pos, uint3
   clshim::float8* d = reinterpret_cast<clshim::float8*>(det);
   run(c->numCells, [&] { ref_fluids::resetGridDetector(d); });
   run(n, [&] { ref_fluids::fillGridDetector(F4(const_cast<float*>(pos)), d); });
+}
+
+int ref_boids_step(const rtp_grid_constants* c, const rtp_boids_params* bp, float dt, int boundary, int dim, uint32_t n,
+                   or_state* s) {
+  return ref_boids_step_target(c, bp, dt, boundary, dim, nullptr, 0.0f, 0, n, s);
+}
+
+// PerlinNoise(seed).computeNoiseValue({x, y, z}); -1 when the copy of PerlinNoise.cpp is absent.
+float ref_perlin_noise(int seed, float x, float y, float z) {
+#ifdef REF_HAS_PERLIN
+  Physics::PerlinNoise noise(seed);
+  return noise.computeNoiseValue(Math::float3(x, y, z));
+#else
+  (void)seed, (void)x, (void)y, (void)z;
+  return -1.0f;
+#endif
 }
 
 }  // extern "C"

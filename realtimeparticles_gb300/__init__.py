@@ -27,7 +27,8 @@ def __getattr__(name):
     # Lazy: importing the package must not load the CUDA library (CPU-only tools and the
     # oracle import abi/scenes).
     if name in ("Model", "Fluids", "Boids", "Clouds", "CreateModel", "RtpError", "get_constants",
-                "default_fluid_params", "default_boids_params", "default_cloud_params", "reference_cloud_env"):
+                "default_fluid_params", "default_boids_params", "default_cloud_params", "default_target_params",
+                "reference_cloud_env"):
         from . import model
         return getattr(model, name)
     raise AttributeError(name)

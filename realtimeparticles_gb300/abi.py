@@ -98,6 +98,16 @@ class BoidsParams(C.Structure):
     ]
 
 
+class TargetParams(C.Structure):
+    """rtp_target_params: the JSON "Target" group (Boids.cpp:45-51) + TargetKernelInputs."""
+    _fields_ = [
+        ("enabled", C.c_int32),
+        ("visible", C.c_int32),
+        ("radiusEffect", C.c_float),
+        ("signEffect", C.c_int32),
+    ]
+
+
 class CloudParams(C.Structure):
     _fields_ = [
         ("dim", C.c_uint32),

@@ -4,7 +4,8 @@
 //   k_boids_keys          fillCellIDs(pos) + sort-tile histogram
 //   sort passes           RadixSort::sort of {pos, vel} (+ ids); acc is recomputed each step
 //   cell table            start/end (cap 3000, Boids.cpp:78)
-//   k_boids_rules_update  bd_applyBoidsRulesWithGrid3D (2D models: ...Grid2D) + bd_updateVel + the boundary
+//   k_boids_rules_update  bd_applyBoidsRulesWithGrid3D (2D models: ...Grid2D) + bd_addTargetRule when the
+//                         target is on + bd_updateVel + the boundary
 //                         condition (bd_updatePosAndApplyPeriodicBC / ...WallBC), reading
 //                         the sorted copies and writing the canonical pos/vel buffers.
 #include "boids.cuh"
@@ -13,10 +14,15 @@ namespace rtp {
 
 __global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, const float4* __restrict__ pos, uint32_t n,
                                                              uint32_t* __restrict__ keys, int bits0,
-                                                             uint32_t* __restrict__ hist0, ZeroJob zero) {
+                                                             uint32_t* __restrict__ hist0, ZeroJob zero,
+                                                             float4* __restrict__ track) {
   pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
   zero_job(zero);
+  if (track && blockIdx.x == 0 && threadIdx.x == 0) {
+    uint32_t* step = reinterpret_cast<uint32_t*>(track);
+    *step = *step + 1u;  // this step's slot of the target track
+  }
   TileHistogram th;
   th.init(s_hist, bits0);
   const uint32_t base = blockIdx.x * kSortTile;
@@ -44,7 +50,7 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
                                                             float4* __restrict__ vel, float4* __restrict__ acc,
-                                                            uint32_t* __restrict__ ids) {
+                                                            uint32_t* __restrict__ ids, TargetK tk) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -110,6 +116,14 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
     const float4 sep = fnorm(sr) * p.velocityScale;
     a = ali * p.alignmentScale + sep * p.separationScale + coh * p.cohesionScale;
   }
+  if (tk.track) {
+    // bd_addTargetRule (boids.cl:226-241): inside the radius, adds sign x vec x
+    // clamp(1.3 / |vec|, 0, 1.4 x MAX_STEERING) with vec = target - x (lengths over four lanes).
+    const uint32_t s = min(*reinterpret_cast<const uint32_t*>(tk.track), tk.cap - 1u);
+    const float4 vec = ld4(tk.track + 1 + s) - xi;
+    const float dist = sqrtf(dot4(vec, vec));
+    if (dist < tk.radius) a = a + (vec * tk.sign) * fminf(fmaxf(1.3f / dist, 0.0f), 0.7f);
+  }
   acc[i] = a;
   // bd_updateVel (boids.cl:246-259).
   const float4 nv = ld4(velS + i) + a * p.dt;
@@ -138,27 +152,27 @@ static int check(const char* what) {
 }
 
 int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
-                  Launcher& L, const ZeroJob& zero) {
+                  Launcher& L, const ZeroJob& zero, const TargetK& tk) {
   L.begin("bd_keys");
-  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, n, keys, plan.bits[0], hist0, zero);
+  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, n, keys, plan.bits[0], hist0, zero, tk.track);
   L.end("bd_keys");
   return check("k_boids_keys");
 }
 
 int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, bool dim2, const float4* posS,
                        const float4* velS, const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos,
-                       float4* vel, float4* acc, uint32_t* ids, Launcher& L) {
+                       float4* vel, float4* acc, uint32_t* ids, Launcher& L, const TargetK& tk) {
   const uint32_t b = (n + 127) / 128;
   L.begin("bd_rules_update");
   if (periodic && dim2)
-    launch(L, k_boids_rules_update<true, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<true, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
   else if (periodic)
-    launch(L, k_boids_rules_update<true, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<true, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
   else if (dim2)
-    launch(L, k_boids_rules_update<false, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids);
+    launch(L, k_boids_rules_update<false, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
   else
     launch(L, k_boids_rules_update<false, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc,
-           ids);
+           ids, tk);
   L.end("bd_rules_update");
   return check("k_boids_rules_update");
 }

@@ -22,6 +22,7 @@
 #include "fluids.cuh"
 #include "rtp_internal.hpp"
 #include "side.cuh"
+#include "target.hpp"
 #include "warmstart.cuh"
 
 namespace rtp {
@@ -211,7 +212,20 @@ struct Handle {
   SortScratch camSS{};
   uint32_t tableCells = 0;  // cells the table was allocated for
   uint32_t sortKeyBits = 0; // key bits the sort scratch was allocated for
+  // Boids target attractor: parameters, the host trajectory, and the device track of the
+  // target positions of up to kTargetChunk steps (slot 0: step counter), filled from
+  // pinned staging ahead of the graph launches that read it.
+  rtp_target_params tp{};
+  bool targetVisible = false;
+  TargetTrajectory traj{0.0f};
+  float4* targetTrack = nullptr;
+  float4* targetHost = nullptr;
+  cudaEvent_t targetUp = nullptr;  // the last upload has read targetHost
+  bool targetUpPending = false;
 };
+
+constexpr uint32_t kTargetChunk = 1024;
+static bool target_on(const Handle* h) { return h->model == RTP_MODEL_BOIDS && h->tp.enabled; }
 
 // The fluids parameters a step's kernels get: shared values, tuning and the batch tables.
 static FluidK fluidk_of(const Handle* h) {
@@ -331,6 +345,8 @@ static void free_handle(Handle* h) {
   if (h->t1) cudaEventDestroy(h->t1);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
+  if (h->targetHost) cudaFreeHost(h->targetHost);
+  if (h->targetUp) cudaEventDestroy(h->targetUp);
   delete h;
 }
 
@@ -549,7 +565,14 @@ static int record_boids_step(Handle* h, Launcher& L) {
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
   // Boids.cpp:335-344.
-  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L, zero));
+  TargetK tk;
+  if (target_on(h)) {
+    tk.track = h->targetTrack;
+    tk.cap = kTargetChunk;
+    tk.radius = h->tp.radiusEffect;
+    tk.sign = (float)h->tp.signEffect;
+  }
+  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L, zero, tk));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -561,7 +584,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
   gl.n1 = 1;
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
   RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L, nullptr, true));
-  // Boids.cpp:346-373.
+  // Boids.cpp:346-373 (the target rule, :351-358, inside the rules kernel).
   BoidsK bk;
   bk.velocityScale = h->bp.velocityScale;
   bk.alignmentScale = h->bp.alignmentScale;
@@ -572,7 +595,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
   // Boids.cpp:346-349: the 2D rules kernel for a 2D model.
   return boids_rules_update(g, bk, h->boundary == RTP_BOUNDARY_CYCLIC_WALL, h->mp.dimension == 2, h->posS, h->velS,
                             h->table, n, h->idsS,
-                            h->pos, h->vel, h->acc, h->ids, L);
+                            h->pos, h->vel, h->acc, h->ids, L, tk);
 }
 
 static CloudK make_cloudk(const Handle* h) {
@@ -1005,10 +1028,41 @@ static int collect_profile(Handle* h) {
   return RTP_OK;
 }
 
+// Target::updatePos for the next k <= kTargetChunk steps (Boids.cpp:351-356), uploaded with
+// the step counter reset ahead of the graph launches that read them.
+static int feed_target(Handle* h, uint32_t k) {
+  if (h->targetUpPending) RTP_CUDA(cudaEventSynchronize(h->targetUp));
+  h->targetUpPending = false;
+  const uint32_t before = 0xffffffffu;
+  std::memcpy(&h->targetHost[0], &before, sizeof before);
+  for (uint32_t s = 0; s < k; ++s) {
+    h->traj.advance(h->mp.dimension != 2, h->bp.velocityScale);
+    const float* p = h->traj.pos();
+    h->targetHost[1 + s] = make_float4(p[0], p[1], p[2], 0.0f);
+  }
+  RTP_CUDA(cudaMemcpyAsync(h->targetTrack, h->targetHost, sizeof(float4) * (1 + (size_t)k), cudaMemcpyHostToDevice,
+                           h->stream));
+  RTP_CUDA(cudaEventRecord(h->targetUp, h->stream));
+  h->targetUpPending = true;
+  return RTP_OK;
+}
+
+static inline uint32_t target_feed_size(const Handle* h, uint32_t s, uint32_t nsteps) {
+  if (!target_on(h) || s % kTargetChunk != 0) return 0;
+  return std::min(kTargetChunk, nsteps - s);
+}
+
 static int run_steps(Handle* h, uint32_t nsteps) {
-  if (h->paused || nsteps == 0 || h->curN == 0) return RTP_OK;
+  if (h->paused || nsteps == 0) return RTP_OK;
+  if (h->curN == 0) {
+    // No particles: the step launches nothing, the target still moves (Boids.cpp:351-353).
+    if (target_on(h))
+      for (uint32_t s = 0; s < nsteps; ++s) h->traj.advance(h->mp.dimension != 2, h->bp.velocityScale);
+    return RTP_OK;
+  }
   if (!h->graphValid || h->graphProfiled != h->profiling) RTP_TRY(build_graph(h));
   for (uint32_t s = 0; s < nsteps; ++s) {
+    if (const uint32_t k = target_feed_size(h, s, nsteps)) RTP_TRY(feed_target(h, k));
     RTP_CUDA(cudaGraphLaunch(h->graph, h->stream));
     if (h->graphProfiled) RTP_TRY(collect_profile(h));
   }
@@ -1135,6 +1189,8 @@ int rtp_create(int model, const rtp_model_params* params, void** out_handle) {
   rtp_boids_params_default(&h->bp);
   rtp_cloud_params_default(&h->cp);
   rtp_cloud_env_reference(&h->env);
+  rtp_target_params_default(&h->tp);
+  h->traj = TargetTrajectory(params->boxSize[0]);  // Boids.cpp:80
   h->iters = (model == RTP_MODEL_CLOUDS) ? 1u : 2u;  // Clouds.cpp:111, Fluids.cpp:81
   cudaGetDevice(&h->device);
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -1187,6 +1243,9 @@ int rtp_reset(void* handle) {
   h->fp.dim = h->cp.dim = h->mp.dimension == 2 ? 2u : 3u;
   h->iters = (h->model == RTP_MODEL_CLOUDS) ? 1u : 2u;
   h->boidsDt = 0.1f;
+  // The JSON defaults switch the target off (Boids.cpp:233); its trajectory keeps going.
+  rtp_target_params_default(&h->tp);
+  h->targetVisible = false;
   invalidate(h);
   return init_case(h);
   RTP_GUARD_END
@@ -1239,6 +1298,47 @@ int rtp_set_boids_time_step(void* handle, float dt) {
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
   H(handle)->boidsDt = dt;
   invalidate(H(handle));
+  return RTP_OK;
+}
+
+// Target group defaults, Boids.cpp:45-51.
+int rtp_target_params_default(rtp_target_params* p) {
+  if (!p) return fail(RTP_ERR_INVALID_ARGUMENT, "null");
+  p->enabled = 0;
+  p->visible = 1;
+  p->radiusEffect = 2.0f;
+  p->signEffect = 1;
+  return RTP_OK;
+}
+
+// Boids::transferJsonInputsToModel, target part (Boids.cpp:193-202).
+int rtp_set_target(void* handle, const rtp_target_params* p) {
+  RTP_GUARD_BEGIN
+  if (!handle || !p) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_target: null argument");
+  Handle* h = H(handle);
+  if (h->model != RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_target: boids only");
+  if (std::isnan(p->radiusEffect)) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_target: radiusEffect is NaN");
+  if (p->enabled && !h->targetTrack) {
+    RTP_TRY(dalloc(h, &h->targetTrack, 1 + (size_t)kTargetChunk));
+    RTP_CUDA(cudaMallocHost((void**)&h->targetHost, sizeof(float4) * (1 + (size_t)kTargetChunk)));
+    RTP_CUDA(cudaEventCreateWithFlags(&h->targetUp, cudaEventDisableTiming));
+  }
+  h->tp = *p;
+  h->tp.enabled = p->enabled ? 1 : 0;
+  h->targetVisible = h->tp.enabled && p->visible;  // Target::show after activate (Target.hpp:25)
+  invalidate(h);
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
+int rtp_get_target(void* handle, float pos[3], int* activated, int* visible) {
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_get_target: null handle");
+  const Handle* h = H(handle);
+  const bool boids = h->model == RTP_MODEL_BOIDS;
+  if (pos)
+    for (int k = 0; k < 3; ++k) pos[k] = boids ? h->traj.pos()[k] : 0.0f;
+  if (activated) *activated = boids && h->tp.enabled;
+  if (visible) *visible = boids && h->targetVisible;
   return RTP_OK;
 }
 
@@ -1454,6 +1554,7 @@ int rtp_time_steps(void* handle, uint32_t nsteps, uint64_t flush_bytes, double* 
   }
   if (!h->graphValid || h->graphProfiled != h->profiling) RTP_TRY(build_graph(h));
   for (uint32_t s = 0; s < nsteps; ++s) {
+    if (const uint32_t k = target_feed_size(h, s, nsteps)) RTP_TRY(feed_target(h, k));
     if (flush_bytes) RTP_CUDA(cudaMemsetAsync(h->flush, (int)(s & 0xff), flush_bytes, h->stream));
     RTP_CUDA(cudaEventRecord(h->t0, h->stream));
     RTP_CUDA(cudaGraphLaunch(h->graph, h->stream));

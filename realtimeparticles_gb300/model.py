@@ -170,6 +170,22 @@ class Model:
     def isInit(self):
         return bool(self._h)
 
+    # target (Model.hpp:130-132): the boids' attractor; other models report none --------
+    def _target(self):
+        pos = (C.c_float * 3)()
+        act, vis = C.c_int(), C.c_int()
+        call("rtp_get_target", self._h, pos, C.byref(act), C.byref(vis))
+        return (float(pos[0]), float(pos[1]), float(pos[2])), bool(act.value), bool(vis.value)
+
+    def targetPos(self):
+        return self._target()[0]
+
+    def isTargetActivated(self):
+        return self._target()[1]
+
+    def isTargetVisible(self):
+        return self._target()[2]
+
     # profiling (OclModel.hpp:28-38) -------------------------------------------------
     def isProfilingEnabled(self):
         v = C.c_int()
@@ -427,7 +443,10 @@ class Boids(Model):
     def setTimeStep(self, dt):
         call("rtp_set_boids_time_step", self._h, float(dt))
 
-    # Boids::transferJsonInputsToModel (Boids.cpp:177-210); the target rule is not built.
+    def setTarget(self, tp):
+        call("rtp_set_target", self._h, C.byref(tp))
+
+    # Boids::transferJsonInputsToModel (Boids.cpp:177-210).
     def transferJsonInputsToModel(self, js):
         b = js["Boids"]
         bp = abi.BoidsParams()
@@ -435,8 +454,14 @@ class Boids(Model):
         bp.alignmentScale = float(b["Alignment"]["Scale##Alignment"][0]) if b["Alignment"]["Enable##Alignment"] else 0.0
         bp.separationScale = float(b["Separation"]["Scale##Separation"][0]) if b["Separation"]["Enable##Separation"] else 0.0
         bp.cohesionScale = float(b["Cohesion"]["Scale##Cohesion"][0]) if b["Cohesion"]["Enable##Cohesion"] else 0.0
-        _ = b["Target"]["Enable##Target"]
+        t = b["Target"]
+        tp = abi.TargetParams()
+        tp.enabled = 1 if t["Enable##Target"] else 0
+        tp.visible = 1 if t["Show"] else 0
+        tp.radiusEffect = float(t["Radius"][0])
+        tp.signEffect = int(bool(t["Attract"]))  # (int)"Attract": 1 or 0
         self.setBoidsParams(bp)
+        self.setTarget(tp)
 
 
 class Clouds(Model):
@@ -579,6 +604,12 @@ def default_fluid_params():
 def default_boids_params():
     p = abi.BoidsParams()
     call("rtp_boids_params_default", C.byref(p))
+    return p
+
+
+def default_target_params():
+    p = abi.TargetParams()
+    call("rtp_target_params_default", C.byref(p))
     return p
 
 

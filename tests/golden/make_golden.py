@@ -70,6 +70,25 @@ def main():
         oracle.ref_boids_step(cb, sb["boids_params"], 0.01, abi.CYCLIC_WALL, st)
     save("boids_3steps.npz", consts=sbytes(cb), params=sbytes(sb["boids_params"]), dt=np.array([0.01], np.float32),
          pos0=pos0, vel0=vel0, **{k: st[k] for k in ("pos", "vel", "acc", "id", "cellId", "table")})
+    # Boids target attractor: the reference's PerlinNoise at seeded points, then 3 boids steps
+    # with bd_addTargetRule.  Target.cpp needs spdlog/nlohmann-json, so the positions come from
+    # the oracle's Target::updatePos restatement and are stored as inputs.
+    pts = np.random.default_rng(13).uniform(-50, 50, (256, 3)).astype(np.float32)
+    seeds = np.array([1, 29, 246], np.int32)
+    noise = np.array([[oracle.ref_perlin_noise(int(sd), *p) for p in pts] for sd in seeds], np.float32)
+    sb = scenes.boids_cloud(n=3000, seed=12)
+    cb = oracle.derive_constants(abi.BOIDS, sb["model_params"])
+    st = oracle.new_state(3000, cb, abi.BOIDS)
+    st["pos"][:] = sb["pos"]
+    st["vel"][:] = sb["vel"]
+    pos0, vel0 = st["pos"].copy(), st["vel"].copy()
+    traj = oracle.target_trajectory(sb["model_params"].boxSize[0], 3, sb["boids_params"].velocityScale, 3)
+    for s in range(3):
+        oracle.ref_boids_step(cb, sb["boids_params"], 0.01, abi.CYCLIC_WALL, st, target=traj[s], target_radius=1.2,
+                              target_sign=1)
+    save("boids_target_3steps.npz", points=pts, seeds=seeds, noise=noise, consts=sbytes(cb),
+         params=sbytes(sb["boids_params"]), dt=np.array([0.01], np.float32), radius=np.array([1.2], np.float32),
+         target=traj, pos0=pos0, vel0=vel0, **{k: st[k] for k in ("pos", "vel", "acc", "id")})
     # Clouds: 3000 particles, the reference environment, 1 iteration, 3 steps.
     scc = scenes.clouds_cumulus(n=3000, noise=False, seed=7)
     cc = oracle.derive_constants(abi.CLOUDS, scc["model_params"])

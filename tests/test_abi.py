@@ -24,6 +24,7 @@ def test_struct_layouts_match_reference_structs():
     assert C.sizeof(abi.FluidParams) == 44   # FluidKernelInputs, 11 x 4 bytes
     assert C.sizeof(abi.CloudParams) == 52   # CloudKernelInputs, 13 x 4 bytes
     assert C.sizeof(abi.BoidsParams) == 16   # BoidsRuleKernelInputs
+    assert C.sizeof(abi.TargetParams) == 16  # JSON Target group; TargetKernelInputs is its last 8 bytes
 
 
 def test_ctypes_layouts_match_the_c_header(tmp_path):
@@ -34,7 +35,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
                "rtp_kernel_time": abi.KernelTime, "rtp_metrics": abi.Metrics, "rtp_mlp": abi.Mlp,
                "rtp_warm_start_config": abi.WarmStartConfig, "rtp_solver_stats": abi.SolverStats,
                "rtp_train_config": abi.TrainConfig, "rtp_batch_scene": abi.BatchScene, "rtp_tuning": abi.Tuning,
-               "rtp_tune_result": abi.TuneResult}
+               "rtp_tune_result": abi.TuneResult, "rtp_target_params": abi.TargetParams}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s/include/rtp.h"' % ROOT, "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))

@@ -70,6 +70,25 @@ def test_boids_golden(oracle_mod):
         _assert_same(st[k], g[k], k)
 
 
+def test_boids_target_golden(oracle_mod):
+    """The reference's PerlinNoise values and 3 boids steps with its bd_addTargetRule."""
+    g = _load("boids_target_3steps.npz")
+    for k, seed in enumerate(g["seeds"]):
+        got = np.array([oracle_mod.perlin_noise(int(seed), *p) for p in g["points"]], np.float32)
+        _assert_same(got, g["noise"][k], "noise seed %d" % seed)
+    c = _struct(abi.GridConstants, g["consts"])
+    bp = _struct(abi.BoidsParams, g["params"])
+    st = oracle_mod.new_state(g["pos0"].shape[0], c, abi.BOIDS)
+    st["pos"][:] = g["pos0"]
+    st["vel"][:] = g["vel0"]
+    assert np.array_equal(g["target"], oracle_mod.target_trajectory(c.absWall[0] * 2, 3, bp.velocityScale, 3))
+    for s in range(3):
+        oracle_mod.boids_step(c, bp, float(g["dt"][0]), abi.CYCLIC_WALL, st, target=g["target"][s],
+                              target_radius=float(g["radius"][0]))
+    for k in ("pos", "vel", "acc", "id"):
+        _assert_same(st[k], g[k], k)
+
+
 def test_clouds_golden(oracle_mod):
     from realtimeparticles_gb300 import scenes
     g = _load("clouds_3steps.npz")
