@@ -105,24 +105,34 @@ __device__ __forceinline__ void visit_list_x4(uint32_t begin, uint32_t end, uint
   }
 }
 
+// c + d for d in {-1, 0, 1} wrapped into [0, R): the same cell as (c + d + R) % R for the
+// c in [0, R] that cell3 can return (c = R is the aliased +W wall).
+__device__ __forceinline__ int wrap_cell(int c, int d, int R) {
+  int v = c + d;
+  if (v < 0) v += R;
+  else if (v >= R) v -= R;
+  return v;
+}
+
 // The 27 cells of the fluids neighbourhood (fluids.cl:101-123), wrapped modulo the
 // resolution, as 9 (x, y) rows of three z cells each, visited x-major then y then z.
 template <class R>
 __device__ __forceinline__ void for_each_fluid_row(const GridK& g, const uint2* __restrict__ table, float4 xi, R&& row_fn) {
   int cx, cy, cz;
   cell3(g, xi, cx, cy, cz);
-  const int z0 = (cz - 1 + g.R[2]) % g.R[2], z1 = cz % g.R[2], z2 = (cz + 1) % g.R[2];
+  const uint32_t z0 = (uint32_t)wrap_cell(cz, -1, g.R[2]), z1 = (uint32_t)wrap_cell(cz, 0, g.R[2]),
+                 z2 = (uint32_t)wrap_cell(cz, 1, g.R[2]);
 #pragma unroll 1
-  for (int a = 0; a < 3; ++a) {
-    const int x = (cx + a - 1 + g.R[0]) % g.R[0];
+  for (int a = -1; a <= 1; ++a) {
+    const int x = wrap_cell(cx, a, g.R[0]);
 #pragma unroll 1
-    for (int b = 0; b < 3; ++b) {
-      const int y = (cy + b - 1 + g.R[1]) % g.R[1];
+    for (int b = -1; b <= 1; ++b) {
+      const int y = wrap_cell(cy, b, g.R[1]);
       const uint32_t row = g.base + ((uint32_t)x * g.R[1] + (uint32_t)y) * g.R[2];
       uint32_t b0, e0, b1, e1, b2, e2;
-      cell_range(table, row + (uint32_t)z0, g.cap, b0, e0);
-      cell_range(table, row + (uint32_t)z1, g.cap, b1, e1);
-      cell_range(table, row + (uint32_t)z2, g.cap, b2, e2);
+      cell_range(table, row + z0, g.cap, b0, e0);
+      cell_range(table, row + z1, g.cap, b1, e1);
+      cell_range(table, row + z2, g.cap, b2, e2);
       row_fn(b0, e0, b1, e1, b2, e2);
     }
   }
