@@ -12,8 +12,9 @@ Metric: particle-steps/s.
   factor) is picked by the library's autotuner before warm-up; candidates and times reported.
 * value: K device-timed steps (CUDA events around each graph replay on the model's
   stream), inputs resident in HBM, L2 flushed before every step by a 256 MiB write.
-* e2e: K steps through the public API with host buffers: upload pos/vel from pinned
-  host memory, update(1), download pos/vel, timed on the host clock.
+* e2e: K steps through the public API with host buffers: one rtp_update_host call per step
+  (upload pos/vel from pinned host memory, one update, download pos/vel, one
+  synchronisation), timed on the host clock.
 * roofline: the dominant kernel's algorithmic bytes / its mean CUDA-event duration
   (captured event nodes inside the same graph replays), against MEASURED_PEAKS.json.
 * cpu_baseline: the reference's own kernels (physics/ocl/kernels/*.cl compiled for the
@@ -518,12 +519,12 @@ def run_ours(args):
     hvel[:] = m.download(abi.BUF_VEL)
     barrier(ws)
     t0 = time.perf_counter()
+    hp, hv = hpos.ctypes.data_as(C.c_void_p), hvel.ctypes.data_as(C.c_void_p)
     for _ in range(args.steps):
-        m.upload(abi.BUF_POS, hpos)
-        m.upload(abi.BUF_VEL, hvel)
-        m.update(1)
-        lib().rtp_download(m.handle, abi.BUF_POS, hpos.ctypes.data_as(C.c_void_p), n)
-        lib().rtp_download(m.handle, abi.BUF_VEL, hvel.ctypes.data_as(C.c_void_p), n)
+        # rtp_update_host: upload pos + vel, one step, download pos + vel, one synchronisation.
+        rc = lib().rtp_update_host(m.handle, hp, hv, n, 1, hp, hv)
+        if rc != 0:
+            raise RuntimeError("rtp_update_host failed: %d" % rc)
     t_e2e = time.perf_counter() - t0
     barrier(ws)
     t_e2e = max_over_ranks(t_e2e, ws)

@@ -280,6 +280,15 @@ int rtp_download(void* handle, int buffer, void* host, uint64_t count);
 int rtp_device_ptr(void* handle, int buffer, void** dptr);
 int rtp_stream(void* handle, void** stream);
 int rtp_synchronize(void* handle);
+/* A step over host-resident state in one call (new: the reference keeps its state in GL
+ * buffers): copies `count` float4 positions and velocities from host memory into the model,
+ * runs nsteps updates (rtp_update) and copies them back, all ordered on the handle's stream
+ * with a single synchronisation at the end; it returns once posOut / velOut hold the result.
+ * count must equal the current particle count.  A NULL input skips that upload, a NULL output
+ * that download; in and out may be the same buffer.  Pinned host memory (cudaHostAlloc,
+ * cudaHostRegister) moves at link speed. */
+int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t count, uint32_t nsteps, void* posOut,
+                    void* velOut);
 
 /* Profiling (OclModel::isProfilingEnabled/enableProfiling, OclModel.hpp:28-38). */
 int rtp_enable_profiling(void* handle, int enable);

@@ -45,6 +45,7 @@ _SIGS = {
     "rtp_set_jacobi_iterations": [P, U32],
     "rtp_set_boids_params": [P, C.POINTER(abi.BoidsParams)],
     "rtp_set_boids_time_step": [P, C.c_float],
+    "rtp_update_host": [P, P, P, C.c_uint64, U32, P, P],
     "rtp_target_params_default": [C.POINTER(abi.TargetParams)],
     "rtp_set_target": [P, C.POINTER(abi.TargetParams)],
     "rtp_get_target": [P, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int)],

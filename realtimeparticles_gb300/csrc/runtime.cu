@@ -1496,6 +1496,26 @@ int rtp_stream(void* handle, void** stream) {
   return RTP_OK;
 }
 
+int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t count, uint32_t nsteps, void* posOut,
+                    void* velOut) {
+  RTP_GUARD_BEGIN
+  if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_update_host: null handle");
+  Handle* h = H(handle);
+  if (count != h->curN) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_update_host: count must equal the particle count");
+  const size_t bytes = sizeof(float4) * (size_t)count;
+  if (posIn && bytes) {
+    RTP_CUDA(cudaMemcpyAsync(h->pos, posIn, bytes, cudaMemcpyHostToDevice, h->stream));
+    RTP_TRY(ws_forget(h));
+  }
+  if (velIn && bytes) RTP_CUDA(cudaMemcpyAsync(h->vel, velIn, bytes, cudaMemcpyHostToDevice, h->stream));
+  RTP_TRY(run_steps(h, nsteps));
+  if (posOut && bytes) RTP_CUDA(cudaMemcpyAsync(posOut, h->pos, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (velOut && bytes) RTP_CUDA(cudaMemcpyAsync(velOut, h->vel, bytes, cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return RTP_OK;
+  RTP_GUARD_END
+}
+
 int rtp_synchronize(void* handle) {
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
   RTP_CUDA(cudaStreamSynchronize(H(handle)->stream));

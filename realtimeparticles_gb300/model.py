@@ -119,6 +119,15 @@ class Model:
         """Model::update(), called nsteps times (graph replays on the handle's stream)."""
         call("rtp_update", self._h, int(nsteps))
 
+    def updateHost(self, pos, vel, nsteps=1):
+        """rtp_update_host: uploads pos / vel ((n, 4) float32, C-contiguous; n = the particle
+        count), runs nsteps updates and writes the result back into the same arrays."""
+        for a in (pos, vel):
+            if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or a.shape != (self.nbParticles(), 4):
+                raise ValueError("updateHost: (n, 4) C-contiguous float32 arrays of the particle count")
+        pp, vp = pos.ctypes.data_as(C.c_void_p), vel.ctypes.data_as(C.c_void_p)
+        call("rtp_update_host", self._h, pp, vp, pos.shape[0], int(nsteps), pp, vp)
+
     def reset(self):
         """Model::reset(): default parameters and the case's initial particles."""
         self._input_json = copy.deepcopy(self._DEFAULT_JSON)

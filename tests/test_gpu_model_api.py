@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from realtimeparticles_gb300 import RtpError, abi, model, scenes
+from realtimeparticles_gb300._lib import call
 
 pytestmark = pytest.mark.gpu
 
@@ -93,3 +94,29 @@ def test_pause_profiling_and_device_pointers():
         assert ms > 0
         with pytest.raises(RtpError):
             m.download(abi.BUF_ACC)
+
+
+def test_update_host_equals_upload_update_download():
+    """rtp_update_host = rtp_upload(pos, vel) + rtp_update + rtp_download(pos, vel), bit for bit."""
+    sc = scenes.dam_break(lattice=(8, 16, 16))
+    n = sc["pos"].shape[0]
+    outs = []
+    for fused in (False, True):
+        with model.Fluids(sc["model_params"]) as m:
+            m.setFluidParams(sc["fluid_params"])
+            m.setJacobiIterations(3)
+            pos, vel = sc["pos"].copy(), sc["vel"].copy()
+            for _ in range(3):
+                if fused:
+                    m.updateHost(pos, vel, nsteps=2)
+                else:
+                    m.upload(abi.BUF_POS, pos)
+                    m.upload(abi.BUF_VEL, vel)
+                    m.update(2)
+                    pos, vel = m.download(abi.BUF_POS), m.download(abi.BUF_VEL)
+            outs.append((pos, vel, m.download(abi.BUF_ID)))
+            with pytest.raises(RtpError):  # count must be the particle count
+                call("rtp_update_host", m.handle, None, None, n - 1, 1, None, None)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+
