@@ -274,12 +274,13 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const bool valid = e < n;
     key[k] = valid ? __ldg(keys_in + e) : 0u;
     dig[k] = valid ? ((key[k] >> shift) & mask) : 0xFFFFFFFFu;
+    // The lowest lane of each digit's peer group adds the group to the warp's counter and
+    // hands the previous count to its peers.
     const uint32_t peers = __match_any_sync(0xffffffffu, dig[k]);
+    const int leader = __ffs(peers) - 1;
     uint32_t old = 0;
-    if (valid) old = s_wc[warp][dig[k]];
-    __syncwarp();
-    if (valid && (peers & ltmask) == 0) s_wc[warp][dig[k]] = old + __popc(peers);
-    __syncwarp();
+    if (valid && lane == leader) old = atomicAdd(&s_wc[warp][dig[k]], (uint32_t)__popc(peers));
+    old = __shfl_sync(0xffffffffu, old, leader);
     rank[k] = old + __popc(peers & ltmask);
   }
   __syncthreads();
