@@ -61,6 +61,8 @@ WORKLOADS = {
                               metric="PBF particle-steps/s @16k (plain, 3 Jacobi iterations)"),
     # 16.7M particles (256^3 lattice, box 6.4 = 256 cells of h per axis): the grid/sort path
     # at a size where its HBM traffic, not launch latency, sets the time.
+    "pbf_dam_break_4m": dict(kind="fluids", lattice=(128, 256, 128), box=3.2, iters=3, max_steps=20,
+                             metric="PBF particle-steps/s @4.2M (plain, 3 Jacobi iterations)"),
     "pbf_dam_break_16m": dict(kind="fluids", lattice=(256, 256, 256), box=6.4, iters=3, max_steps=10,
                               metric="PBF particle-steps/s @16.7M (plain, 3 Jacobi iterations)"),
     "boids_131k": dict(kind="boids", n=131072, metric="boids particle-steps/s @131k"),
