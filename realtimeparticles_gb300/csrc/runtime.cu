@@ -1596,9 +1596,9 @@ int rtp_get_metrics(void* handle, rtp_metrics* out) {
   Handle* h = H(handle);
   std::memset(out, 0, sizeof *out);
   if (h->model == RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_get_metrics: fluids and clouds only");
-  if (!h->hasStep) return fail(RTP_ERR_STATE, "rtp_get_metrics: run a step first (the cell table is built by update)");
   const uint32_t n = (uint32_t)h->curN;
-  if (n == 0) return RTP_OK;
+  if (n == 0) return RTP_OK;  // no particles: all zero
+  if (!h->hasStep) return fail(RTP_ERR_STATE, "rtp_get_metrics: run a step first (the cell table is built by update)");
   RTP_CUDA(cudaMemsetAsync(h->mAcc, 0, sizeof(double) * 4, h->stream));
   RTP_CUDA(cudaMemsetAsync(h->mHist, 0, sizeof(uint32_t) * 80, h->stream));
   Launcher L;
