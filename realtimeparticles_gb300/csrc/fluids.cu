@@ -25,12 +25,13 @@ namespace rtp {
 
 // fld_predictPosition (fluids.cl:62-74) + fillCellIDs (grid.cl:76-86) + digit-0 histogram.
 // Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
+// With io.inPos / io.inVel the inputs come from host memory and are mirrored into pos / vel.
 template <bool BATCH>
-__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK p0, const float4* __restrict__ pos,
-                                                                const float4* __restrict__ vel, uint32_t n,
+__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK p0, float4* __restrict__ pos,
+                                                                float4* __restrict__ vel, uint32_t n,
                                                                 float4* __restrict__ pred, uint32_t* __restrict__ keys,
                                                                 int bits0, uint32_t* __restrict__ hist0, int clampOut,
-                                                                ZeroJob zero) {
+                                                                ZeroJob zero, HostIO io) {
   pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
   zero_job(zero);
@@ -46,7 +47,19 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK
       GridK g = g0;
       FluidK p = p0;
       scene_of<BATCH>(i, g, p);
-      const float4 x = ld4(pos + i), v = ld4(vel + i);
+      float4 x, v;
+      if (io.inPos) {
+        x = io.inPos[i];
+        pos[i] = x;
+      } else {
+        x = ld4(pos + i);
+      }
+      if (io.inVel) {
+        v = io.inVel[i];
+        vel[i] = v;
+      } else {
+        v = ld4(vel + i);
+      }
       const float4 nv = f4(__fadd_rn(v.x, gx), __fadd_rn(v.y, gy), __fadd_rn(v.z, gx), __fadd_rn(v.w, gx));
       const float4 pp = f4(__fadd_rn(x.x, __fmul_rn(nv.x, dt)), __fadd_rn(x.y, __fmul_rn(nv.y, dt)),
                            __fadd_rn(x.z, __fmul_rn(nv.z, dt)), __fadd_rn(x.w, __fmul_rn(nv.w, dt)));
@@ -288,7 +301,7 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
                                                           const uint2* __restrict__ table, uint32_t n,
                                                           const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
                                                           float4* __restrict__ vel, uint32_t* __restrict__ ids,
-                                                          PairList pl) {
+                                                          PairList pl, HostIO io) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
@@ -320,20 +333,26 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
   az = quad_sum<LANES>(az);
   aw = quad_sum<LANES>(aw);
   if (!active || q != 0) return;
-  vel[i] = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
+  const float4 vo = f4(vi.x + p.xsph * ax, vi.y + p.xsph * ay, vi.z + p.xsph * az, vi.w + p.xsph * aw);
+  vel[i] = vo;
   pos[i] = xi;
+  if (io.outVel) io.outVel[i] = vo;
+  if (io.outPos) io.outPos[i] = xi;
   if (ids) ids[i] = __ldg(idsS + i);
 }
 
 // fld_updatePosition alone (vorticity confinement disabled: Fluids.cpp:444 skips XSPH too).
 __global__ void k_fluid_final(const float4* __restrict__ pred, const float4* __restrict__ velS, uint32_t n,
                               const uint32_t* __restrict__ idsS, float4* __restrict__ pos, float4* __restrict__ vel,
-                              uint32_t* __restrict__ ids) {
+                              uint32_t* __restrict__ ids, HostIO io) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  pos[i] = ld4(pred + i);
-  vel[i] = ld4(velS + i);
+  const float4 x = ld4(pred + i), v = ld4(velS + i);
+  pos[i] = x;
+  vel[i] = v;
+  if (io.outPos) io.outPos[i] = x;
+  if (io.outVel) io.outVel[i] = v;
   if (ids) ids[i] = __ldg(idsS + i);
 }
 
@@ -408,15 +427,16 @@ static int check(const char* what) {
 
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
-int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
-                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L, const ZeroJob& zero) {
+int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uint32_t n, float4* pred,
+                  uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L, const ZeroJob& zero,
+                  const HostIO& io) {
   L.begin("fld_predict");
   if (p.bt.scenes)
     launch(L, k_fluid_predict<true>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
-                                                                     clampOut ? 1 : 0, zero);
+                                                                     clampOut ? 1 : 0, zero, io);
   else
     launch(L, k_fluid_predict<false>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0],
-                                                                      hist0, clampOut ? 1 : 0, zero);
+                                                                      hist0, clampOut ? 1 : 0, zero, io);
   L.end("fld_predict");
   return check("k_fluid_predict");
 }
@@ -489,7 +509,7 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
 
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L, bool vorticityDone) {
+               Launcher& L, bool vorticityDone, const HostIO& io) {
   if (p.vorticity) {
     int rc = RTP_OK;
     if (!vorticityDone) {
@@ -510,13 +530,13 @@ int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS
       constexpr bool BATCH = decltype(B)::value;
       constexpr int LANES = decltype(LN)::value;
       launch(L, k_fluid_xsph_final<BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128), g, p, pred, velS, table, n, idsS,
-                                                                                      pos, vel, ids, pl);
+                                                                                      pos, vel, ids, pl, io);
     });
     L.end("fld_xsph_final");
     return check("k_fluid_xsph_final");
   }
   L.begin("fld_final");
-  launch(L, k_fluid_final, dim3(blocks(n, 256)), dim3(256), pred, velS, n, idsS, pos, vel, ids);
+  launch(L, k_fluid_final, dim3(blocks(n, 256)), dim3(256), pred, velS, n, idsS, pos, vel, ids, io);
   L.end("fld_final");
   return check("k_fluid_final");
 }

@@ -83,9 +83,21 @@ __device__ __forceinline__ void block_error_partial(float v, float* out) {
 // Total-lambda bookkeeping of k_fluid_lambda (warm start).
 constexpr int kTotNone = 0, kTotWrite = 1, kTotAdd = 2;
 
-int fluid_presort(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, uint32_t n, float4* pred,
+// Host-resident input and output of one step (pinned host memory, device-visible pointers):
+// the step's first kernel reads pos / vel from inPos / inVel (and mirrors them into the
+// canonical device buffers), its last kernel also writes the results to outPos / outVel.
+// A null pointer leaves that transfer to the device buffers alone.
+struct HostIO {
+  const float4* inPos = nullptr;
+  const float4* inVel = nullptr;
+  float4* outPos = nullptr;
+  float4* outVel = nullptr;
+};
+
+// pos / vel are the canonical device buffers (written only to mirror io.inPos / io.inVel).
+int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L,
-                  const ZeroJob& zero = ZeroJob{});
+                  const ZeroJob& zero = ZeroJob{}, const HostIO& io = HostIO{});
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table,
                     uint32_t n, float* lambda, float* density, bool last, const float4* posS, float4* velS,
                     const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone);
@@ -100,7 +112,7 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
                      Launcher& L);
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L, bool vorticityDone = false);
+               Launcher& L, bool vorticityDone = false, const HostIO& io = HostIO{});
 int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, const uint2* table, uint32_t n,
                   double* acc, uint32_t* hist, Launcher& L);
 

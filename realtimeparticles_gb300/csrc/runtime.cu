@@ -163,6 +163,12 @@ struct Handle {
   cudaGraphExec_t graph = nullptr;
   bool graphValid = false;
   bool graphProfiled = false;
+  // A fluids step over host-resident state (rtp_update_host with pinned buffers): the same
+  // step captured with the host pointers it reads and writes (io, set while capturing).
+  HostIO io{};
+  cudaGraphExec_t graphHost = nullptr;
+  bool graphHostValid = false;
+  HostIO graphHostIO{};
 
   // Profiling.
   bool profiling = false;
@@ -337,6 +343,7 @@ static int alloc_buffers(Handle* h) {
 static void free_handle(Handle* h) {
   if (!h) return;
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->graphHost) cudaGraphExecDestroy(h->graphHost);
   for (void* p : h->allocs) cudaFree(p);
   if (h->ground) cudaFree(h->ground);
   if (h->flush) cudaFree(h->flush);
@@ -382,7 +389,10 @@ static int ws_forget(Handle* h) {
   return RTP_OK;
 }
 
-static void invalidate(Handle* h) { h->graphValid = false; }
+static void invalidate(Handle* h) {
+  h->graphValid = false;
+  h->graphHostValid = false;
+}
 
 // ---- one model step (the update() sequences) ------------------------------------------
 // Fluids.cpp:412-424: predict, cell ids, sort {pos, vel, predPos} (+ ids), cell table.
@@ -392,7 +402,7 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
   const GridK& g = h->g;
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
-  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L, zero));
+  RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L, zero, h->io));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -463,7 +473,8 @@ static int record_fluids_step(Handle* h, Launcher& L) {
     RTP_TRY(ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, false, L));
   }
   // Fluids.cpp:444-457.
-  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L, vortDone);
+  return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L, vortDone,
+                    h->io);
 }
 
 // Warm-started substep: the network's lambda and residual give the first correction, then
@@ -534,7 +545,7 @@ static int record_fluids_ws_step(Handle* h, Launcher& L) {
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(guard body)");
   }
   return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
-                    vortDone);
+                    vortDone, h->io);
 }
 
 // One plain step with `iters` iterations that also writes training samples.
@@ -1013,6 +1024,49 @@ static int build_graph(Handle* h) {
   h->graphValid = true;
   h->graphProfiled = h->profiling;
   return RTP_OK;
+}
+
+// The fluids step capturing host I/O `io` (no profiling events) into graphHost.
+static int build_host_graph(Handle* h, const HostIO& io) {
+  if (h->graphHost) {
+    cudaGraphExecDestroy(h->graphHost);
+    h->graphHost = nullptr;
+  }
+  h->graphHostValid = false;
+  Launcher L;
+  L.stream = h->stream;
+  h->io = io;
+  RTP_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = record_step(h, L);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(h->stream, &graph);
+  h->io = HostIO{};
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+  const cudaError_t ei = cudaGraphInstantiate(&h->graphHost, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate");
+  h->graphHostValid = true;
+  h->graphHostIO = io;
+  return RTP_OK;
+}
+
+// The device-visible address of pinned host memory p (nullptr in, nullptr out); false when p
+// is not pinned (pageable memory goes through cudaMemcpyAsync instead).
+static bool pinned_device_ptr(const void* p, void** out) {
+  *out = nullptr;
+  if (!p) return true;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+  *out = a.devicePointer;
+  return true;
 }
 
 static int collect_profile(Handle* h) {
@@ -1503,6 +1557,28 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
   Handle* h = H(handle);
   if (count != h->curN) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_update_host: count must equal the particle count");
   const size_t bytes = sizeof(float4) * (size_t)count;
+  // One fluids step on pinned buffers: its first kernel reads them and its last writes them
+  // (no separate copies); other cases copy with cudaMemcpyAsync around rtp_update.
+  if (h->model == RTP_MODEL_FLUIDS && nsteps == 1 && count > 0 && !h->paused && !h->profiling) {
+    void *ip, *iv, *op, *ov;
+    if (pinned_device_ptr(posIn, &ip) && pinned_device_ptr(velIn, &iv) && pinned_device_ptr(posOut, &op) &&
+        pinned_device_ptr(velOut, &ov)) {
+      HostIO io;
+      io.inPos = (const float4*)ip;
+      io.inVel = (const float4*)iv;
+      io.outPos = (float4*)op;
+      io.outVel = (float4*)ov;
+      const HostIO& k = h->graphHostIO;
+      if (!h->graphHostValid || k.inPos != io.inPos || k.inVel != io.inVel || k.outPos != io.outPos ||
+          k.outVel != io.outVel)
+        RTP_TRY(build_host_graph(h, io));
+      if (posIn) RTP_TRY(ws_forget(h));
+      RTP_CUDA(cudaGraphLaunch(h->graphHost, h->stream));
+      h->hasStep = true;
+      RTP_CUDA(cudaStreamSynchronize(h->stream));
+      return RTP_OK;
+    }
+  }
   if (posIn && bytes) {
     RTP_CUDA(cudaMemcpyAsync(h->pos, posIn, bytes, cudaMemcpyHostToDevice, h->stream));
     RTP_TRY(ws_forget(h));

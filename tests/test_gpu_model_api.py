@@ -1,5 +1,7 @@
 """Model API behaviour on the GPU: reset cases, setters, JSON inputs, errors, buffers,
 profiling (physics/Model.hpp:81-216, physics/ocl/OclModel.hpp)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -120,3 +122,40 @@ def test_update_host_equals_upload_update_download():
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
 
+
+
+def test_update_host_pinned_buffers():
+    """Pinned host buffers take the path whose first and last kernels read and write host memory
+    directly; results equal the copy path bit for bit, for shared and separate in/out buffers and
+    after the buffers change."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.dam_break(lattice=(8, 16, 16))
+    n = sc["pos"].shape[0]
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True).numpy()
+        t[:] = a
+        return t
+
+    ref, fast = model.Fluids(sc["model_params"]), model.Fluids(sc["model_params"])
+    with ref, fast:
+        for m in (ref, fast):
+            m.setFluidParams(sc["fluid_params"])
+            m.setJacobiIterations(3)
+        rp, rv = sc["pos"].copy(), sc["vel"].copy()          # pageable: the copy path
+        fp, fv = pinned(sc["pos"]), pinned(sc["vel"])        # pinned: the direct path
+        for _ in range(3):
+            ref.updateHost(rp, rv, 1)
+            fast.updateHost(fp, fv, 1)
+            assert np.array_equal(rp, fp) and np.array_equal(rv, fv)
+        # Separate output buffers, then new input buffers (the step is captured again).
+        op, ov = pinned(np.zeros_like(fp)), pinned(np.zeros_like(fv))
+        P = lambda a: a.ctypes.data_as(C.c_void_p)
+        call("rtp_update_host", fast.handle, P(fp), P(fv), n, 1, P(op), P(ov))
+        ref.updateHost(rp, rv, 1)
+        assert np.array_equal(op, rp) and np.array_equal(ov, rv)
+        fp2, fv2 = pinned(op), pinned(ov)
+        call("rtp_update_host", fast.handle, P(fp2), P(fv2), n, 2, P(fp2), P(fv2))   # two steps: copy path
+        ref.updateHost(rp, rv, 2)
+        assert np.array_equal(fp2, rp) and np.array_equal(fv2, rv)
+        assert np.array_equal(fast.download(abi.BUF_POS), rp)  # the device state follows
