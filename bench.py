@@ -17,6 +17,9 @@ Metric: particle-steps/s.
   synchronisation), timed on the host clock.
 * roofline: the dominant kernel's algorithmic bytes / its mean CUDA-event duration
   (captured event nodes inside the same graph replays), against MEASURED_PEAKS.json.
+* sweep (fluids, when the dominant kernel is the density/lambda sweep): candidates tested and
+  pairs within h evaluated per second by that kernel (it is bound by dependent loads, so its
+  HBM fraction says little).
 * cpu_baseline: the reference's own kernels (physics/ocl/kernels/*.cl compiled for the
   CPU by oracle/ref/build_ref.py, OpenMP over the host cores) on a bounded sample of the
   same workload; the oracle's restatement when those are not built.
@@ -385,6 +388,22 @@ GRID_SORT_KERNELS = ("fld_predict", "sort_clear", "sort_scan", "sort_pass", "sor
                      "cellTable")
 
 
+def mean_candidates(c, table, keys):
+    """Mean number of particles in the 27 cells (wrapped modulo the grid, as the fluids sweeps
+    visit them, fluids.cl:101-123) around each particle's cell: the candidates one full sweep
+    tests per particle.  table: the reference-format cell table; keys: the sorted cell keys."""
+    res = tuple(int(r) for r in c.gridRes)
+    cnt = np.where(table[:, 1] >= table[:, 0], table[:, 1].astype(np.int64) - table[:, 0] + 1, 0)
+    cnt = cnt[:int(np.prod(res))].reshape(res)
+    cand = np.zeros_like(cnt)
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                cand += np.roll(cnt, (-dx, -dy, -dz), axis=(0, 1, 2))
+    k = keys[keys < cand.size]
+    return float(cand.reshape(-1)[k].mean()) if k.size else 0.0
+
+
 def grid_sort_summary(kt, steps, n, c, nonempty, peak):
     """HBM roofline of the grid/sort path of the PBF step (predict + cell keys, stable radix
     sort with the payload gather, cell table): algorithmic bytes of its kernels per step
@@ -501,11 +520,18 @@ def run_ours(args):
     alg = KERNEL_BYTES.get(dom_name, 0) * n
     achieved = alg / (dom_avg_ms / 1000.0) / 1e9
     share = {k: round(v[1] / sum(x[1] for x in kt.values()), 4) for k, v in kt.items()}
-    grid_sort = None
+    grid_sort = sweep = None
     if w["kind"] == "fluids":  # (a batch has one grid per scene)
         tab = m.download(abi.BUF_CELL_TABLE)
         nonempty = int(np.count_nonzero(tab[:, 1] >= tab[:, 0]))
         grid_sort = grid_sort_summary(kt, args.steps, n, m.constants(), nonempty, peak)
+        if dom_name == "fld_lambda":
+            # The dominant sweep is bound by dependent loads, not HBM: its work rates.
+            cand = mean_candidates(m.constants(), tab, m.download(abi.BUF_CELL_ID))
+            nbr = m.metrics().meanNeighbours
+            sweep = {"kernel": dom_name, "candidates_per_particle": cand, "neighbours_per_particle": nbr,
+                     "candidate_tests_per_s": n * cand / (dom_avg_ms / 1000.0),
+                     "pair_evaluations_per_s": n * nbr / (dom_avg_ms / 1000.0)}
 
     # End to end through the public API with pinned host buffers.
     try:
@@ -558,6 +584,8 @@ def run_ours(args):
         }
         if grid_sort:
             out["grid_sort"] = grid_sort
+        if sweep:
+            out["sweep"] = sweep
         if tune:
             out["autotune"] = tune
         if batch:
