@@ -56,36 +56,62 @@ __device__ __forceinline__ void image_shift(const GridK& g, uint32_t code, float
 }
 
 // Filter pass over the clouds neighbourhood: add(entry) for each candidate within h2, in
-// visiting order, four position loads in flight.
+// visiting order.  Each (x, y) row's three z cells are read from the table together and
+// visited as one range where they are contiguous with the same image shift (all but the
+// z-wrapped cells at the box faces), eight position loads in flight.
 template <class ADD>
 __device__ __forceinline__ void filter_cloud_neighbours(const GridK& g, const uint2* __restrict__ table,
                                                         const float4* __restrict__ pos, float4 xi, float h2,
                                                         ADD&& add) {
   int cx, cy, cz;
   cell3(g, xi, cx, cy, cz);
+  auto wrap = [](int u, int R) { return u < 0 ? u + R : (u >= R ? u - R : u); };
+  auto shift = [](int u, int R, float w) { return u >= R ? 2.0f * w : (u < 0 ? -2.0f * w : 0.0f); };
+  const uint32_t z0 = (uint32_t)wrap(cz - 1, g.R[2]), z1 = (uint32_t)wrap(cz, g.R[2]), z2 = (uint32_t)wrap(cz + 1, g.R[2]);
+  const float s0 = shift(cz - 1, g.R[2], g.W[2]), s1 = shift(cz, g.R[2], g.W[2]), s2 = shift(cz + 1, g.R[2], g.W[2]);
 #pragma unroll 1
   for (int dx = -1; dx <= 1; ++dx) {
     const int ux = cx + dx;
-    const int nx = (ux + g.R[0]) % g.R[0];
-    const float shx = ux >= g.R[0] ? 2.0f * g.W[0] : (ux < 0 ? -2.0f * g.W[0] : 0.0f);
+    const int nx = wrap(ux, g.R[0]);
+    const float shx = shift(ux, g.R[0], g.W[0]);
 #pragma unroll 1
     for (int dy = -1; dy <= 1; ++dy) {
       const int ny = cy + dy;
       if (ny >= g.R[1] || ny < 0) continue;
       const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
-#pragma unroll 1
-      for (int dz = -1; dz <= 1; ++dz) {
-        const int uz = cz + dz;
-        const int nz = (uz + g.R[2]) % g.R[2];
-        const float shz = uz >= g.R[2] ? 2.0f * g.W[2] : (uz < 0 ? -2.0f * g.W[2] : 0.0f);
+      uint32_t b0, e0, b1, e1, b2, e2;
+      cell_range(table, row + z0, g.cap, b0, e0);
+      cell_range(table, row + z1, g.cap, b1, e1);
+      cell_range(table, row + z2, g.cap, b2, e2);
+      auto run = [&](uint32_t b, uint32_t e, float shz) {
         const uint32_t code = image_code(shx, shz) << 28;
-        uint32_t j0, j1;
-        cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
-        visit_range_x4(j0, j1, [&](uint32_t j) { return ld4(pos + j); }, [&](uint32_t j, float4 xj) {
+        visit_range_x8(b, e, [&](uint32_t j) { return ld4(pos + j); }, [&](uint32_t j, float4 xj) {
           const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
           if (vx * vx + vy * vy + vz * vz < h2) add(j | code);
         });
+      };
+      // Cells in visiting order, joined while contiguous with the same shift.
+      uint32_t cb = b0, ce = e0;
+      float cs = s0;
+      const uint32_t rb[2] = {b1, b2}, re[2] = {e1, e2};
+      const float rs[2] = {s1, s2};
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        if (rb[r] == re[r]) continue;
+        if (cb == ce) {
+          cb = rb[r];
+          ce = re[r];
+          cs = rs[r];
+        } else if (ce == rb[r] && cs == rs[r]) {
+          ce = re[r];
+        } else {
+          run(cb, ce, cs);
+          cb = rb[r];
+          ce = re[r];
+          cs = rs[r];
+        }
       }
+      if (cb != ce) run(cb, ce, cs);
     }
   }
 }
@@ -112,12 +138,22 @@ __device__ __forceinline__ void quad_cloud_pairs(const GridK& g, const uint2* __
   const uint32_t c = __ldg(L.count + i);
   if (c != kListOverflow) {
     const uint32_t* base = L.idx + i;
-    for (uint32_t kk = q; kk < c; kk += kQuad) {
-      const uint32_t e = __ldg(base + (size_t)kk * L.stride);
+    auto visit = [&](uint32_t e) {
       float shx, shz;
       image_shift(g, e >> 28, shx, shz);
       f(e & 0x0FFFFFFFu, shx, shz);
+    };
+    uint32_t kk = q;
+    for (; kk + 3 * kQuad < c; kk += 4 * kQuad) {  // four entries in flight
+      const uint32_t e0 = __ldg(base + (size_t)kk * L.stride), e1 = __ldg(base + (size_t)(kk + kQuad) * L.stride);
+      const uint32_t e2 = __ldg(base + (size_t)(kk + 2 * kQuad) * L.stride);
+      const uint32_t e3 = __ldg(base + (size_t)(kk + 3 * kQuad) * L.stride);
+      visit(e0);
+      visit(e1);
+      visit(e2);
+      visit(e3);
     }
+    for (; kk < c; kk += kQuad) visit(__ldg(base + (size_t)kk * L.stride));
   } else if (q == 0) {
     for_each_cloud_neighbour(g, table, xi, f);
   }
@@ -210,30 +246,30 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g
   ListWriter lw(pl, i);
   filter_cloud_neighbours(g, table, pos, xi, k.h2, lw);
   float lap = 0.0f, sg = 0.0f, ssq = 0.0f;
-  auto body = [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pos + j);
+  auto body_at = [&](float4 xj, float tj, float shx, float shz) {
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
       float r;
       const float s = k.gs(r2, r);
       const float vg = r2 * s;  // dot(vec, gradSpiky(vec))
-      lap += (ti - __ldg(temp + j)) * vg / (r2 + kFloatEps);
+      lap += (ti - tj) * vg / (r2 + kFloatEps);
       const float d = vg / (r2 * c.cloudRho0 + kFloatEps);
       sg += d;
       ssq += d * d;
     }
   };
-  if (lw.ok()) {
-    for (uint32_t kk = 0; kk < lw.n; ++kk) {
-      const uint32_t e = lw.at(kk);
-      float shx, shz;
-      image_shift(g, e >> 28, shx, shz);
-      body(e & 0x0FFFFFFFu, shx, shz);
-    }
-  } else {
+  auto body = [&](uint32_t j, float shx, float shz) { body_at(ld4(pos + j), __ldg(temp + j), shx, shz); };
+  if (lw.ok())
+    visit_list_x4(0, lw.n, 1, [&](uint32_t kk) { return lw.at(kk); },
+                  [&](uint32_t e) { return Pair4{ld4(pos + (e & 0x0FFFFFFFu)), __ldg(temp + (e & 0x0FFFFFFFu))}; },
+                  [&](uint32_t e, Pair4 a) {
+                    float shx, shz;
+                    image_shift(g, e >> 28, shx, shz);
+                    body_at(a.x, a.s, shx, shz);
+                  });
+  else
     for_each_cloud_neighbour(g, table, xi, body);
-  }
   pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   lap /= c.cloudRho0;
   ssq += sg * sg;
@@ -242,7 +278,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g
 
 // cld_computeConstraintCorrectionTemp + cld_correctTemperature (in place: the sweep reads
 // only lamT and positions of the neighbours).  kQuad lanes per particle.
-__global__ void __launch_bounds__(128) k_cloud_temp_correct(GridK g, CloudK c, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(128, 8) k_cloud_temp_correct(GridK g, CloudK c, const float4* __restrict__ pos,
                                                             const float* __restrict__ lamT,
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             float* __restrict__ temp, PairList pl) {
@@ -284,8 +320,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
   ListWriter lw(pl, i);
   filter_cloud_neighbours(g, table, pred, xi, k.h2, lw);
   float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
-  auto body = [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pred + j);
+  auto body_at = [&](float4 xj, float shx, float shz) {
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
@@ -299,16 +334,16 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
       ssq += a * a + b * b + cc * cc;
     }
   };
-  if (lw.ok()) {
-    for (uint32_t kk = 0; kk < lw.n; ++kk) {
-      const uint32_t e = lw.at(kk);
-      float shx, shz;
-      image_shift(g, e >> 28, shx, shz);
-      body(e & 0x0FFFFFFFu, shx, shz);
-    }
-  } else {
+  auto body = [&](uint32_t j, float shx, float shz) { body_at(ld4(pred + j), shx, shz); };
+  if (lw.ok())
+    visit_list_x4(0, lw.n, 1, [&](uint32_t kk) { return lw.at(kk); },
+                  [&](uint32_t e) { return ld4(pred + (e & 0x0FFFFFFFu)); }, [&](uint32_t e, float4 xj) {
+                    float shx, shz;
+                    image_shift(g, e >> 28, shx, shz);
+                    body_at(xj, shx, shz);
+                  });
+  else
     for_each_cloud_neighbour(g, table, xi, body);
-  }
   pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
@@ -320,7 +355,7 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
 // cld_computeConstraintCorrection, cld_correctPosition x2 and the mixed boundary
 // (Clouds.cpp:577-586); LAST adds cld_updateVel (clouds.cl:958-966).  kQuad lanes.
 template <bool LAST>
-__global__ void __launch_bounds__(128) k_cloud_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(128, 8) k_cloud_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut, float4* __restrict__ tot,
                                                       float4* __restrict__ velS, PairList pl) {
@@ -389,32 +424,32 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, 
   ListWriter lw(pl, i);
   filter_cloud_neighbours(g, table, pred, xi, k.h2, lw);
   float4 w = f4(0.f, 0.f, 0.f, 0.f);
-  auto body = [&](uint32_t j, float shx, float shz) {
-    const float4 xj = ld4(pred + j);
+  auto body_at = [&](float4 xj, float4 vj, float shx, float shz) {
     const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
       float r;
       const float s = k.gs(r2, r);
-      w = w + cross4(ld4(velS + j) - vi, f4(vx * s, vy * s, vz * s, 0.0f));
+      w = w + cross4(vj - vi, f4(vx * s, vy * s, vz * s, 0.0f));
     }
   };
-  if (lw.ok()) {
-    for (uint32_t kk = 0; kk < lw.n; ++kk) {
-      const uint32_t e = lw.at(kk);
-      float shx, shz;
-      image_shift(g, e >> 28, shx, shz);
-      body(e & 0x0FFFFFFFu, shx, shz);
-    }
-  } else {
+  auto body = [&](uint32_t j, float shx, float shz) { body_at(ld4(pred + j), ld4(velS + j), shx, shz); };
+  if (lw.ok())
+    visit_list_x4(0, lw.n, 1, [&](uint32_t kk) { return lw.at(kk); },
+                  [&](uint32_t e) { return Pair44{ld4(pred + (e & 0x0FFFFFFFu)), ld4(velS + (e & 0x0FFFFFFFu))}; },
+                  [&](uint32_t e, Pair44 a) {
+                    float shx, shz;
+                    image_shift(g, e >> 28, shx, shz);
+                    body_at(a.x, a.v, shx, shz);
+                  });
+  else
     for_each_cloud_neighbour(g, table, xi, body);
-  }
   pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   vort[i] = w;
 }
 
 // cld_applyVorticityConfinement (clouds.cl:790-850).  kQuad lanes per particle.
-__global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(128, 8) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
                                                        uint32_t n, float4* __restrict__ velS, PairList pl) {
   pdl_enter();
@@ -455,7 +490,7 @@ __global__ void __launch_bounds__(128) k_cloud_confine(GridK g, FluidK p, const 
 
 // cld_applyXsphViscosityCorrection (clouds.cl:856-915) + cld_updatePosition (:942-953);
 // writes the canonical state (pos, vel, temp, vapor, cloud, buoyancy, ids).  kQuad lanes.
-__global__ void __launch_bounds__(128) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(128, 8) k_cloud_final(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred,
                                                      const float4* __restrict__ velS, const uint2* __restrict__ table,
                                                      uint32_t n, CloudState s, PairList pl) {
   pdl_enter();
