@@ -2,6 +2,7 @@
 #pragma once
 
 #include "rtp_internal.hpp"
+#include "sweep.cuh"
 
 namespace rtp {
 
