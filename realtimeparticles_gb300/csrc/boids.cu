@@ -12,10 +12,12 @@
 
 namespace rtp {
 
-__global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, const float4* __restrict__ pos, uint32_t n,
+// With io.inPos / io.inVel the state comes from host memory and is mirrored into pos / vel.
+__global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, float4* __restrict__ pos,
+                                                             float4* __restrict__ vel, uint32_t n,
                                                              uint32_t* __restrict__ keys, int bits0,
                                                              uint32_t* __restrict__ hist0, ZeroJob zero,
-                                                             float4* __restrict__ track) {
+                                                             float4* __restrict__ track, HostIO io) {
   pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
   zero_job(zero);
@@ -30,7 +32,15 @@ __global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, const floa
   for (int k = 0; k < kSortItems; ++k) {
     const uint32_t i = base + k * kSortThreads + threadIdx.x;
     if (i < n) {
-      const uint32_t key = cell_key(g, ld4(pos + i));
+      float4 x;
+      if (io.inPos) {
+        x = io.inPos[i];
+        pos[i] = x;
+      } else {
+        x = ld4(pos + i);
+      }
+      if (io.inVel) vel[i] = io.inVel[i];
+      const uint32_t key = cell_key(g, x);
       keys[i] = key;
       th.add(key);
     }
@@ -50,7 +60,7 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             const uint32_t* __restrict__ idsS, float4* __restrict__ pos,
                                                             float4* __restrict__ vel, float4* __restrict__ acc,
-                                                            uint32_t* __restrict__ ids, TargetK tk) {
+                                                            uint32_t* __restrict__ ids, TargetK tk, HostIO io) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -171,6 +181,8 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
   }
   pos[i] = cp;
   vel[i] = v;
+  if (io.outPos) io.outPos[i] = cp;
+  if (io.outVel) io.outVel[i] = v;
   if (ids) ids[i] = __ldg(idsS + i);
 }
 
@@ -179,28 +191,29 @@ static int check(const char* what) {
   return e == cudaSuccess ? RTP_OK : cuda_fail(e, what);
 }
 
-int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
-                  Launcher& L, const ZeroJob& zero, const TargetK& tk) {
+int boids_presort(const GridK& g, float4* pos, float4* vel, uint32_t n, uint32_t* keys, const SortPlan& plan,
+                  uint32_t* hist0, Launcher& L, const ZeroJob& zero, const TargetK& tk, const HostIO& io) {
   L.begin("bd_keys");
-  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, n, keys, plan.bits[0], hist0, zero, tk.track);
+  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, vel, n, keys, plan.bits[0], hist0, zero, tk.track,
+         io);
   L.end("bd_keys");
   return check("k_boids_keys");
 }
 
 int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, bool dim2, const float4* posS,
                        const float4* velS, const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos,
-                       float4* vel, float4* acc, uint32_t* ids, Launcher& L, const TargetK& tk) {
+                       float4* vel, float4* acc, uint32_t* ids, Launcher& L, const TargetK& tk, const HostIO& io) {
   const uint32_t b = (n + 127) / 128;
   L.begin("bd_rules_update");
   if (periodic && dim2)
-    launch(L, k_boids_rules_update<true, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
+    launch(L, k_boids_rules_update<true, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk, io);
   else if (periodic)
-    launch(L, k_boids_rules_update<true, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
+    launch(L, k_boids_rules_update<true, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk, io);
   else if (dim2)
-    launch(L, k_boids_rules_update<false, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk);
+    launch(L, k_boids_rules_update<false, true>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc, ids, tk, io);
   else
     launch(L, k_boids_rules_update<false, false>, dim3(b), dim3(128), g, p, posS, velS, table, n, idsS, pos, vel, acc,
-           ids, tk);
+           ids, tk, io);
   L.end("bd_rules_update");
   return check("k_boids_rules_update");
 }

@@ -23,10 +23,12 @@ struct TargetK {
   float sign = 0.0f;        // (float)targetSignEffect
 };
 
-int boids_presort(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, const SortPlan& plan, uint32_t* hist0,
-                  Launcher& L, const ZeroJob& zero = ZeroJob{}, const TargetK& tk = TargetK{});
+// pos / vel are the canonical device buffers (written only to mirror io.inPos / io.inVel).
+int boids_presort(const GridK& g, float4* pos, float4* vel, uint32_t n, uint32_t* keys, const SortPlan& plan,
+                  uint32_t* hist0, Launcher& L, const ZeroJob& zero = ZeroJob{}, const TargetK& tk = TargetK{},
+                  const HostIO& io = HostIO{});
 int boids_rules_update(const GridK& g, const BoidsK& p, bool periodic, bool dim2, const float4* posS, const float4* velS,
                        const uint2* table, uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, float4* acc,
-                       uint32_t* ids, Launcher& L, const TargetK& tk = TargetK{});
+                       uint32_t* ids, Launcher& L, const TargetK& tk = TargetK{}, const HostIO& io = HostIO{});
 
 }  // namespace rtp

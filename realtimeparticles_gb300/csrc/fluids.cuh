@@ -83,17 +83,6 @@ __device__ __forceinline__ void block_error_partial(float v, float* out) {
 // Total-lambda bookkeeping of k_fluid_lambda (warm start).
 constexpr int kTotNone = 0, kTotWrite = 1, kTotAdd = 2;
 
-// Host-resident input and output of one step (pinned host memory, device-visible pointers):
-// the step's first kernel reads pos / vel from inPos / inVel (and mirrors them into the
-// canonical device buffers), its last kernel also writes the results to outPos / outVel.
-// A null pointer leaves that transfer to the device buffers alone.
-struct HostIO {
-  const float4* inPos = nullptr;
-  const float4* inVel = nullptr;
-  float4* outPos = nullptr;
-  float4* outVel = nullptr;
-};
-
 // pos / vel are the canonical device buffers (written only to mirror io.inPos / io.inVel).
 int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L,

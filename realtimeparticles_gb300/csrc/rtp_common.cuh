@@ -171,6 +171,17 @@ __device__ __forceinline__ void zero_job(const ZeroJob& z) {
   }
 }
 
+// Host-resident input and output of one step (pinned host memory, device-visible pointers):
+// the step's first kernel reads pos / vel from inPos / inVel (and mirrors them into the
+// canonical device buffers), its last kernel also writes the results to outPos / outVel.
+// A null pointer leaves that transfer to the device buffers alone.
+struct HostIO {
+  const float4* inPos = nullptr;
+  const float4* inVel = nullptr;
+  float4* outPos = nullptr;
+  float4* outVel = nullptr;
+};
+
 // Sort-tile histogram of digit 0, for the kernels that produce the keys.  The calling
 // block has kSortThreads threads and handles tile blockIdx.x: element
 // blockIdx.x * kSortTile + k * kSortThreads + threadIdx.x for k < kSortItems.

@@ -163,8 +163,8 @@ struct Handle {
   cudaGraphExec_t graph = nullptr;
   bool graphValid = false;
   bool graphProfiled = false;
-  // A fluids step over host-resident state (rtp_update_host with pinned buffers): the same
-  // step captured with the host pointers it reads and writes (io, set while capturing).
+  // A fluids or boids step over host-resident state (rtp_update_host with pinned buffers): the
+  // same step captured with the host pointers it reads and writes (io, set while capturing).
   HostIO io{};
   cudaGraphExec_t graphHost = nullptr;
   bool graphHostValid = false;
@@ -583,7 +583,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
     tk.radius = h->tp.radiusEffect;
     tk.sign = (float)h->tp.signEffect;
   }
-  RTP_TRY(boids_presort(g, h->pos, n, h->ss.keysA, plan, h->ss.hist, L, zero, tk));
+  RTP_TRY(boids_presort(g, h->pos, h->vel, n, h->ss.keysA, plan, h->ss.hist, L, zero, tk, h->io));
   GatherList gl;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
@@ -606,7 +606,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
   // Boids.cpp:346-349: the 2D rules kernel for a 2D model.
   return boids_rules_update(g, bk, h->boundary == RTP_BOUNDARY_CYCLIC_WALL, h->mp.dimension == 2, h->posS, h->velS,
                             h->table, n, h->idsS,
-                            h->pos, h->vel, h->acc, h->ids, L, tk);
+                            h->pos, h->vel, h->acc, h->ids, L, tk, h->io);
 }
 
 static CloudK make_cloudk(const Handle* h) {
@@ -1026,7 +1026,7 @@ static int build_graph(Handle* h) {
   return RTP_OK;
 }
 
-// The fluids step capturing host I/O `io` (no profiling events) into graphHost.
+// The step capturing host I/O `io` (no profiling events) into graphHost.
 static int build_host_graph(Handle* h, const HostIO& io) {
   if (h->graphHost) {
     cudaGraphExecDestroy(h->graphHost);
@@ -1557,9 +1557,10 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
   Handle* h = H(handle);
   if (count != h->curN) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_update_host: count must equal the particle count");
   const size_t bytes = sizeof(float4) * (size_t)count;
-  // One fluids step on pinned buffers: its first kernel reads them and its last writes them
-  // (no separate copies); other cases copy with cudaMemcpyAsync around rtp_update.
-  if (h->model == RTP_MODEL_FLUIDS && nsteps == 1 && count > 0 && !h->paused && !h->profiling) {
+  // One fluids or boids step on pinned buffers: its first kernel reads them and its last
+  // writes them (no separate copies); other cases copy with cudaMemcpyAsync around rtp_update.
+  const bool direct = h->model == RTP_MODEL_FLUIDS || h->model == RTP_MODEL_BOIDS;
+  if (direct && nsteps == 1 && count > 0 && !h->paused && !h->profiling) {
     void *ip, *iv, *op, *ov;
     if (pinned_device_ptr(posIn, &ip) && pinned_device_ptr(velIn, &iv) && pinned_device_ptr(posOut, &op) &&
         pinned_device_ptr(velOut, &ov)) {
@@ -1573,6 +1574,7 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
           k.outVel != io.outVel)
         RTP_TRY(build_host_graph(h, io));
       if (posIn) RTP_TRY(ws_forget(h));
+      if (target_on(h)) RTP_TRY(feed_target(h, 1));
       RTP_CUDA(cudaGraphLaunch(h->graphHost, h->stream));
       h->hasStep = true;
       RTP_CUDA(cudaStreamSynchronize(h->stream));

@@ -159,3 +159,32 @@ def test_update_host_pinned_buffers():
         ref.updateHost(rp, rv, 2)
         assert np.array_equal(fp2, rp) and np.array_equal(fv2, rv)
         assert np.array_equal(fast.download(abi.BUF_POS), rp)  # the device state follows
+
+
+def test_update_host_pinned_boids_with_target():
+    """The direct host path for boids (keys kernel reads, rules kernel writes host memory),
+    target attractor on: equal to the copy path bit for bit."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.boids_cloud(n=5000, seed=3)
+    runs = []
+    for use_pinned in (False, True):
+        with model.Boids(sc["model_params"]) as m:
+            m.setBoidsParams(sc["boids_params"])
+            m.setTimeStep(0.01)
+            m.setBoundary(abi.CYCLIC_WALL)
+            tp = model.default_target_params()
+            tp.enabled = 1
+            tp.radiusEffect = 0.8
+            m.setTarget(tp)
+            if use_pinned:
+                pos = torch.empty((5000, 4), dtype=torch.float32, pin_memory=True).numpy()
+                vel = torch.empty((5000, 4), dtype=torch.float32, pin_memory=True).numpy()
+                pos[:], vel[:] = sc["pos"], sc["vel"]
+            else:
+                pos, vel = sc["pos"].copy(), sc["vel"].copy()
+            for _ in range(4):
+                m.updateHost(pos, vel, 1)
+            runs.append((pos.copy(), vel.copy(), m.download(abi.BUF_ACC), m.targetPos()))
+    for a, b in zip(runs[0][:3], runs[1][:3]):
+        assert np.array_equal(a, b)
+    assert runs[0][3] == runs[1][3]
