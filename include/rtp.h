@@ -285,10 +285,10 @@ int rtp_synchronize(void* handle);
  * runs nsteps updates (rtp_update) and copies them back, all ordered on the handle's stream
  * with a single synchronisation at the end; it returns once posOut / velOut hold the result.
  * count must equal the current particle count.  A NULL input skips that upload, a NULL output
- * that download; in and out may be the same buffer.  For one fluids or boids step on pinned host memory
- * (cudaHostAlloc, cudaHostRegister) the step's first kernel reads the inputs and its last kernel
- * writes the outputs over the host link directly (no separate copies); otherwise the buffers are
- * copied with cudaMemcpyAsync. */
+ * that download; in and out may be the same buffer.  For one fluids or boids step on pinned
+ * host memory (cudaHostAlloc, cudaHostRegister) the step's first kernel reads the inputs and
+ * its last kernel writes the outputs over the host link directly (no separate copies);
+ * otherwise the buffers are copied with cudaMemcpyAsync. */
 int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t count, uint32_t nsteps, void* posOut,
                     void* velOut);
 
