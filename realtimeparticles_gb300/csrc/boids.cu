@@ -13,7 +13,7 @@
 namespace rtp {
 
 // With io.inPos / io.inVel the state comes from host memory and is mirrored into pos / vel.
-__global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, float4* __restrict__ pos,
+__global__ void __launch_bounds__(kKeyThreads) k_boids_keys(GridK g, float4* __restrict__ pos,
                                                              float4* __restrict__ vel, uint32_t n,
                                                              uint32_t* __restrict__ keys, int bits0,
                                                              uint32_t* __restrict__ hist0, ZeroJob zero,
@@ -29,8 +29,8 @@ __global__ void __launch_bounds__(kSortThreads) k_boids_keys(GridK g, float4* __
   th.init(s_hist, bits0);
   const uint32_t base = blockIdx.x * kSortTile;
 #pragma unroll 2
-  for (int k = 0; k < kSortItems; ++k) {
-    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+  for (int k = 0; k < kKeyItems; ++k) {
+    const uint32_t i = base + k * kKeyThreads + threadIdx.x;
     if (i < n) {
       float4 x;
       if (io.inPos) {
@@ -194,7 +194,7 @@ static int check(const char* what) {
 int boids_presort(const GridK& g, float4* pos, float4* vel, uint32_t n, uint32_t* keys, const SortPlan& plan,
                   uint32_t* hist0, Launcher& L, const ZeroJob& zero, const TargetK& tk, const HostIO& io) {
   L.begin("bd_keys");
-  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kSortThreads), g, pos, vel, n, keys, plan.bits[0], hist0, zero, tk.track,
+  launch(L, k_boids_keys, dim3(plan.tiles), dim3(kKeyThreads), g, pos, vel, n, keys, plan.bits[0], hist0, zero, tk.track,
          io);
   L.end("bd_keys");
   return check("k_boids_keys");

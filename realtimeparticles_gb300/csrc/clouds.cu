@@ -187,7 +187,7 @@ __device__ __forceinline__ float4 mixed_bc(const GridK& g, float4 np) {
   return r;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_cloud_thermo_predict(
+__global__ void __launch_bounds__(kKeyThreads) k_cloud_thermo_predict(
     GridK g, CloudK c, const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
     float* __restrict__ temp, float* __restrict__ vapor, float* __restrict__ cloud, float* __restrict__ buoy,
     float4* __restrict__ pred, float4* __restrict__ tot, uint32_t* __restrict__ keys, int bits0,
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(kSortThreads) k_cloud_thermo_predict(
   th.init(s_hist, bits0);
   const float dt = c.dt;
   const uint32_t base = blockIdx.x * kSortTile;
-  for (int k = 0; k < kSortItems; ++k) {
-    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+  for (int k = 0; k < kKeyItems; ++k) {
+    const uint32_t i = base + k * kKeyThreads + threadIdx.x;
     if (i >= n) continue;
     const float4 p = ld4(pos + i), v = ld4(vel + i);
     const float tIn = temp[i];
@@ -560,7 +560,7 @@ int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const floa
                   float* vapor, float* cloud, float* buoy, float4* pred, float4* tot, uint32_t* keys,
                   const SortPlan& plan, uint32_t* hist0, Launcher& L, const ZeroJob& zero) {
   L.begin("cld_thermo_predict");
-  launch(L, k_cloud_thermo_predict, dim3(plan.tiles), dim3(kSortThreads), g, c, pos, vel, n, temp, vapor, cloud, buoy, pred,
+  launch(L, k_cloud_thermo_predict, dim3(plan.tiles), dim3(kKeyThreads), g, c, pos, vel, n, temp, vapor, cloud, buoy, pred,
                                                                     tot, keys, plan.bits[0], hist0, zero);
   L.end("cld_thermo_predict");
   return check("k_cloud_thermo_predict");

@@ -27,7 +27,7 @@ namespace rtp {
 // Round-to-nearest intrinsics make predPos, and so the cell keys, bit-identical to the CPU.
 // With io.inPos / io.inVel the inputs come from host memory and are mirrored into pos / vel.
 template <bool BATCH>
-__global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK p0, float4* __restrict__ pos,
+__global__ void __launch_bounds__(kKeyThreads) k_fluid_predict(GridK g0, FluidK p0, float4* __restrict__ pos,
                                                                 float4* __restrict__ vel, uint32_t n,
                                                                 float4* __restrict__ pred, uint32_t* __restrict__ keys,
                                                                 int bits0, uint32_t* __restrict__ hist0, int clampOut,
@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(kSortThreads) k_fluid_predict(GridK g0, FluidK
   const float gx = __fmul_rn(0.0f, dt), gy = __fmul_rn(-kAbsGravityY, dt);
   const uint32_t base = blockIdx.x * kSortTile;
 #pragma unroll 2
-  for (int k = 0; k < kSortItems; ++k) {
-    const uint32_t i = base + k * kSortThreads + threadIdx.x;
+  for (int k = 0; k < kKeyItems; ++k) {
+    const uint32_t i = base + k * kKeyThreads + threadIdx.x;
     if (i < n) {
       GridK g = g0;
       FluidK p = p0;
@@ -432,10 +432,10 @@ int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uin
                   const HostIO& io) {
   L.begin("fld_predict");
   if (p.bt.scenes)
-    launch(L, k_fluid_predict<true>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
+    launch(L, k_fluid_predict<true>, dim3(plan.tiles), dim3(kKeyThreads), g, p, pos, vel, n, pred, keys, plan.bits[0], hist0,
                                                                      clampOut ? 1 : 0, zero, io);
   else
-    launch(L, k_fluid_predict<false>, dim3(plan.tiles), dim3(kSortThreads), g, p, pos, vel, n, pred, keys, plan.bits[0],
+    launch(L, k_fluid_predict<false>, dim3(plan.tiles), dim3(kKeyThreads), g, p, pos, vel, n, pred, keys, plan.bits[0],
                                                                       hist0, clampOut ? 1 : 0, zero, io);
   L.end("fld_predict");
   return check("k_fluid_predict");

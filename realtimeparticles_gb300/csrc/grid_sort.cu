@@ -37,6 +37,10 @@ SortPlan make_sort_plan(uint32_t n, uint32_t keyBits) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Up to this many tiles the scatter passes run 16-warp blocks (measured: faster over few
+// tiles, slower at millions of keys where the larger shared footprint limits residency).
+constexpr uint32_t kWidePassTiles = 256;
+
 // Tile groups of the two-kernel digit scan (1 = the single-kernel scan).
 static uint32_t scan_groups(uint32_t tiles) {
   return std::min<uint32_t>(kScanGroupsMax, (tiles + kScanTilesPerGroup - 1) / kScanTilesPerGroup);
@@ -76,7 +80,7 @@ __global__ void k_fill_cell_ids(GridK g, const float4* __restrict__ pos, uint32_
 }
 
 // Per-tile histogram of the digit at `shift` (pass 0 of externally supplied keys).
-__global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+__global__ void __launch_bounds__(kKeyThreads) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
                                                             int bits, uint32_t* __restrict__ hist) {
   pdl_enter();
   __shared__ uint32_t s_hist[kMaxBins];
@@ -84,8 +88,8 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_hist(const uint32_t* __re
   th.init(s_hist, bits);
   const uint32_t base = blockIdx.x * kSortTile;
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    const uint32_t e = base + k * kSortThreads + threadIdx.x;
+  for (int k = 0; k < kKeyItems; ++k) {
+    const uint32_t e = base + k * kKeyThreads + threadIdx.x;
     if (e < n) th.add(__ldg(keys + e) >> shift);
   }
   th.store(hist);
@@ -208,8 +212,9 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-// Exclusive scan of a[2 t], a[2 t + 1] over the block (kSortThreads threads, 2 values per
-// thread): returns the prefixes of both values; s_wsum holds kSortWarps words of scratch.
+// Exclusive scan of a[2 t], a[2 t + 1] over the block (WARPS warps, 2 values per thread):
+// returns the prefixes of both values; s_wsum holds WARPS words of scratch.
+template <int WARPS>
 __device__ __forceinline__ void block_scan2(uint32_t v0, uint32_t v1, uint32_t* s_wsum, uint32_t& e0, uint32_t& e1) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v0 + v1;
@@ -222,7 +227,7 @@ __device__ __forceinline__ void block_scan2(uint32_t v0, uint32_t v1, uint32_t* 
   __syncthreads();
   uint32_t wpre = 0;
 #pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) wpre += (w < warp) ? s_wsum[w] : 0u;
+  for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? s_wsum[w] : 0u;
   e0 = wpre + x - (v0 + v1);
   e1 = e0 + v0;
   __syncthreads();  // s_wsum may be reused
@@ -232,17 +237,20 @@ __device__ __forceinline__ void block_scan2(uint32_t v0, uint32_t v1, uint32_t* 
 // prefix over tiles per digit (k_sort_scan); totals the per-digit totals.
 // The tile's keys are ranked stably (warp w owns a contiguous chunk, items in index order),
 // placed in shared memory in tile-local digit order, and written out from there, so that
-// consecutive threads write consecutive addresses of each digit's run.
-template <bool LAST>
-__global__ void __launch_bounds__(kSortThreads) k_sort_pass(
+// consecutive threads write consecutive addresses of each digit's run.  WARPS warps per
+// block, kSortTile / (32 WARPS) keys per lane: 16 warps at small tile counts (more threads
+// in flight over few tiles), 8 at large ones (smaller shared-memory footprint).
+template <bool LAST, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ idx_in, uint32_t n, int shift, int bits,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ idx_out, uint32_t* __restrict__ hist_next, int next_shift, int next_bits, GatherList g) {
   pdl_enter();
+  constexpr int ITEMS = kSortTile / (32 * WARPS), THREADS = 32 * WARPS;
   __shared__ uint32_t s_base[kMaxBins];    // global start of (this tile, digit)
   __shared__ uint32_t s_lstart[kMaxBins];  // tile-local start of each digit
-  __shared__ uint32_t s_wc[kSortWarps][kMaxBins];
-  __shared__ uint32_t s_wsum[kSortWarps];
+  __shared__ uint32_t s_wc[WARPS][kMaxBins];
+  __shared__ uint32_t s_wsum[WARPS];
   __shared__ uint32_t s_key[kSortTile];
   __shared__ uint32_t s_src[kSortTile];
   const int bins = 1 << bits;
@@ -256,20 +264,20 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     const uint32_t v0 = d0 < bins ? __ldg(totals + d0) : 0u;
     const uint32_t v1 = d1 < bins ? __ldg(totals + d1) : 0u;
     uint32_t e0, e1;
-    block_scan2(v0, v1, s_wsum, e0, e1);
+    block_scan2<WARPS>(v0, v1, s_wsum, e0, e1);
     const uint32_t* tp = hist + (size_t)tile * kMaxBins;
     if (d0 < bins) s_base[d0] = e0 + __ldg(tp + d0);
     if (d1 < bins) s_base[d1] = e1 + __ldg(tp + d1);
   }
-  for (int i = tid; i < kSortWarps * bins; i += kSortThreads) s_wc[i / bins][i % bins] = 0;
+  for (int i = tid; i < WARPS * bins; i += THREADS) s_wc[i / bins][i % bins] = 0;
   __syncthreads();
 
   // Stable rank within the warp's contiguous chunk, items in index order.
-  const uint32_t wbase = tile * kSortTile + warp * (32 * kSortItems);
+  const uint32_t wbase = tile * kSortTile + warp * (32 * ITEMS);
   const uint32_t ltmask = lanemask_lt();
-  uint32_t key[kSortItems], dig[kSortItems], rank[kSortItems];
+  uint32_t key[ITEMS], dig[ITEMS], rank[ITEMS];
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     const uint32_t e = wbase + k * 32 + lane;
     const bool valid = e < n;
     key[k] = valid ? __ldg(keys_in + e) : 0u;
@@ -293,7 +301,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
       if (d < bins) {
         uint32_t run = 0;
 #pragma unroll
-        for (int w = 0; w < kSortWarps; ++w) {
+        for (int w = 0; w < WARPS; ++w) {
           const uint32_t t = s_wc[w][d];
           s_wc[w][d] = run;
           run += t;
@@ -302,14 +310,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
       }
     }
     uint32_t e0, e1;
-    block_scan2(c[0], c[1], s_wsum, e0, e1);
+    block_scan2<WARPS>(c[0], c[1], s_wsum, e0, e1);
     if (2 * tid < bins) s_lstart[2 * tid] = e0;
     if (2 * tid + 1 < bins) s_lstart[2 * tid + 1] = e1;
   }
   __syncthreads();
   // Place each key (and its source index) at its tile-local sorted slot.
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     const uint32_t e = wbase + k * 32 + lane;
     if (e < n) {
       const uint32_t d = dig[k];
@@ -323,8 +331,8 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
   const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
   const uint32_t nmask = (1u << next_bits) - 1u;
 #pragma unroll 2
-  for (int it = 0; it < kSortItems; ++it) {
-    const uint32_t j = it * kSortThreads + tid;
+  for (int it = 0; it < ITEMS; ++it) {
+    const uint32_t j = it * THREADS + tid;
     const bool valid = j < count;
     uint32_t kk = 0, pos = 0;
     if (valid) {
@@ -401,7 +409,7 @@ int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t
 
 int launch_sort_histogram(const SortPlan& p, const uint32_t* keys, const SortScratch& s, Launcher& L) {
   L.begin("sort_hist0");
-  launch(L, k_sort_hist, dim3(p.tiles), dim3(kSortThreads), keys, p.n, 0, p.bits[0], s.hist);
+  launch(L, k_sort_hist, dim3(p.tiles), dim3(kKeyThreads), keys, p.n, 0, p.bits[0], s.hist);
   L.end("sort_hist0");
   return check_launch("k_sort_hist");
 }
@@ -439,6 +447,7 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
     uint32_t* totals = s.totals + (size_t)kMaxBins * pass;
     const int bins = 1 << p.bits[pass];
     const uint32_t groups = scan_groups(p.tiles);
+    const bool wide = p.tiles <= kWidePassTiles;
     L.begin("sort_scan");
     if (groups <= 1) {
       launch(L, k_sort_scan, dim3((bins + 31) / 32), dim3(256), hist, p.tiles, bins, totals);
@@ -455,14 +464,21 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
     if (!last && kout == kin) kout = (kout == s.keysA) ? s.keysB : s.keysA;
     if (last) {
       L.begin("sort_pass_gather");
-      launch(L, k_sort_pass<true>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
-                                                                totals, kout, nullptr, nullptr, 0, 1, g);
+      if (wide)
+        launch(L, k_sort_pass<true, 16>, dim3(p.tiles), dim3(512), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+               totals, kout, nullptr, nullptr, 0, 1, g);
+      else
+        launch(L, k_sort_pass<true, kSortWarps>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass],
+               p.bits[pass], hist, totals, kout, nullptr, nullptr, 0, 1, g);
       L.end("sort_pass_gather");
     } else {
       L.begin("sort_pass");
-      launch(L, k_sort_pass<false>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
-                                                                 totals, kout, iout, hist + per, p.shift[pass + 1],
-                                                                 p.bits[pass + 1], g);
+      if (wide)
+        launch(L, k_sort_pass<false, 16>, dim3(p.tiles), dim3(512), kin, iin, p.n, p.shift[pass], p.bits[pass], hist,
+               totals, kout, iout, hist + per, p.shift[pass + 1], p.bits[pass + 1], g);
+      else
+        launch(L, k_sort_pass<false, kSortWarps>, dim3(p.tiles), dim3(kSortThreads), kin, iin, p.n, p.shift[pass],
+               p.bits[pass], hist, totals, kout, iout, hist + per, p.shift[pass + 1], p.bits[pass + 1], g);
       L.end("sort_pass");
     }
     rc = check_launch("k_sort_pass");

@@ -10,10 +10,12 @@ namespace rtp {
 
 constexpr float kFloatEps = 0.00000001f;   // FLOAT_EPS, kernels/define.cl:6
 constexpr float kAbsGravityY = 9.81f;      // ABS_GRAVITY_ACC_Y, kernels/define.cl:8
-constexpr int kSortWarps = 8;              // warps per sort tile
-constexpr int kSortItems = 8;              // keys per lane per sort tile
+constexpr int kSortTile = 2048;            // keys per sort tile
+constexpr int kSortWarps = 8;              // warps of a scatter-pass block at large tile counts
+constexpr int kSortItems = kSortTile / (32 * kSortWarps);  // keys per lane
 constexpr int kSortThreads = kSortWarps * 32;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per tile
+constexpr int kKeyThreads = 512;           // threads of the key-producing kernels (one tile each)
+constexpr int kKeyItems = kSortTile / kKeyThreads;
 constexpr int kMaxRadixBits = 9;
 constexpr int kMaxBins = 1 << kMaxRadixBits;
 
@@ -183,8 +185,8 @@ struct HostIO {
 };
 
 // Sort-tile histogram of digit 0, for the kernels that produce the keys.  The calling
-// block has kSortThreads threads and handles tile blockIdx.x: element
-// blockIdx.x * kSortTile + k * kSortThreads + threadIdx.x for k < kSortItems.
+// block has kKeyThreads threads and handles tile blockIdx.x: element
+// blockIdx.x * kSortTile + k * kKeyThreads + threadIdx.x for k < kKeyItems.
 struct TileHistogram {
   uint32_t* s;
   int mask;
