@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kKeyThreads) k_fluid_predict(GridK g0, FluidK 
 // 27 cells writes the pairs within h to the device list (kept for k_fluid_deltap), then
 // the SPH terms are summed over that list.
 template <bool BATCH>
-__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
                                                                 float* __restrict__ density, PairList pl,
@@ -208,7 +208,7 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
 // GUARD also evaluates fld_computeDensity at those positions and writes each block's sum
 // of |rho_i / rho0 - 1| to errPartial[blockIdx.x] (warm-start guard, solver statistics).
 template <bool GUARD, bool BATCH>
-__global__ void __launch_bounds__(kSweepThreads, 16) k_fluid_vorticity(GridK g, FluidK p, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vorticity(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                     const float4* __restrict__ velS,
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float4* __restrict__ vort, PairList pl,
