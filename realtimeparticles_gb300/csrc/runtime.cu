@@ -165,10 +165,17 @@ struct Handle {
   bool graphProfiled = false;
   // A fluids or boids step over host-resident state (rtp_update_host with pinned buffers): the
   // same step captured with the host pointers it reads and writes (io, set while capturing).
+  // A few captures are kept (least recently used replaced), so alternating buffer pairs do
+  // not recapture on every call.
   HostIO io{};
-  cudaGraphExec_t graphHost = nullptr;
-  bool graphHostValid = false;
-  HostIO graphHostIO{};
+  struct HostGraph {
+    HostIO io{};
+    cudaGraphExec_t exec = nullptr;
+    bool valid = false;
+    uint64_t used = 0;
+  };
+  HostGraph hostGraphs[4];
+  uint64_t hostGraphClock = 0;
 
   // Profiling.
   bool profiling = false;
@@ -343,7 +350,8 @@ static int alloc_buffers(Handle* h) {
 static void free_handle(Handle* h) {
   if (!h) return;
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  if (h->graphHost) cudaGraphExecDestroy(h->graphHost);
+  for (auto& hg : h->hostGraphs)
+    if (hg.exec) cudaGraphExecDestroy(hg.exec);
   for (void* p : h->allocs) cudaFree(p);
   if (h->ground) cudaFree(h->ground);
   if (h->flush) cudaFree(h->flush);
@@ -391,7 +399,7 @@ static int ws_forget(Handle* h) {
 
 static void invalidate(Handle* h) {
   h->graphValid = false;
-  h->graphHostValid = false;
+  for (auto& hg : h->hostGraphs) hg.valid = false;
 }
 
 // ---- one model step (the update() sequences) ------------------------------------------
@@ -1026,31 +1034,51 @@ static int build_graph(Handle* h) {
   return RTP_OK;
 }
 
-// The step capturing host I/O `io` (no profiling events) into graphHost.
-static int build_host_graph(Handle* h, const HostIO& io) {
-  if (h->graphHost) {
-    cudaGraphExecDestroy(h->graphHost);
-    h->graphHost = nullptr;
+static bool same_io(const HostIO& a, const HostIO& b) {
+  return a.inPos == b.inPos && a.inVel == b.inVel && a.outPos == b.outPos && a.outVel == b.outVel;
+}
+
+// The step capturing host I/O `io` (no profiling events): a kept capture, or a new one in the
+// least recently used slot.
+static int host_graph(Handle* h, const HostIO& io, cudaGraphExec_t* out) {
+  Handle::HostGraph* slot = nullptr;
+  for (auto& hg : h->hostGraphs)
+    if (hg.valid && same_io(hg.io, io)) slot = &hg;
+  if (!slot) {
+    slot = &h->hostGraphs[0];
+    for (auto& hg : h->hostGraphs) {
+      if (!hg.valid) {
+        slot = &hg;
+        break;
+      }
+      if (hg.used < slot->used) slot = &hg;
+    }
+    if (slot->exec) {
+      cudaGraphExecDestroy(slot->exec);
+      slot->exec = nullptr;
+    }
+    slot->valid = false;
+    Launcher L;
+    L.stream = h->stream;
+    h->io = io;
+    RTP_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = record_step(h, L);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &graph);
+    h->io = HostIO{};
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+    const cudaError_t ei = cudaGraphInstantiate(&slot->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate");
+    slot->io = io;
+    slot->valid = true;
   }
-  h->graphHostValid = false;
-  Launcher L;
-  L.stream = h->stream;
-  h->io = io;
-  RTP_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  const int rc = record_step(h, L);
-  cudaGraph_t graph = nullptr;
-  const cudaError_t ec = cudaStreamEndCapture(h->stream, &graph);
-  h->io = HostIO{};
-  if (rc) {
-    if (graph) cudaGraphDestroy(graph);
-    return rc;
-  }
-  if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
-  const cudaError_t ei = cudaGraphInstantiate(&h->graphHost, graph, 0);
-  cudaGraphDestroy(graph);
-  if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate");
-  h->graphHostValid = true;
-  h->graphHostIO = io;
+  slot->used = ++h->hostGraphClock;
+  *out = slot->exec;
   return RTP_OK;
 }
 
@@ -1569,13 +1597,11 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
       io.inVel = (const float4*)iv;
       io.outPos = (float4*)op;
       io.outVel = (float4*)ov;
-      const HostIO& k = h->graphHostIO;
-      if (!h->graphHostValid || k.inPos != io.inPos || k.inVel != io.inVel || k.outPos != io.outPos ||
-          k.outVel != io.outVel)
-        RTP_TRY(build_host_graph(h, io));
+      cudaGraphExec_t exec = nullptr;
+      RTP_TRY(host_graph(h, io, &exec));
       if (posIn) RTP_TRY(ws_forget(h));
       if (target_on(h)) RTP_TRY(feed_target(h, 1));
-      RTP_CUDA(cudaGraphLaunch(h->graphHost, h->stream));
+      RTP_CUDA(cudaGraphLaunch(exec, h->stream));
       h->hasStep = true;
       RTP_CUDA(cudaStreamSynchronize(h->stream));
       return RTP_OK;

@@ -159,6 +159,14 @@ def test_update_host_pinned_buffers():
         ref.updateHost(rp, rv, 2)
         assert np.array_equal(fp2, rp) and np.array_equal(fv2, rv)
         assert np.array_equal(fast.download(abi.BUF_POS), rp)  # the device state follows
+        # Ping-pong between two pinned buffer pairs (kept captures are reused).
+        qa = (pinned(fp2), pinned(fv2))
+        qb = (pinned(np.zeros_like(fp2)), pinned(np.zeros_like(fv2)))
+        for k in range(4):
+            src, dst = (qa, qb) if k % 2 == 0 else (qb, qa)
+            call("rtp_update_host", fast.handle, P(src[0]), P(src[1]), n, 1, P(dst[0]), P(dst[1]))
+            ref.updateHost(rp, rv, 1)
+            assert np.array_equal(dst[0], rp) and np.array_equal(dst[1], rv)
 
 
 def test_update_host_pinned_boids_with_target():
