@@ -251,8 +251,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
   __shared__ uint32_t s_lstart[kMaxBins];  // tile-local start of each digit
   __shared__ uint32_t s_wc[WARPS][kMaxBins];
   __shared__ uint32_t s_wsum[WARPS];
-  __shared__ uint32_t s_key[kSortTile];
-  __shared__ uint32_t s_src[kSortTile];
+  __shared__ uint2 s_ks[kSortTile];  // (key, source index) in tile-local sorted order
   const int bins = 1 << bits;
   const uint32_t mask = (uint32_t)(bins - 1);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -311,8 +310,15 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
     }
     uint32_t e0, e1;
     block_scan2<WARPS>(c[0], c[1], s_wsum, e0, e1);
-    if (2 * tid < bins) s_lstart[2 * tid] = e0;
-    if (2 * tid + 1 < bins) s_lstart[2 * tid + 1] = e1;
+    // s_base becomes the output offset of tile-local slot 0 for each digit.
+    if (2 * tid < bins) {
+      s_lstart[2 * tid] = e0;
+      s_base[2 * tid] -= e0;
+    }
+    if (2 * tid + 1 < bins) {
+      s_lstart[2 * tid + 1] = e1;
+      s_base[2 * tid + 1] -= e1;
+    }
   }
   __syncthreads();
   // Place each key (and its source index) at its tile-local sorted slot.
@@ -322,8 +328,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
     if (e < n) {
       const uint32_t d = dig[k];
       const uint32_t lp = s_lstart[d] + s_wc[warp][d] + rank[k];
-      s_key[lp] = key[k];
-      s_src[lp] = idx_in ? __ldg(idx_in + e) : e;
+      s_ks[lp] = make_uint2(key[k], idx_in ? __ldg(idx_in + e) : e);
     }
   }
   __syncthreads();
@@ -334,18 +339,18 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
   for (int it = 0; it < ITEMS; ++it) {
     const uint32_t j = it * THREADS + tid;
     const bool valid = j < count;
-    uint32_t kk = 0, pos = 0;
+    uint32_t kk = 0, pos = 0, src = 0;
     if (valid) {
-      kk = s_key[j];
-      const uint32_t d = (kk >> shift) & mask;
-      pos = s_base[d] + (j - s_lstart[d]);
+      const uint2 ks = s_ks[j];
+      kk = ks.x;
+      src = ks.y;
+      pos = s_base[(kk >> shift) & mask] + j;  // wraps back into [0, n) for a consistent histogram
     }
     // A consistent histogram gives pos < n; the guard keeps an inconsistent one (a bug)
     // from writing out of bounds: the element is dropped and the parity tests fail.
     const bool ok = valid && pos < n;
     if (ok) {
       keys_out[pos] = kk;
-      const uint32_t src = s_src[j];
       if (!LAST) {
         idx_out[pos] = src;
       } else {
