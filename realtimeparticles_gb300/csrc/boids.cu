@@ -100,10 +100,17 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
       }
     }
   } else {
-    // bd_applyBoidsRulesWithGrid3D (boids.cl:78-113): 27 cells, no wrap.  A row's z cells
-    // are read from the table together and visited as one range where contiguous, four
-    // position loads in flight; velocities are loaded for the boids inside the radius.
-    auto test = [&](uint32_t j, float4 xj) {
+    // bd_applyBoidsRulesWithGrid3D (boids.cl:78-113): 27 cells, no wrap.  Two phases: the
+    // row ranges (a row's z cells joined where contiguous, four position loads in flight)
+    // are filtered into a per-thread list of the boids inside the radius, then the rules are
+    // summed over that list in the same order, so the lanes of a warp do not all pay for the
+    // neighbour body whenever one of them has a neighbour.  More than kBoidHits neighbours:
+    // the sums run inline over the rows instead.
+    constexpr int kBoidHits = 32;
+    uint32_t hits[kBoidHits];
+    int nh = 0;
+    bool inline_sums = false;
+    auto add = [&](uint32_t j, float4 xj) {
       const float4 v = xi - xj;
       const float sq = dot4(v, v);
       if (sq < g.boidsR2 && sq > kFloatEps) {
@@ -113,36 +120,56 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
         ++count;
       }
     };
+    auto filt = [&](uint32_t j, float4 xj) {
+      const float4 v = xi - xj;
+      const float sq = dot4(v, v);
+      if (sq < g.boidsR2 && sq > kFloatEps) {
+        if (nh < kBoidHits) hits[nh] = j;
+        ++nh;
+      }
+    };
     auto ldp = [&](uint32_t j) { return ld4(posS + j); };
+    auto rows = [&](auto&& test) {
 #pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-      const int nx = cx + dx;
-      if (nx < 0 || nx >= g.R[0]) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int nx = cx + dx;
+        if (nx < 0 || nx >= g.R[0]) continue;
 #pragma unroll 1
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int ny = cy + dy;
-        if (ny < 0 || ny >= g.R[1]) continue;
-        const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
-        uint32_t cb = 0, ce = 0;
+        for (int dy = -1; dy <= 1; ++dy) {
+          const int ny = cy + dy;
+          if (ny < 0 || ny >= g.R[1]) continue;
+          const uint32_t row = ((uint32_t)nx * g.R[1] + (uint32_t)ny) * g.R[2];
+          uint32_t cb = 0, ce = 0;
 #pragma unroll
-        for (int dz = -1; dz <= 1; ++dz) {
-          const int nz = cz + dz;
-          if (nz < 0 || nz >= g.R[2]) continue;
-          uint32_t j0, j1;
-          cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
-          if (j0 == j1) continue;
-          if (cb == ce) {
-            cb = j0;
-            ce = j1;
-          } else if (ce == j0) {
-            ce = j1;
-          } else {
-            visit_range_x4(cb, ce, ldp, test);
-            cb = j0;
-            ce = j1;
+          for (int dz = -1; dz <= 1; ++dz) {
+            const int nz = cz + dz;
+            if (nz < 0 || nz >= g.R[2]) continue;
+            uint32_t j0, j1;
+            cell_range(table, row + (uint32_t)nz, g.cap, j0, j1);
+            if (j0 == j1) continue;
+            if (cb == ce) {
+              cb = j0;
+              ce = j1;
+            } else if (ce == j0) {
+              ce = j1;
+            } else {
+              visit_range_x4(cb, ce, ldp, test);
+              cb = j0;
+              ce = j1;
+            }
           }
+          if (cb != ce) visit_range_x4(cb, ce, ldp, test);
         }
-        if (cb != ce) visit_range_x4(cb, ce, ldp, test);
+      }
+    };
+    rows(filt);
+    inline_sums = nh > kBoidHits;
+    if (inline_sums) {
+      rows(add);
+    } else {
+      for (int k = 0; k < nh; ++k) {
+        const uint32_t j = hits[k];
+        add(j, ld4(posS + j));
       }
     }
   }
