@@ -32,7 +32,9 @@ Metric: particle-steps/s.
   interpolated (log-log) at its error.
 * --impl reference: that CPU implementation alone (rank 0), same metric and config.
 Under torchrun (N > 1) each rank runs an independent replica of the workload on its
-own GPU (one scene does not shard): barrier + max-over-ranks timing.
+own GPU (one scene does not shard; a batch shards by scene: rank r steps its own seeded
+scene set, seed + r): barrier + max-over-ranks timing, value = the particles of all ranks
+over that time.
 """
 import argparse
 import ctypes as C
@@ -76,11 +78,12 @@ WORKLOADS = {
 }
 
 
-def make_model(w):
-    """The model of workload w with its seeded inputs uploaded."""
+def make_model(w, rank=0):
+    """The model of workload w with its seeded inputs uploaded.  A batch shards by scene:
+    rank r steps its own seeded scene set (seed + r)."""
     from realtimeparticles_gb300 import model
     if w["kind"] == "batch":
-        sc = scenes.batched_dam_breaks(count=w["count"], seed=w["seed"])
+        sc = scenes.batched_dam_breaks(count=w["count"], seed=w["seed"] + rank)
         m = model.FluidsBatch(sc["scenes"], sc["h"])
         m.setFluidParams(sc["fluid_params"])
         m.setJacobiIterations(w["iters"])
@@ -218,6 +221,18 @@ def max_over_ranks(value, ws):
     dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
     t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value, ws):
+    """Sum of a count over all ranks (identity for one rank)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
@@ -485,7 +500,8 @@ def run_ours(args):
     w = WORKLOADS[args.workload]
     if "max_steps" in w:
         args.steps = min(args.steps, w["max_steps"])
-    m, n = make_model(w)
+    m, n = make_model(w, rank)
+    n_all = sum_over_ranks(n, ws)  # a batch's ranks hold different scene sets
     tune = None
     if w["kind"] in ("batch", "fluids"):
         best, cands = m.autotune(steps=5)
@@ -504,7 +520,7 @@ def run_ours(args):
     barrier(ws)
     clk = clocks.stop()
     ms = max_over_ranks(ms, ws)
-    value = n * args.steps * ws / (ms / 1000.0)
+    value = n_all * args.steps / (ms / 1000.0)
 
     # Per-kernel times from captured events inside the same kind of graph replays.
     m.enableProfiling(True)
@@ -556,7 +572,7 @@ def run_ours(args):
     t_e2e = time.perf_counter() - t0
     barrier(ws)
     t_e2e = max_over_ranks(t_e2e, ws)
-    e2e = n * args.steps * ws / t_e2e
+    e2e = n_all * args.steps / t_e2e
     metrics = m.metrics() if w["kind"] != "boids" else None
     batch = batch_study(m, w, args.steps, max(3, args.warmup)) if w["kind"] == "batch" and rank == 0 else None
     m.close()
@@ -571,7 +587,8 @@ def run_ours(args):
             "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": args.workload, "particles": n, "jacobi_iterations": w.get("iters"),
                        "l2": "flushed before every timed step (256 MiB write)",
-                       "parallelism": "replicas" if ws > 1 else "single"},
+                       "parallelism": ("scenes by rank" if w["kind"] == "batch" else "replicas") if ws > 1
+                       else "single"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": 2 * 16 * n,
                     "d2h_bytes_per_step": 2 * 16 * n, "pinned_host": pinned},
             "gpu_launches": int(round(launches_per_step * args.steps)),
