@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
 // LAST adds fld_updateVel (fluids.cl:263-273).  LANES lanes per particle.  Input positions
 // are already clamped by fld_applyBoundaryCondition (done by their producer).
 template <bool LAST, bool BATCH, int LANES>
-__global__ void __launch_bounds__(128) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
+__global__ void __launch_bounds__(128, BATCH ? 1 : 12) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut,
                                                       const float4* __restrict__ posS, float4* __restrict__ velS,
