@@ -404,6 +404,19 @@ static int check_launch(const char* what) {
   return RTP_OK;
 }
 
+// resetCellIDs (grid.cl:65-71): a key above every cell for each slot; the slots a step does not
+// fill keep theirs, so they stay at the tail of the sorted keys in slot order.
+__global__ void k_reset_cell_ids(uint32_t* __restrict__ keys, uint32_t n, uint32_t base) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keys[i] = base + i;
+}
+
+int launch_reset_cell_ids(uint32_t* keys, uint32_t n, uint32_t numCells, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_reset_cell_ids, dim3((n + 255) / 256), dim3(256), keys, n, 2u * numCells);
+  return check_launch("k_reset_cell_ids");
+}
+
 int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L) {
   if (n == 0) return RTP_OK;
   L.begin("fillCellIDs");

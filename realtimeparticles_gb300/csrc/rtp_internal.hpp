@@ -110,5 +110,7 @@ ZeroJob step_zero_job(const SortPlan& p, const SortScratch& s, uint2* table, uin
 // Internal encoding -> the reference's inclusive (start, end) with (1, 0) for empty cells.
 int launch_cell_table_to_reference(const GridK& g, const uint2* table, uint2* out, Launcher& L);
 int launch_fill_cell_ids(const GridK& g, const float4* pos, uint32_t n, uint32_t* keys, Launcher& L);
+// resetCellIDs (grid.cl:65-71): key[i] = 2 * numCells + i for the n slots.
+int launch_reset_cell_ids(uint32_t* keys, uint32_t n, uint32_t numCells, Launcher& L);
 
 }  // namespace rtp

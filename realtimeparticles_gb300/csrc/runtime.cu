@@ -853,6 +853,11 @@ static bool subdiv3(uint64_t n, int out[3]) {
 }
 
 static int init_case(Handle* h) {
+  {  // Fluids.cpp:214, Boids.cpp:271, Clouds.cpp:397: resetCellIDs over maxNb slots.
+    Launcher L;
+    L.stream = h->stream;
+    RTP_TRY(launch_reset_cell_ids(h->cellId, (uint32_t)h->maxN, h->gc.numCells, L));
+  }
   const float bx = h->mp.boxSize[0], by = h->mp.boxSize[1], bz = h->mp.boxSize[2];
   std::vector<V3> verts;
   int res[3];
@@ -1281,6 +1286,11 @@ int rtp_create(int model, const rtp_model_params* params, void** out_handle) {
     return cuda_fail(e, "cudaStreamCreate");
   }
   rc = alloc_buffers(h);
+  if (!rc) {
+    Launcher L;
+    L.stream = h->stream;
+    rc = launch_reset_cell_ids(h->cellId, (uint32_t)h->maxN, h->gc.numCells, L);
+  }
   if (!rc) {
     e = cudaEventCreate(&h->t0);
     if (e == cudaSuccess) e = cudaEventCreate(&h->t1);

@@ -196,3 +196,19 @@ def test_update_host_pinned_boids_with_target():
     for a, b in zip(runs[0][:3], runs[1][:3]):
         assert np.array_equal(a, b)
     assert runs[0][3] == runs[1][3]
+
+
+def test_inactive_slots_keep_sentinel_cell_ids():
+    """resetCellIDs (grid.cl:65-71, run over maxNb at reset): the slots a step does not fill keep
+    2 * numCells + slot and stay at the tail of the sorted keys."""
+    sc = scenes.dam_break(lattice=(8, 16, 16), max_n=5000)
+    n = sc["pos"].shape[0]
+    with model.Fluids(sc["model_params"]) as m:
+        m.setFluidParams(sc["fluid_params"])
+        m.upload(abi.BUF_POS, sc["pos"])
+        m.upload(abi.BUF_VEL, sc["vel"])
+        m.update(2)
+        keys = m.download(abi.BUF_CELL_ID, 5000)
+        nc = m.constants().numCells
+        assert np.all(keys[:n] < nc) and np.all(np.diff(keys[:n].astype(np.int64)) >= 0)
+        assert np.array_equal(keys[n:], 2 * nc + np.arange(n, 5000, dtype=np.uint32))
