@@ -117,6 +117,12 @@ def make_model(w, rank=0):
 
 # Algorithmic bytes per particle of each kernel of the PBF substep (minimal dataflow of
 # the fused kernels: every array a kernel must read or write once).
+# DRAM bytes (read + write) per launch of a workload's dominant kernel from one ncu capture
+# (cold cache, serialised), with the summary that records the capture.
+KERNEL_TRAFFIC = {
+    ("pbf_dam_break_131k", "fld_lambda"): (6455893, "profiles/k_fluid_lambda_131k_traffic.md"),
+}
+
 KERNEL_BYTES = {
     "fld_predict": 16 + 16 + 16 + 4,          # pos, vel in; predPos, key out
     "sort_pass": 4 + 4 + 4,                   # key in; key, index out
@@ -594,7 +600,9 @@ def run_ours(args):
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": None, "algorithmic_bytes_per_launch": alg,
+                         "traffic": KERNEL_TRAFFIC.get((args.workload, dom_name), (None, None))[0],
+                         "traffic_source": KERNEL_TRAFFIC.get((args.workload, dom_name), (None, None))[1],
+                         "algorithmic_bytes_per_launch": alg,
                          "mean_launch_ms": dom_avg_ms},
             "kernel_share": share,
             "clocks": clk,
