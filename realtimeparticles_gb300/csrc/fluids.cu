@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kKeyThreads) k_fluid_predict(GridK g0, FluidK 
 // the pairs within h for k_fluid_deltap.  One thread per particle: a filter pass over the
 // 27 cells writes the pairs within h to the device list (kept for k_fluid_deltap), then
 // the SPH terms are summed over that list.
-template <bool BATCH>
+template <bool BATCH, bool MASK>
 __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
   const float4 xi = ld4(pred + i);
   uint32_t cnt = 0;
   uint32_t* lst = pl.idx + i;
-  filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+  filter_fluid_neighbours_to<MASK>(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
     if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
     ++cnt;
   });
@@ -207,7 +207,7 @@ __global__ void k_fluid_update_vel(GridK g, FluidK p, const float4* __restrict__
 // positions for confinement and XSPH (same two-phase scheme as k_fluid_lambda).
 // GUARD also evaluates fld_computeDensity at those positions and writes each block's sum
 // of |rho_i / rho0 - 1| to errPartial[blockIdx.x] (warm-start guard, solver statistics).
-template <bool GUARD, bool BATCH>
+template <bool GUARD, bool BATCH, bool MASK>
 __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vorticity(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                     const float4* __restrict__ velS,
                                                                     const uint2* __restrict__ table, uint32_t n,
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vortic
     const float4 xi = ld4(pred + i), vi = ld4(velS + i);
     uint32_t cnt = 0;
     uint32_t* lst = pl.idx + i;
-    filter_fluid_neighbours_to(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+    filter_fluid_neighbours_to<MASK>(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
       if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
       ++cnt;
     });
@@ -427,6 +427,10 @@ static int check(const char* what) {
 
 static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
+// From this many particles the full sweeps record hits through a bit mask per eight
+// candidates (measured: 4 % faster at 4.2M, 3 % slower at 131k).
+constexpr uint32_t kMaskFilterParticles = 1u << 20;
+
 int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L, const ZeroJob& zero,
                   const HostIO& io) {
@@ -445,12 +449,16 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
                     float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
                     Launcher& L, float* lamTot, int totMode) {
   L.begin("fld_lambda");
-  if (p.bt.scenes)
-    launch(L, k_fluid_lambda<true>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda,
-                                                                                   density, pl, lamTot, totMode);
+  const dim3 nb(blocks(n, kSweepThreads)), nt(kSweepThreads);
+  const bool mask = n >= kMaskFilterParticles;
+  if (p.bt.scenes && mask)
+    launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+  else if (p.bt.scenes)
+    launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+  else if (mask)
+    launch(L, k_fluid_lambda<false, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
   else
-    launch(L, k_fluid_lambda<false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda,
-                                                                                    density, pl, lamTot, totMode);
+    launch(L, k_fluid_lambda<false, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
   if (rc) return rc;
@@ -490,18 +498,20 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
                     const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L) {
   L.begin("fld_vorticity");
   const uint32_t nb = blocks(n, kSweepThreads);
-  if (p.bt.scenes) {
-    if (errPartial)
-      launch(L, k_fluid_vorticity<true, true>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, errPartial);
-    else
-      launch(L, k_fluid_vorticity<false, true>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, nullptr);
+  auto go = [&](auto GUARD, auto BATCH, auto MASK) {
+    launch(L, k_fluid_vorticity<decltype(GUARD)::value, decltype(BATCH)::value, decltype(MASK)::value>, dim3(nb),
+           dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, errPartial);
+  };
+  using T = std::true_type;
+  using F = std::false_type;
+  const bool mask = n >= kMaskFilterParticles;
+  const bool guard = errPartial != nullptr, batch = p.bt.scenes != nullptr;
+  if (guard) {
+    if (batch) mask ? go(T{}, T{}, T{}) : go(T{}, T{}, F{});
+    else mask ? go(T{}, F{}, T{}) : go(T{}, F{}, F{});
   } else {
-    if (errPartial)
-      launch(L, k_fluid_vorticity<true, false>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl,
-                                                                         errPartial);
-    else
-      launch(L, k_fluid_vorticity<false, false>, dim3(nb), dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl,
-                                                                          nullptr);
+    if (batch) mask ? go(F{}, T{}, T{}) : go(F{}, T{}, F{});
+    else mask ? go(F{}, F{}, T{}) : go(F{}, F{}, F{});
   }
   L.end("fld_vorticity");
   return check("k_fluid_vorticity");

@@ -85,6 +85,36 @@ __device__ __forceinline__ void visit_range_x8(uint32_t b, uint32_t e, G&& g, F&
   visit_range_x4(j, e, g, f);
 }
 
+// Filter of [b, e): hit(loaded) tests a candidate, add(j) records it, in ascending j.  Eight
+// candidates are loaded and tested at a time into a bit mask, then the hits are recorded from
+// the mask, so a warp pays the recording once per hit of its busiest lane rather than once per
+// candidate slot.
+template <class G, class H, class A>
+__device__ __forceinline__ void filter_range_x8(uint32_t b, uint32_t e, G&& g, H&& hit, A&& add) {
+  uint32_t j = b;
+  for (; j + 8 <= e; j += 8) {
+    const auto a0 = g(j), a1 = g(j + 1), a2 = g(j + 2), a3 = g(j + 3);
+    const auto a4 = g(j + 4), a5 = g(j + 5), a6 = g(j + 6), a7 = g(j + 7);
+    uint32_t m = (hit(a0) ? 1u : 0u) | (hit(a1) ? 2u : 0u) | (hit(a2) ? 4u : 0u) | (hit(a3) ? 8u : 0u) |
+                 (hit(a4) ? 16u : 0u) | (hit(a5) ? 32u : 0u) | (hit(a6) ? 64u : 0u) | (hit(a7) ? 128u : 0u);
+    while (m) {
+      add(j + (uint32_t)(__ffs(m) - 1));
+      m &= m - 1u;
+    }
+  }
+  if (j + 4 <= e) {
+    const auto a0 = g(j), a1 = g(j + 1), a2 = g(j + 2), a3 = g(j + 3);
+    uint32_t m = (hit(a0) ? 1u : 0u) | (hit(a1) ? 2u : 0u) | (hit(a2) ? 4u : 0u) | (hit(a3) ? 8u : 0u);
+    while (m) {
+      add(j + (uint32_t)(__ffs(m) - 1));
+      m &= m - 1u;
+    }
+    j += 4;
+  }
+  for (; j < e; ++j)
+    if (hit(g(j))) add(j);
+}
+
 // Walks list entries begin, begin + step, ... < end in order, four at a time: the four
 // indices idx(kk) are loaded, then g(j) loads each pair's operands, then f(j, loaded)
 // consumes them, so a lane keeps several dependent load chains in flight.
@@ -147,13 +177,24 @@ __device__ __forceinline__ void for_each_fluid_neighbour(const GridK& g, const u
 }
 
 // Filter pass over the fluids neighbourhood: calls add(j), in visiting order, for each
-// candidate with |xi - ld(j)|^2 < h2 (ld loads j's position).
-template <class LD, class ADD>
+// candidate with |xi - ld(j)|^2 < h2 (ld loads j's position).  MASK records the hits of
+// each eight candidates from a bit mask (faster with millions of particles, slower at 131k
+// where fewer warps hide the extra loop).
+template <bool MASK = false, class LD, class ADD>
 __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const uint2* __restrict__ table, float4 xi,
                                                            float h2, LD&& ld, ADD&& add) {
-  auto test = [&](uint32_t j, float4 xj) {
+  auto hit = [&](float4 xj) {
     const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
-    if (vx * vx + vy * vy + vz * vz < h2) add(j);
+    return vx * vx + vy * vy + vz * vz < h2;
+  };
+  auto test = [&](uint32_t j, float4 xj) {
+    if (hit(xj)) add(j);
+  };
+  auto range = [&](uint32_t b, uint32_t e) {
+    if constexpr (MASK)
+      filter_range_x8(b, e, ld, hit, add);
+    else
+      visit_range_x8(b, e, ld, test);
   };
   for_each_fluid_row(g, table, xi, [&](uint32_t b0, uint32_t e0, uint32_t b1, uint32_t e1, uint32_t b2, uint32_t e2) {
     uint32_t cb = b0, ce = e0;
@@ -167,12 +208,12 @@ __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const
       } else if (ce == rb[r]) {
         ce = re[r];
       } else {
-        visit_range_x8(cb, ce, ld, test);
+        range(cb, ce);
         cb = rb[r];
         ce = re[r];
       }
     }
-    visit_range_x8(cb, ce, ld, test);
+    range(cb, ce);
   });
 }
 
