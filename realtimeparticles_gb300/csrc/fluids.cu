@@ -129,6 +129,59 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
   else if (totMode == kTotAdd) lamTot[i] += lam;
 }
 
+// k_fluid_lambda with a group of LW lanes per particle (particle counts too small to keep the
+// GPU busy with one lane each): the group filters the 27 cells together (filter_fluid_group)
+// and sums the SPH terms over the list, one entry per lane.
+template <bool BATCH, int LW>
+__global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                            const uint2* __restrict__ table, uint32_t n,
+                                                            float* __restrict__ lambda, float* __restrict__ density,
+                                                            PairList pl, float* __restrict__ lamTot, int totMode) {
+  pdl_enter();
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, q = t % LW;
+  if ((t & ~31u) / LW >= n) return;  // the whole warp is past the last particle
+  const bool live = t / LW < n;
+  const uint32_t i = live ? t / LW : n - 1u;  // a group past the end shadows the last particle
+  scene_of<BATCH>(i, g, p);
+  const Sph k(g);
+  const float4 xi = ld4(pred + i);
+  auto ldp = [&](uint32_t j) { return ld4(pred + j); };
+  uint32_t* lst = pl.idx + i;
+  const uint32_t cnt = filter_fluid_group<LW>(g, table, xi, live, k.h2, ldp, lst, pl.stride, pl.K);
+  float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
+  auto body = [&](uint32_t, float4 xj) {
+    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
+    const float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < k.h2) {
+      rho += k.w(r2);
+      float r;
+      const float s = k.gs(r2, r);
+      const float gxx = vx * s, gyy = vy * s, gzz = vz * s;
+      sgx += gxx;
+      sgy += gyy;
+      sgz += gzz;
+      ssq += gxx * gxx + gyy * gyy + gzz * gzz;
+    }
+  };
+  walk_list_group<LW>(lst, pl.stride, cnt <= pl.K ? cnt : 0u, ldp, body);
+  if (cnt > pl.K && q == 0) for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ldp(j)); });
+  rho = quad_sum<LW>(rho);
+  sgx = quad_sum<LW>(sgx);
+  sgy = quad_sum<LW>(sgy);
+  sgz = quad_sum<LW>(sgz);
+  ssq = quad_sum<LW>(ssq);
+  if (q != 0 || !live) return;
+  pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
+  const float C = rho / p.rho0 - 1.0f;
+  ssq += sgx * sgx + sgy * sgy + sgz * sgz;
+  ssq *= p.invRho0Sq;
+  const float lam = -C / (ssq + p.relaxCFM);
+  lambda[i] = lam;
+  density[i] = rho;
+  if (totMode == kTotWrite) lamTot[i] = lam;
+  else if (totMode == kTotAdd) lamTot[i] += lam;
+}
+
 // fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
 // LAST adds fld_updateVel (fluids.cl:263-273).  LANES lanes per particle.  Input positions
 // are already clamped by fld_applyBoundaryCondition (done by their producer).
@@ -248,6 +301,78 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vortic
     if (GUARD) err = fabsf(rho / p.rho0 - 1.0f);
   }
   if (GUARD) block_error_partial(err, errPartial);
+}
+
+// Threads of a guarded k_fluid_vorticity_group block: 64 particles of LW lanes, at most 1024.
+template <int LW>
+constexpr int kGuardGroupThreads = 64 * LW < 1024 ? 64 * LW : 1024;
+
+// k_fluid_vorticity with a group of LW lanes per particle.  Without GUARD a block is 128
+// threads.  With GUARD a block covers the 64 particles of one errPartial entry (particle
+// blockIdx.x * 64 + r * P + t / LW, P = blockDim.x / LW, for r < 64 / P) and sums their
+// errors in a fixed order; a particle's vorticity is the same either way.
+template <bool GUARD, bool BATCH, int LW>
+__global__ void __launch_bounds__(GUARD ? kGuardGroupThreads<LW> : 128) k_fluid_vorticity_group(
+    GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ velS,
+    const uint2* __restrict__ table, uint32_t n, float4* __restrict__ vort, PairList pl,
+    float* __restrict__ errPartial) {
+  pdl_enter();
+  constexpr uint32_t P = (GUARD ? kGuardGroupThreads<LW> : 128) / LW;  // particles per pass of the block
+  constexpr uint32_t R = GUARD ? 64 / P : 1;
+  static_assert(!GUARD || R * P == 64, "64 particles per guarded block");
+  const uint32_t q = threadIdx.x % LW, slot = threadIdx.x / LW;
+  __shared__ float s_err[GUARD ? 64 : 1];
+  if (GUARD && q == 0)  // each entry is zeroed and later written by the same thread
+    for (uint32_t r = 0; r < R; ++r) s_err[r * P + slot] = 0.0f;
+#pragma unroll 1
+  for (uint32_t r = 0; r < R; ++r) {
+    const uint32_t i0 = GUARD ? blockIdx.x * 64u + r * P : blockIdx.x * P;  // first particle of the pass
+    const uint32_t warpFirst = i0 + (slot & ~(32u / LW - 1u));                   // first of this warp
+    if (warpFirst >= n) break;  // the whole warp is past the last particle
+    const bool live = i0 + slot < n;
+    const uint32_t i = live ? i0 + slot : n - 1u;  // a group past the end shadows the last particle
+    GridK gi = g;
+    FluidK pi = p;
+    scene_of<BATCH>(i, gi, pi);
+    const Sph k(gi);
+    const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+    uint32_t* lst = pl.idx + i;
+    const uint32_t cnt = filter_fluid_group<LW>(gi, table, xi, live, k.h2,
+                                                [&](uint32_t j) { return ld4(pred + j); }, lst, pl.stride, pl.K);
+    float4 w = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    float rho = 0.0f;
+    auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
+    auto body = [&](uint32_t, Pair44 a) {
+      const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        if (GUARD) rho += k.w(r2);
+        float rr;
+        const float s = k.gs(r2, rr);
+        w = w + cross4(a.v - vi, f4(vx * s, vy * s, vz * s, 0.0f));
+      }
+    };
+    walk_list_group<LW>(lst, pl.stride, cnt <= pl.K ? cnt : 0u, ld, body);
+    if (cnt > pl.K && q == 0) for_each_fluid_neighbour(gi, table, xi, [&](uint32_t j) { body(j, ld(j)); });
+    w.x = quad_sum<LW>(w.x);
+    w.y = quad_sum<LW>(w.y);
+    w.z = quad_sum<LW>(w.z);
+    w.w = quad_sum<LW>(w.w);
+    if (GUARD) rho = quad_sum<LW>(rho);
+    if (q == 0 && live) {
+      pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
+      vort[i] = w;
+      if (GUARD) s_err[r * P + slot] = fabsf(rho / pi.rho0 - 1.0f);
+    }
+  }
+  if (GUARD) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float e = 0.0f;
+      for (int u = 0; u < 64; ++u) e += s_err[u];
+      errPartial[blockIdx.x] = e;
+    }
+  }
 }
 
 // fld_applyVorticityConfinement (fluids.cl:329-377), LANES lanes per particle.
@@ -430,6 +555,22 @@ static inline uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; 
 // From this many particles the full sweeps record hits through a bit mask per eight
 // candidates (measured: 4 % faster at 4.2M, 3 % slower at 131k).
 constexpr uint32_t kMaskFilterParticles = 1u << 20;
+// Lanes per particle of the full sweeps (density / lambda and vorticity): a group of lanes
+// (k_fluid_lambda_group, k_fluid_vorticity_group) while the particles are too few to keep
+// the GPU busy one lane each, 0 for the lane-per-particle kernels.  Measured PBF steps (dam
+// break, 3 iterations), us per step for one lane / 2 / 4 / 8 / 16 lanes: 16k 182 / 148 / 125 /
+// 119 / 145; 32k 200 / 172 / 161 / 169 / 220; 65k 252 / 254 / 256 / 273 / 385; 131k 342 /
+// 406 / 420 / 467 / 697.
+static inline int sweep_group_lanes(uint32_t n) {
+  if (n <= 24576u) return 8;
+  if (n <= 49152u) return 4;
+  return 0;
+}
+template <class F>
+static inline void dispatch_group(int lw, F&& f) {
+  if (lw == 8) f(std::integral_constant<int, 8>{});
+  else f(std::integral_constant<int, 4>{});
+}
 
 int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uint32_t n, float4* pred,
                   uint32_t* keys, const SortPlan& plan, uint32_t* hist0, bool clampOut, Launcher& L, const ZeroJob& zero,
@@ -451,7 +592,16 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
   L.begin("fld_lambda");
   const dim3 nb(blocks(n, kSweepThreads)), nt(kSweepThreads);
   const bool mask = n >= kMaskFilterParticles;
-  if (p.bt.scenes && mask)
+  if (const int lw = sweep_group_lanes(n)) {
+    dispatch_group(lw, [&](auto LW) {
+      const dim3 gb(blocks(n, 128 / LW)), gt(128);
+      if (p.bt.scenes)
+        launch(L, k_fluid_lambda_group<true, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+      else
+        launch(L, k_fluid_lambda_group<false, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot,
+               totMode);
+    });
+  } else if (p.bt.scenes && mask)
     launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
   else if (p.bt.scenes)
     launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
@@ -506,7 +656,24 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
   using F = std::false_type;
   const bool mask = n >= kMaskFilterParticles;
   const bool guard = errPartial != nullptr, batch = p.bt.scenes != nullptr;
-  if (guard) {
+  if (const int lw = sweep_group_lanes(n)) {
+    dispatch_group(lw, [&](auto LW) {
+      if (guard) {  // 64 particles per block: one errPartial entry each
+        const dim3 gb(blocks(n, 64)), gt(kGuardGroupThreads<LW>);
+        if (batch)
+          launch(L, k_fluid_vorticity_group<true, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+        else
+          launch(L, k_fluid_vorticity_group<true, false, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+      } else {
+        const dim3 gb(blocks(n, 128 / LW)), gt(128);
+        if (batch)
+          launch(L, k_fluid_vorticity_group<false, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+        else
+          launch(L, k_fluid_vorticity_group<false, false, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl,
+                 errPartial);
+      }
+    });
+  } else if (guard) {
     if (batch) mask ? go(T{}, T{}, T{}) : go(T{}, T{}, F{});
     else mask ? go(T{}, F{}, T{}) : go(T{}, F{}, F{});
   } else {

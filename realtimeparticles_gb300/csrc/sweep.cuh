@@ -217,6 +217,81 @@ __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const
   });
 }
 
+// The filter pass with a group of LW lanes (LW = 4 ... 32, aligned in the warp) on one
+// particle, the warp's 32 / LW groups in lockstep: every group walks the same 9 rows and, per
+// row, as many chunks as the group with the most candidates there needs, so all 32 lanes
+// stay converged (a group whose own candidates are done tests nothing).  Within a row lane q
+// of a group tests candidates q, q + LW, ... of the row's three z cells taken in order, four
+// chunks of LW at a time, and a warp ballot compacts the group's hits into lst[0..K)
+// (stride apart) in visiting order, the list the one-lane pass writes.  Returns the number
+// of pairs within h2 on every lane of the group.  The whole warp must call; a group with
+// live = false (past the last particle) records nothing.  For particle counts too small to
+// keep the GPU busy with one lane each.
+template <int LW, class LD>
+__device__ __forceinline__ uint32_t filter_fluid_group(const GridK& g, const uint2* __restrict__ table, float4 xi,
+                                                       bool live, float h2, LD&& ld, uint32_t* lst, uint32_t stride,
+                                                       uint32_t K) {
+  static_assert(LW >= 2 && LW <= 32 && (LW & (LW - 1)) == 0, "power-of-two group");
+  const uint32_t lane = threadIdx.x & 31u, q = lane & (LW - 1u), first = lane - q;
+  const uint32_t gbits = LW == 32 ? 0xffffffffu : (1u << LW) - 1u;
+  const uint32_t below = (1u << q) - 1u;
+  uint32_t cnt = 0;
+  for_each_fluid_row(g, table, xi, [&](uint32_t b0, uint32_t e0, uint32_t b1, uint32_t e1, uint32_t b2, uint32_t e2) {
+    const uint32_t n0 = e0 - b0, n01 = n0 + (e1 - b1), tot = live ? n01 + (e2 - b2) : 0u;
+    const uint32_t most = __reduce_max_sync(0xffffffffu, tot);
+    for (uint32_t c0 = 0; c0 < most; c0 += 4u * LW) {
+      uint32_t j[4];
+      float4 x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t c = c0 + u * LW + q;
+        j[u] = c < n0 ? b0 + c : (c < n01 ? b1 + (c - n0) : b2 + (c - n01));
+        if (c < tot) x[u] = ld(j[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        bool hit = false;
+        if (c0 + u * LW + q < tot) {
+          const float vx = xi.x - x[u].x, vy = xi.y - x[u].y, vz = xi.z - x[u].z;
+          hit = vx * vx + vy * vy + vz * vz < h2;
+        }
+        const uint32_t m = (__ballot_sync(0xffffffffu, hit) >> first) & gbits;
+        if (hit) {
+          const uint32_t at = cnt + __popc(m & below);
+          if (at < K) lst[(size_t)at * stride] = j[u];
+        }
+        cnt += __popc(m);
+      }
+    }
+  });
+  __syncwarp();  // the entries other lanes of the group wrote are visible to it
+  return cnt;
+}
+
+// The list walk of a lane group in lockstep with the warp's other groups: lane q visits
+// entries q, q + LW, ... of lst[0..cnt) (stride apart), four at a time, for as many rounds as
+// the warp's longest list needs.  The whole warp must call; cnt = 0 visits nothing.
+template <int LW, class G, class F>
+__device__ __forceinline__ void walk_list_group(const uint32_t* lst, uint32_t stride, uint32_t cnt, G&& ld, F&& f) {
+  const uint32_t q = threadIdx.x & (LW - 1u);
+  const uint32_t most = __reduce_max_sync(0xffffffffu, cnt);
+  for (uint32_t k0 = 0; k0 < most; k0 += 4u * LW) {
+    uint32_t j[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t kk = k0 + u * LW + q;
+      j[u] = kk < cnt ? lst[(size_t)kk * stride] : 0u;
+    }
+    decltype(ld(0u)) a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (k0 + u * LW + q < cnt) a[u] = ld(j[u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (k0 + u * LW + q < cnt) f(j[u], a[u]);
+  }
+}
+
 // Visits the pairs recorded for particle i, one in LANES per lane (lane q takes entries
 // q, q + LANES, ...); an overflowed particle searches its 27 cells on lane 0.
 template <int LANES = kQuad, class G, class F>
