@@ -67,6 +67,21 @@ def test_batch_steps_match_the_oracle_per_scene(lanes, factor):
             _compare(m, sc, before, fp)
 
 
+def test_large_batch_matches_the_oracle_per_scene():
+    """A batch of more than 49,152 particles: its full sweeps run one lane per particle (the
+    small batches above run lane groups)."""
+    sc, m = _batch(count=4, seed=9, n_range=(14000, 20000))
+    with m:
+        assert m.nbParticles() > 49152
+        fp = sc["fluid_params"]
+        for _ in range(2):
+            before = _scene_states(m, sc)
+            for c, off, cnt, st in before:
+                oracle.fluids_step(c, fp, 2, st)
+            m.update(1)
+            _compare(m, sc, before, fp)
+
+
 def test_batch_scene_equals_the_same_scene_alone():
     """One scene of a batch and the same scene on its own handle: same trajectory."""
     sc, m = _batch(count=4, seed=11)
