@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, c
       ssq += gxx * gxx + gyy * gyy + gzz * gzz;
     }
   };
-  walk_list_group<LW>(lst, pl.stride, cnt <= pl.K ? cnt : 0u, ldp, body);
+  walk_list_group<LW>(cnt <= pl.K ? cnt : 0u, i, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ldp,
+                      body);
   if (cnt > pl.K && q == 0) for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ldp(j)); });
   rho = quad_sum<LW>(rho);
   sgx = quad_sum<LW>(sgx);
@@ -195,15 +196,16 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : 12) k_fluid_deltap(GridK g, F
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;  // a lane past the end shadows the last particle
   float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-  float4 xi = f4(0.f, 0.f, 0.f, 0.f);
-  if (active) {
-    scene_of<BATCH>(i, g, p);
+  float4 xi;
+  {
+    scene_of<BATCH>(ii, g, p);
     const Sph k(g);
-    xi = ld4(pred + i);  // clamped by the producer
-    const float li = __ldg(lambda + i);
+    xi = ld4(pred + ii);  // clamped by the producer
+    const float li = __ldg(lambda + ii);
     auto ld = [&](uint32_t j) { return Pair4{ld4(pred + j), __ldg(lambda + j)}; };
-    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair4 a) {
+    quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair4 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
@@ -352,7 +354,8 @@ __global__ void __launch_bounds__(GUARD ? kGuardGroupThreads<LW> : 128) k_fluid_
         w = w + cross4(a.v - vi, f4(vx * s, vy * s, vz * s, 0.0f));
       }
     };
-    walk_list_group<LW>(lst, pl.stride, cnt <= pl.K ? cnt : 0u, ld, body);
+    walk_list_group<LW>(cnt <= pl.K ? cnt : 0u, i, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ld,
+                        body);
     if (cnt > pl.K && q == 0) for_each_fluid_neighbour(gi, table, xi, [&](uint32_t j) { body(j, ld(j)); });
     w.x = quad_sum<LW>(w.x);
     w.y = quad_sum<LW>(w.y);
@@ -384,13 +387,14 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;  // a lane past the end shadows the last particle
   float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-  if (active) {
-    scene_of<BATCH>(i, g, p);
+  {
+    scene_of<BATCH>(ii, g, p);
     const Sph k(g);
-    const float4 xi = ld4(pred + i);
+    const float4 xi = ld4(pred + ii);
     auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(vort + j)}; };
-    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+    quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair44 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
@@ -431,15 +435,16 @@ __global__ void __launch_bounds__(128) k_fluid_xsph_final(GridK g, FluidK p, con
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
   const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;  // a lane past the end shadows the last particle
   float ax = 0.0f, ay = 0.0f, az = 0.0f, aw = 0.0f;
-  float4 xi = f4(0.f, 0.f, 0.f, 0.f), vi = xi;
-  if (active) {
-    scene_of<BATCH>(i, g, p);
+  float4 xi, vi;
+  {
+    scene_of<BATCH>(ii, g, p);
     const Sph k(g);
-    xi = ld4(pred + i);
-    vi = ld4(velS + i);
+    xi = ld4(pred + ii);
+    vi = ld4(velS + ii);
     auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(velS + j)}; };
-    quad_pairs<LANES>(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+    quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair44 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;

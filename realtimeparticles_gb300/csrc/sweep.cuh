@@ -269,26 +269,23 @@ __device__ __forceinline__ uint32_t filter_fluid_group(const GridK& g, const uin
 }
 
 // The list walk of a lane group in lockstep with the warp's other groups: lane q visits
-// entries q, q + LW, ... of lst[0..cnt) (stride apart), four at a time, for as many rounds as
-// the warp's longest list needs.  The whole warp must call; cnt = 0 visits nothing.
-template <int LW, class G, class F>
-__device__ __forceinline__ void walk_list_group(const uint32_t* lst, uint32_t stride, uint32_t cnt, G&& ld, F&& f) {
+// entries q, q + LW, ... of a list of cnt entries (idx(kk) loads entry kk), four at a time,
+// for as many rounds as the warp's longest list needs, so the lanes stay converged and every
+// round has four loads in flight.  A slot past the lane's own list loads particle `self`
+// (any valid index) and is not visited.  The whole warp must call; cnt = 0 visits nothing.
+template <int LW, class IDX, class G, class F>
+__device__ __forceinline__ void walk_list_group(uint32_t cnt, uint32_t self, IDX&& idx, G&& ld, F&& f) {
   const uint32_t q = threadIdx.x & (LW - 1u);
   const uint32_t most = __reduce_max_sync(0xffffffffu, cnt);
-  for (uint32_t k0 = 0; k0 < most; k0 += 4u * LW) {
+  for (uint32_t k0 = q; k0 < most; k0 += 4u * LW) {
     uint32_t j[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint32_t kk = k0 + u * LW + q;
-      j[u] = kk < cnt ? lst[(size_t)kk * stride] : 0u;
-    }
-    decltype(ld(0u)) a[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (k0 + u * LW + q < cnt) a[u] = ld(j[u]);
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (k0 + u * LW + q < cnt) f(j[u], a[u]);
+    for (int u = 0; u < 4; ++u) j[u] = k0 + u * LW < cnt ? idx(k0 + u * LW) : self;
+    const auto a0 = ld(j[0]), a1 = ld(j[1]), a2 = ld(j[2]), a3 = ld(j[3]);
+    if (k0 < cnt) f(j[0], a0);
+    if (k0 + LW < cnt) f(j[1], a1);
+    if (k0 + 2 * LW < cnt) f(j[2], a2);
+    if (k0 + 3 * LW < cnt) f(j[3], a3);
   }
 }
 
@@ -303,6 +300,24 @@ __device__ __forceinline__ void quad_pairs(const GridK& g, const uint2* __restri
     visit_list_x4(q, c, LANES, [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
   } else if (q == 0) {
     for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
+  }
+}
+
+// quad_pairs called by every lane of the warp (a lane past the last particle with active =
+// false visits nothing).  SYNC walks the warp's particles in lockstep (walk_list_group):
+// measured 0.5 % faster on the 131k dam break and 1.8 % at 16k, but 1.5 % slower for 48
+// batched scenes, whose larger kernels spill under it; !SYNC is quad_pairs on the active lanes.
+template <int LANES, bool SYNC, class G, class F>
+__device__ __forceinline__ void quad_pairs_sync(const GridK& g, const uint2* __restrict__ table, const PairList& L,
+                                                uint32_t i, uint32_t q, bool active, float4 xi, G&& ld, F&& f) {
+  if constexpr (SYNC) {
+    const uint32_t c = active ? __ldg(L.count + i) : 0u;
+    const uint32_t* base = L.idx + i;
+    walk_list_group<LANES>(c != kListOverflow ? c : 0u, i,
+                           [&](uint32_t kk) { return __ldg(base + (size_t)kk * L.stride); }, ld, f);
+    if (c == kListOverflow && q == 0) for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { f(j, ld(j)); });
+  } else if (active) {
+    quad_pairs<LANES>(g, table, L, i, q, xi, ld, f);
   }
 }
 
