@@ -61,10 +61,12 @@ def test_switches(vort, ap):
         _step_and_compare(m, c, fp, 2, steps=3)
 
 
-def test_ragged_count_and_spare_capacity():
-    # N not a multiple of the sort tile, maxNb > N: the tail stays untouched.
-    sc = scenes.dam_break(lattice=(8, 16, 16), max_n=5000)
-    n = 8 * 16 * 16 - 37
+@pytest.mark.parametrize("lattice,spare", [((8, 16, 16), 5000), ((16, 32, 64), 33000)])
+def test_ragged_count_and_spare_capacity(lattice, spare):
+    # N not a multiple of the sort tile nor of the particles per warp of the lane-group sweeps
+    # (4 with 8 lanes at 2k, 8 with 4 lanes at 33k), maxNb > N: the tail stays untouched.
+    sc = scenes.dam_break(lattice=lattice, max_n=spare)
+    n = lattice[0] * lattice[1] * lattice[2] - 37
     sc["pos"] = sc["pos"][:n].copy()
     sc["vel"] = sc["vel"][:n].copy()
     sc["model_params"].currNbParticles = n
@@ -72,7 +74,7 @@ def test_ragged_count_and_spare_capacity():
     with fluids_model(sc, 2) as m:
         assert m.nbParticles() == n
         _step_and_compare(m, c, sc["fluid_params"], 2, steps=2)
-        tail = m.download(abi.BUF_POS, 5000)[n:]
+        tail = m.download(abi.BUF_POS, spare)[n:]
         assert np.all(tail == 0)
 
 
