@@ -84,7 +84,8 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
                                                                 const uint2* __restrict__ table, uint32_t n,
                                                                 float* __restrict__ lambda,
                                                                 float* __restrict__ density, PairList pl,
-                                                                float* __restrict__ lamTot, int totMode) {
+                                                                float* __restrict__ lamTot, int totMode,
+                                                                float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
   const float lam = -C / (ssq + p.relaxCFM);
   lambda[i] = lam;
   density[i] = rho;
+  if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
   // Total lambda of the step (warm start): kTotWrite starts it, kTotAdd accumulates.
   if (totMode == kTotWrite) lamTot[i] = lam;
   else if (totMode == kTotAdd) lamTot[i] += lam;
@@ -136,7 +138,8 @@ template <bool BATCH, int LW>
 __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, const float4* __restrict__ pred,
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             float* __restrict__ lambda, float* __restrict__ density,
-                                                            PairList pl, float* __restrict__ lamTot, int totMode) {
+                                                            PairList pl, float* __restrict__ lamTot, int totMode,
+                                                            float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, q = t % LW;
   if ((t & ~31u) / LW >= n) return;  // the whole warp is past the last particle
@@ -179,6 +182,7 @@ __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, c
   const float lam = -C / (ssq + p.relaxCFM);
   lambda[i] = lam;
   density[i] = rho;
+  if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
   if (totMode == kTotWrite) lamTot[i] = lam;
   else if (totMode == kTotAdd) lamTot[i] += lam;
 }
@@ -186,12 +190,15 @@ __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, c
 // fld_computeConstraintCorrection + fld_correctPosition (Jacobi: writes a second buffer);
 // LAST adds fld_updateVel (fluids.cl:263-273).  LANES lanes per particle.  Input positions
 // are already clamped by fld_applyBoundaryCondition (done by their producer).
-template <bool LAST, bool BATCH, int LANES>
+// PACKED: the neighbours' positions and lambdas come from one float4 array (x, y, z, lambda)
+// written by the lambda sweep, one load per pair instead of two.
+template <bool LAST, bool BATCH, int LANES, bool PACKED>
 __global__ void __launch_bounds__(128, BATCH ? 1 : 12) k_fluid_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut,
                                                       const float4* __restrict__ posS, float4* __restrict__ velS,
-                                                      PairList pl, const float4* __restrict__ res) {
+                                                      PairList pl, const float4* __restrict__ res,
+                                                      const float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
@@ -203,8 +210,15 @@ __global__ void __launch_bounds__(128, BATCH ? 1 : 12) k_fluid_deltap(GridK g, F
     scene_of<BATCH>(ii, g, p);
     const Sph k(g);
     xi = ld4(pred + ii);  // clamped by the producer
-    const float li = __ldg(lambda + ii);
-    auto ld = [&](uint32_t j) { return Pair4{ld4(pred + j), __ldg(lambda + j)}; };
+    const float li = PACKED ? ld4(packed + ii).w : __ldg(lambda + ii);
+    auto ld = [&](uint32_t j) {
+      if constexpr (PACKED) {
+        const float4 a = ld4(packed + j);
+        return Pair4{a, a.w};
+      } else {
+        return Pair4{ld4(pred + j), __ldg(lambda + j)};
+      }
+    };
     quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair4 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
@@ -593,7 +607,7 @@ int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uin
 
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table, uint32_t n,
                     float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
-                    Launcher& L, float* lamTot, int totMode) {
+                    Launcher& L, float* lamTot, int totMode, float4* packed) {
   L.begin("fld_lambda");
   const dim3 nb(blocks(n, kSweepThreads)), nt(kSweepThreads);
   const bool mask = n >= kMaskFilterParticles;
@@ -601,38 +615,47 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
     dispatch_group(lw, [&](auto LW) {
       const dim3 gb(blocks(n, 128 / LW)), gt(128);
       if (p.bt.scenes)
-        launch(L, k_fluid_lambda_group<true, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+        launch(L, k_fluid_lambda_group<true, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode,
+               packed);
       else
         launch(L, k_fluid_lambda_group<false, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot,
-               totMode);
+               totMode, packed);
     });
   } else if (p.bt.scenes && mask)
-    launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+    launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
   else if (p.bt.scenes)
-    launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+    launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
   else if (mask)
-    launch(L, k_fluid_lambda<false, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+    launch(L, k_fluid_lambda<false, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
   else
-    launch(L, k_fluid_lambda<false, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode);
+    launch(L, k_fluid_lambda<false, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode,
+           packed);
   L.end("fld_lambda");
   int rc = check("k_fluid_lambda");
   if (rc) return rc;
-  return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L);
+  return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L, packed);
 }
 
 int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
                  const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
-                 const float4* res, Launcher& L) {
+                 const float4* res, Launcher& L, const float4* packed) {
   L.begin(last ? "fld_deltap_vel" : "fld_deltap");
   dispatch_fluid(p, [&](auto B, auto LN) {
     constexpr bool BATCH = decltype(B)::value;
     constexpr int LANES = decltype(LN)::value;
-    if (last)
-      launch(L, k_fluid_deltap<true, BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128),
-          g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
+    const dim3 gb(blocks(n * LANES, 128)), gt(128);
+    if (last && packed)
+      launch(L, k_fluid_deltap<true, BATCH, LANES, true>, gb, gt, g, p, predIn, lambda, table, n, predOut, posS, velS,
+             pl, res, packed);
+    else if (last)
+      launch(L, k_fluid_deltap<true, BATCH, LANES, false>, gb, gt, g, p, predIn, lambda, table, n, predOut, posS, velS,
+             pl, res, packed);
+    else if (packed)
+      launch(L, k_fluid_deltap<false, BATCH, LANES, true>, gb, gt, g, p, predIn, lambda, table, n, predOut, posS,
+             velS, pl, res, packed);
     else
-      launch(L, k_fluid_deltap<false, BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128),
-          g, p, predIn, lambda, table, n, predOut, posS, velS, pl, res);
+      launch(L, k_fluid_deltap<false, BATCH, LANES, false>, gb, gt, g, p, predIn, lambda, table, n, predOut, posS,
+             velS, pl, res, packed);
   });
   L.end(last ? "fld_deltap_vel" : "fld_deltap");
   return check("k_fluid_deltap");

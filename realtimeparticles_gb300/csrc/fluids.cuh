@@ -89,11 +89,14 @@ int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uin
                   const ZeroJob& zero = ZeroJob{}, const HostIO& io = HostIO{});
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table,
                     uint32_t n, float* lambda, float* density, bool last, const float4* posS, float4* velS,
-                    const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone);
-// Position correction alone with given lambdas (+ an optional residual displacement).
+                    const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone,
+                    float4* packed = nullptr);
+// Position correction alone with given lambdas (+ an optional residual displacement).  With
+// `packed` (x, y, z, lambda per particle, written by the lambda sweep) the neighbours' data
+// come from there.
 int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
                  const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
-                 const float4* res, Launcher& L);
+                 const float4* res, Launcher& L, const float4* packed = nullptr);
 // fld_computeVorticity; with errPartial also the per-block density-error sums.
 int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
                     const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L);

@@ -146,6 +146,7 @@ struct Handle {
   float4 *predTmp = nullptr, *predA = nullptr, *predB = nullptr, *predFinal = nullptr;
   float4 *vort = nullptr, *acc = nullptr, *totCorr = nullptr, *totCorrS = nullptr;
   float *lambda = nullptr, *density = nullptr;
+  float4* predLam = nullptr;  // (x, y, z, lambda) of the current Jacobi iteration
   float *temp = nullptr, *vapor = nullptr, *cloud = nullptr, *buoy = nullptr;
   float *tempS = nullptr, *vaporS = nullptr, *cloudS = nullptr, *buoyS = nullptr;
   float *lapT = nullptr, *lamT = nullptr;
@@ -311,6 +312,7 @@ static int alloc_buffers(Handle* h) {
     RTP_TRY(dalloc(h, &h->predB, M));
     RTP_TRY(dalloc(h, &h->vort, M));
     RTP_TRY(dalloc(h, &h->lambda, M));
+    RTP_TRY(dalloc(h, &h->predLam, M));
     RTP_TRY(dalloc(h, &h->density, M));
     h->predFinal = h->predA;
     RTP_TRY(dalloc(h, &h->pairs.idx, (size_t)kPairListK * M));
@@ -437,7 +439,7 @@ static int plain_iterations(Handle* h, Launcher& L, const FluidK& fk, const floa
     float4* out = ((count - it) % 2 == 1) ? dest : spare;
     const int mode = !trackTot ? kTotNone : ((it == 0 && !firstAdds) ? kTotWrite : kTotAdd);
     RTP_TRY(fluid_iteration(h->g, fk, cur, out, h->table, n, h->lambda, h->density, it + 1 == count, h->posS, h->velS,
-                            h->pairs, L, h->lamTot, mode));
+                            h->pairs, L, h->lamTot, mode, h->predLam));
     cur = out;
   }
   return RTP_OK;
@@ -470,7 +472,7 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   float4* nxt = h->predB;
   for (uint32_t it = 0; it < h->iters; ++it) {
     RTP_TRY(fluid_iteration(g, fk, cur, nxt, h->table, n, h->lambda, h->density, it + 1 == h->iters, h->posS, h->velS,
-                            h->pairs, L));
+                            h->pairs, L, nullptr, kTotNone, h->predLam));
     std::swap(cur, nxt);
   }
   if (h->iters == 0) RTP_TRY(fluid_update_vel(g, fk, cur, h->posS, n, h->velS, L));
