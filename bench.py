@@ -120,7 +120,8 @@ def make_model(w, rank=0):
 # DRAM bytes (read + write) per launch of a workload's dominant kernel from one ncu capture
 # (cold cache, serialised), with the summary that records the capture.
 KERNEL_TRAFFIC = {
-    ("pbf_dam_break_131k", "fld_lambda"): (6455893, "profiles/k_fluid_lambda_131k_traffic.md"),
+    ("pbf_dam_break_131k", "fld_lambda"): (6600021, "profiles/k_fluid_lambda_131k_traffic.md"),
+    ("pbf_dam_break_16k", "fld_lambda"): (523520, "profiles/k_fluid_lambda_group_16k_traffic.md"),
 }
 
 KERNEL_BYTES = {
