@@ -50,8 +50,21 @@ __device__ __forceinline__ void visit_ranges3(uint32_t b0, uint32_t e0, uint32_t
   for (uint32_t j = cb; j < ce; ++j) f(j);
 }
 
+// The last 1..N indices [j, e) of a range in one round: N loads in flight, the indices past
+// e - 1 loading e - 1 again (a line already being fetched) and not visited.
+template <int N, class G, class F>
+__device__ __forceinline__ void visit_tail(uint32_t j, uint32_t e, G&& g, F&& f) {
+  decltype(g(j)) a[N];
+#pragma unroll
+  for (int u = 0; u < N; ++u) a[u] = g(min(j + u, e - 1u));
+#pragma unroll
+  for (int u = 0; u < N; ++u)
+    if (j + u < e) f(j + u, a[u]);
+}
+
 // Visits every index of [b, e) with f(j), four loads in flight: g(j) loads what f needs for
-// candidate j, f(j, loaded) consumes it.  Order of f calls = ascending j.
+// candidate j, f(j, loaded) consumes it.  Order of f calls = ascending j.  The last 1-3
+// indices take one round, not one round each.
 template <class G, class F>
 __device__ __forceinline__ void visit_range_x4(uint32_t b, uint32_t e, G&& g, F&& f) {
   uint32_t j = b;
@@ -62,7 +75,7 @@ __device__ __forceinline__ void visit_range_x4(uint32_t b, uint32_t e, G&& g, F&
     f(j + 2, a2);
     f(j + 3, a3);
   }
-  for (; j < e; ++j) f(j, g(j));
+  if (j < e) visit_tail<3>(j, e, g, f);
 }
 
 // As visit_range_x4 with eight loads in flight first (the distance-only filter passes, whose
@@ -129,9 +142,13 @@ __device__ __forceinline__ void visit_list_x4(uint32_t begin, uint32_t end, uint
     f(j2, a2);
     f(j3, a3);
   }
-  for (; kk < end; kk += step) {
-    const uint32_t j = idx(kk);
-    f(j, g(j));
+  if (kk < end) {  // 1-3 entries left: one round of index loads, one of operand loads
+    const uint32_t last = kk + (end - 1u - kk) / step * step;
+    const uint32_t j0 = idx(kk), j1 = idx(min(kk + step, last)), j2 = idx(min(kk + 2 * step, last));
+    const auto a0 = g(j0), a1 = g(j1), a2 = g(j2);
+    f(j0, a0);
+    if (kk + step < end) f(j1, a1);
+    if (kk + 2 * step < end) f(j2, a2);
   }
 }
 
