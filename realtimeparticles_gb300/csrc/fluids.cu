@@ -281,7 +281,8 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vortic
                                                                     const float4* __restrict__ velS,
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float4* __restrict__ vort, PairList pl,
-                                                                    float* __restrict__ errPartial) {
+                                                                    float* __restrict__ errPartial,
+                                                                    float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
@@ -314,6 +315,7 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_vortic
       for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ld(j)); });
     pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
     vort[i] = w;
+    if (packed) packed[i] = f4(xi.x, xi.y, xi.z, sqrtf(dot4(w, w)));
     if (GUARD) err = fabsf(rho / p.rho0 - 1.0f);
   }
   if (GUARD) block_error_partial(err, errPartial);
@@ -331,7 +333,7 @@ template <bool GUARD, bool BATCH, int LW>
 __global__ void __launch_bounds__(GUARD ? kGuardGroupThreads<LW> : 128) k_fluid_vorticity_group(
     GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ velS,
     const uint2* __restrict__ table, uint32_t n, float4* __restrict__ vort, PairList pl,
-    float* __restrict__ errPartial) {
+    float* __restrict__ errPartial, float4* __restrict__ packed) {
   pdl_enter();
   constexpr uint32_t P = (GUARD ? kGuardGroupThreads<LW> : 128) / LW;  // particles per pass of the block
   constexpr uint32_t R = GUARD ? 64 / P : 1;
@@ -379,6 +381,7 @@ __global__ void __launch_bounds__(GUARD ? kGuardGroupThreads<LW> : 128) k_fluid_
     if (q == 0 && live) {
       pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
       vort[i] = w;
+      if (packed) packed[i] = f4(xi.x, xi.y, xi.z, sqrtf(dot4(w, w)));
       if (GUARD) s_err[r * P + slot] = fabsf(rho / pi.rho0 - 1.0f);
     }
   }
@@ -392,11 +395,14 @@ __global__ void __launch_bounds__(GUARD ? kGuardGroupThreads<LW> : 128) k_fluid_
   }
 }
 
-// fld_applyVorticityConfinement (fluids.cl:329-377), LANES lanes per particle.
-template <bool BATCH, int LANES>
+// fld_applyVorticityConfinement (fluids.cl:329-377), LANES lanes per particle.  PACKED: each
+// neighbour's position and |omega| come from one float4 (x, y, z, |omega|) written by the
+// vorticity sweep.
+template <bool BATCH, int LANES, bool PACKED>
 __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
-                                                       uint32_t n, float4* __restrict__ velS, PairList pl) {
+                                                       uint32_t n, float4* __restrict__ velS, PairList pl,
+                                                       const float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / LANES, q = t % LANES;
@@ -407,16 +413,23 @@ __global__ void __launch_bounds__(128) k_fluid_confine(GridK g, FluidK p, const 
     scene_of<BATCH>(ii, g, p);
     const Sph k(g);
     const float4 xi = ld4(pred + ii);
-    auto ld = [&](uint32_t j) { return Pair44{ld4(pred + j), ld4(vort + j)}; };
-    quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair44 a) {
+    auto ld = [&](uint32_t j) {
+      if constexpr (PACKED) {
+        const float4 a = ld4(packed + j);
+        return Pair4{a, a.w};
+      } else {
+        const float4 wj = ld4(vort + j);
+        return Pair4{ld4(pred + j), sqrtf(dot4(wj, wj))};
+      }
+    };
+    quad_pairs_sync<LANES, !BATCH>(g, table, pl, ii, q, active, xi, ld, [&](uint32_t, Pair4 a) {
       const float4 xj = a.x;
       const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
         float r;
         const float s = k.gs(r2, r);
-        const float4 wj = a.v;
-        const float f = sqrtf(dot4(wj, wj)) * s;
+        const float f = a.s * s;
         ex += vx * f;
         ey += vy * f;
         ez += vz * f;
@@ -673,12 +686,13 @@ int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const 
 }
 
 int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
-                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L) {
+                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L,
+                    float4* packed) {
   L.begin("fld_vorticity");
   const uint32_t nb = blocks(n, kSweepThreads);
   auto go = [&](auto GUARD, auto BATCH, auto MASK) {
     launch(L, k_fluid_vorticity<decltype(GUARD)::value, decltype(BATCH)::value, decltype(MASK)::value>, dim3(nb),
-           dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, errPartial);
+           dim3(kSweepThreads), g, p, pred, velS, table, n, vort, pl, errPartial, packed);
   };
   using T = std::true_type;
   using F = std::false_type;
@@ -689,16 +703,19 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
       if (guard) {  // 64 particles per block: one errPartial entry each
         const dim3 gb(blocks(n, 64)), gt(kGuardGroupThreads<LW>);
         if (batch)
-          launch(L, k_fluid_vorticity_group<true, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+          launch(L, k_fluid_vorticity_group<true, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial,
+                 packed);
         else
-          launch(L, k_fluid_vorticity_group<true, false, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+          launch(L, k_fluid_vorticity_group<true, false, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial,
+                 packed);
       } else {
         const dim3 gb(blocks(n, 128 / LW)), gt(128);
         if (batch)
-          launch(L, k_fluid_vorticity_group<false, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial);
+          launch(L, k_fluid_vorticity_group<false, true, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl, errPartial,
+                 packed);
         else
           launch(L, k_fluid_vorticity_group<false, false, LW>, gb, gt, g, p, pred, velS, table, n, vort, pl,
-                 errPartial);
+                 errPartial, packed);
       }
     });
   } else if (guard) {
@@ -714,18 +731,22 @@ int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const f
 
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L, bool vorticityDone, const HostIO& io) {
+               Launcher& L, bool vorticityDone, const HostIO& io, float4* packed) {
   if (p.vorticity) {
     int rc = RTP_OK;
     if (!vorticityDone) {
-      rc = fluid_vorticity(g, p, pred, velS, vort, table, n, pl, nullptr, L);
+      rc = fluid_vorticity(g, p, pred, velS, vort, table, n, pl, nullptr, L, packed);
       if (rc) return rc;
     }
     L.begin("fld_confine");
     dispatch_fluid(p, [&](auto B, auto LN) {
       constexpr bool BATCH = decltype(B)::value;
       constexpr int LANES = decltype(LN)::value;
-      launch(L, k_fluid_confine<BATCH, LANES>, dim3(blocks(n * LANES, 128)), dim3(128), g, p, pred, vort, table, n, velS, pl);
+      const dim3 gb(blocks(n * LANES, 128)), gt(128);
+      if (packed)
+        launch(L, k_fluid_confine<BATCH, LANES, true>, gb, gt, g, p, pred, vort, table, n, velS, pl, packed);
+      else
+        launch(L, k_fluid_confine<BATCH, LANES, false>, gb, gt, g, p, pred, vort, table, n, velS, pl, packed);
     });
     L.end("fld_confine");
     rc = check("k_fluid_confine");

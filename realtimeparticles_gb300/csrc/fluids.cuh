@@ -97,14 +97,17 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
 int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,
                  const uint2* table, uint32_t n, bool last, const float4* posS, float4* velS, const PairList& pl,
                  const float4* res, Launcher& L, const float4* packed = nullptr);
-// fld_computeVorticity; with errPartial also the per-block density-error sums.
+// fld_computeVorticity; with errPartial also the per-block density-error sums; with `packed`
+// also (x, y, z, |omega|) per particle for the confinement sweep (fluid_post with the same
+// `packed`).
 int fluid_vorticity(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, float4* vort,
-                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L);
+                    const uint2* table, uint32_t n, const PairList& pl, float* errPartial, Launcher& L,
+                    float4* packed = nullptr);
 int fluid_update_vel(const GridK& g, const FluidK& p, const float4* pred, const float4* posS, uint32_t n, float4* velS,
                      Launcher& L);
 int fluid_post(const GridK& g, const FluidK& p, const float4* pred, float4* velS, float4* vort, const uint2* table,
                uint32_t n, const uint32_t* idsS, float4* pos, float4* vel, uint32_t* ids, const PairList& pl,
-               Launcher& L, bool vorticityDone = false, const HostIO& io = HostIO{});
+               Launcher& L, bool vorticityDone = false, const HostIO& io = HostIO{}, float4* packed = nullptr);
 int fluid_metrics(const GridK& g, const FluidK& p, const float4* pos, const float4* vel, const uint2* table, uint32_t n,
                   double* acc, uint32_t* hist, Launcher& L);
 

@@ -146,7 +146,7 @@ struct Handle {
   float4 *predTmp = nullptr, *predA = nullptr, *predB = nullptr, *predFinal = nullptr;
   float4 *vort = nullptr, *acc = nullptr, *totCorr = nullptr, *totCorrS = nullptr;
   float *lambda = nullptr, *density = nullptr;
-  float4* predLam = nullptr;  // (x, y, z, lambda) of the current Jacobi iteration
+  float4* predLam = nullptr;  // (x, y, z, lambda) in each Jacobi iteration, then (x, y, z, |omega|)
   float *temp = nullptr, *vapor = nullptr, *cloud = nullptr, *buoy = nullptr;
   float *tempS = nullptr, *vaporS = nullptr, *cloudS = nullptr, *buoyS = nullptr;
   float *lapT = nullptr, *lamT = nullptr;
@@ -450,7 +450,7 @@ static int plain_iterations(Handle* h, Launcher& L, const FluidK& fk, const floa
 static int solver_error(Handle* h, Launcher& L, const FluidK& fk, const float4* x, bool* vortDone) {
   const uint32_t n = (uint32_t)h->curN;
   if (fk.vorticity) {
-    RTP_TRY(fluid_vorticity(h->g, fk, x, h->velS, h->vort, h->table, n, h->pairs, h->errPartial, L));
+    RTP_TRY(fluid_vorticity(h->g, fk, x, h->velS, h->vort, h->table, n, h->pairs, h->errPartial, L, h->predLam));
     *vortDone = true;
     return RTP_OK;
   }
@@ -484,7 +484,7 @@ static int record_fluids_step(Handle* h, Launcher& L) {
   }
   // Fluids.cpp:444-457.
   return fluid_post(g, fk, cur, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L, vortDone,
-                    h->io);
+                    h->io, h->predLam);
 }
 
 // Warm-started substep: the network's lambda and residual give the first correction, then
@@ -555,7 +555,7 @@ static int record_fluids_ws_step(Handle* h, Launcher& L) {
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(guard body)");
   }
   return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
-                    vortDone, h->io);
+                    vortDone, h->io, h->predLam);
 }
 
 // One plain step with `iters` iterations that also writes training samples.
@@ -576,7 +576,8 @@ static int record_sample_step(Handle* h, uint32_t iters, uint32_t stride, uint32
   RTP_TRY(ws_record_targets(g, fk, h->predA, h->lamTot, h->table, n, h->predB, h->pairsRec, stride, phase, count,
                             targets, L));
   h->predFinal = h->predB;
-  return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L);
+  return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
+                    false, HostIO{}, h->predLam);
 }
 
 static int record_boids_step(Handle* h, Launcher& L) {
