@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(kKeyThreads) k_cloud_thermo_predict(
 __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g, CloudK c, const float4* __restrict__ pos,
                                                                          const float* __restrict__ temp,
                                                                          const uint2* __restrict__ table, uint32_t n,
-                                                                         float* __restrict__ lamT, PairList pl) {
+                                                                         float* __restrict__ lamT, PairList pl,
+                                                                         float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -273,15 +274,19 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_temp_lambda(GridK g
   pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   lap /= c.cloudRho0;
   ssq += sg * sg;
-  lamT[i] = -lap / (ssq + c.cloudRelax);
+  const float lt = -lap / (ssq + c.cloudRelax);
+  lamT[i] = lt;
+  packed[i] = f4(xi.x, xi.y, xi.z, lt);
 }
 
 // cld_computeConstraintCorrectionTemp + cld_correctTemperature (in place: the sweep reads
-// only lamT and positions of the neighbours).  kQuad lanes per particle.
+// only lamT and positions of the neighbours, both from `packed` = (x, y, z, lamT) written by
+// k_cloud_temp_lambda).  kQuad lanes per particle.
 __global__ void __launch_bounds__(128, 8) k_cloud_temp_correct(GridK g, CloudK c, const float4* __restrict__ pos,
                                                             const float* __restrict__ lamT,
                                                             const uint2* __restrict__ table, uint32_t n,
-                                                            float* __restrict__ temp, PairList pl) {
+                                                            float* __restrict__ temp, PairList pl,
+                                                            const float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
@@ -292,14 +297,14 @@ __global__ void __launch_bounds__(128, 8) k_cloud_temp_correct(GridK g, CloudK c
     const float4 xi = ld4(pos + i);
     const float li = __ldg(lamT + i);
     quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
-      const float4 xj = ld4(pos + j);
+      const float4 xj = ld4(packed + j);
       const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
         float r;
         const float s = k.gs(r2, r);
         const float d = r2 * s / (r2 * c.cloudRho0 + kFloatEps);
-        corr += (li + __ldg(lamT + j)) * d;
+        corr += (li + xj.w) * d;
       }
     });
   }
@@ -311,7 +316,8 @@ __global__ void __launch_bounds__(128, 8) k_cloud_temp_correct(GridK g, CloudK c
 __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
                                                                     const uint2* __restrict__ table, uint32_t n,
                                                                     float* __restrict__ lambda,
-                                                                    float* __restrict__ density, PairList pl) {
+                                                                    float* __restrict__ density, PairList pl,
+                                                                    float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -348,8 +354,10 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
-  lambda[i] = -C / (ssq + p.relaxCFM);
+  const float lam = -C / (ssq + p.relaxCFM);
+  lambda[i] = lam;
   density[i] = rho;
+  packed[i] = f4(xi.x, xi.y, xi.z, lam);
 }
 
 // cld_computeConstraintCorrection, cld_correctPosition x2 and the mixed boundary
@@ -358,7 +366,8 @@ template <bool LAST>
 __global__ void __launch_bounds__(128, 8) k_cloud_deltap(GridK g, FluidK p, const float4* __restrict__ pred,
                                                       const float* __restrict__ lambda, const uint2* __restrict__ table,
                                                       uint32_t n, float4* __restrict__ predOut, float4* __restrict__ tot,
-                                                      float4* __restrict__ velS, PairList pl) {
+                                                      float4* __restrict__ velS, PairList pl,
+                                                      const float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
@@ -370,7 +379,7 @@ __global__ void __launch_bounds__(128, 8) k_cloud_deltap(GridK g, FluidK p, cons
     xi = ld4(pred + i);
     const float li = __ldg(lambda + i);
     quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
-      const float4 xj = ld4(pred + j);
+      const float4 xj = ld4(packed + j);  // (x, y, z, lambda) from k_cloud_lambda
       const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
@@ -378,7 +387,7 @@ __global__ void __launch_bounds__(128, 8) k_cloud_deltap(GridK g, FluidK p, cons
         const float s = k.gs(r2, r);
         float sc = 0.0f;
         if (p.artPressure) sc = -p.apCoeff * powi(k.w(r2) * p.apInvWq, p.apExp);
-        const float f = (li + __ldg(lambda + j) + sc) * s;
+        const float f = (li + xj.w + sc) * s;
         ax += vx * f;
         ay += vy * f;
         az += vz * f;
@@ -415,7 +424,8 @@ __global__ void k_cloud_update_vel(GridK g, FluidK p, const float4* __restrict__
 __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, const float4* __restrict__ pred,
                                                                        const float4* __restrict__ velS,
                                                                        const uint2* __restrict__ table, uint32_t n,
-                                                                       float4* __restrict__ vort, PairList pl) {
+                                                                       float4* __restrict__ vort, PairList pl,
+                                                                       float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -446,12 +456,14 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_vorticity(GridK g, 
     for_each_cloud_neighbour(g, table, xi, body);
   pl.count[i] = lw.ok() ? lw.n : kListOverflow;
   vort[i] = w;
+  packed[i] = f4(xi.x, xi.y, xi.z, sqrtf(dot4(w, w)));
 }
 
 // cld_applyVorticityConfinement (clouds.cl:790-850).  kQuad lanes per particle.
 __global__ void __launch_bounds__(128, 8) k_cloud_confine(GridK g, FluidK p, const float4* __restrict__ pred,
                                                        const float4* __restrict__ vort, const uint2* __restrict__ table,
-                                                       uint32_t n, float4* __restrict__ velS, PairList pl) {
+                                                       uint32_t n, float4* __restrict__ velS, PairList pl,
+                                                       const float4* __restrict__ packed) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
@@ -461,14 +473,13 @@ __global__ void __launch_bounds__(128, 8) k_cloud_confine(GridK g, FluidK p, con
     const Sph k(g);
     const float4 xi = ld4(pred + i);
     quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
-      const float4 xj = ld4(pred + j);
+      const float4 xj = ld4(packed + j);  // (x, y, z, |omega|) from k_cloud_vorticity
       const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
       const float r2 = vx * vx + vy * vy + vz * vz;
       if (r2 < k.h2) {
         float r;
         const float s = k.gs(r2, r);
-        const float4 wj = ld4(vort + j);
-        const float f = sqrtf(dot4(wj, wj)) * s;
+        const float f = xj.w * s;
         ex += vx * f;
         ey += vy * f;
         ez += vz * f;
@@ -567,33 +578,36 @@ int cloud_presort(const GridK& g, const CloudK& c, const float4* pos, const floa
 }
 
 int cloud_temperature(const GridK& g, const CloudK& c, const float4* posS, float* tempS, float* lamT, const uint2* table,
-                      uint32_t n, const PairList& pl, Launcher& L) {
+                      uint32_t n, const PairList& pl, Launcher& L, float4* packed) {
   L.begin("cld_temp_lambda");
-  launch(L, k_cloud_temp_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, c, posS, tempS, table, n, lamT, pl);
+  launch(L, k_cloud_temp_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, c, posS, tempS, table, n, lamT, pl,
+         packed);
   L.end("cld_temp_lambda");
   int rc = check("k_cloud_temp_lambda");
   if (rc) return rc;
   L.begin("cld_temp_correct");
-  launch(L, k_cloud_temp_correct, dim3(blocks(n * kQuad, 128)), dim3(128), g, c, posS, lamT, table, n, tempS, pl);
+  launch(L, k_cloud_temp_correct, dim3(blocks(n * kQuad, 128)), dim3(128), g, c, posS, lamT, table, n, tempS, pl,
+         packed);
   L.end("cld_temp_correct");
   return check("k_cloud_temp_correct");
 }
 
 int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, float4* totS,
                     const uint2* table, uint32_t n, float* lambda, float* density, bool last, float4* velS,
-                    const PairList& pl, Launcher& L) {
+                    const PairList& pl, Launcher& L, float4* packed) {
   L.begin("cld_lambda");
-  launch(L, k_cloud_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda, density, pl);
+  launch(L, k_cloud_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, predIn, table, n, lambda, density, pl,
+         packed);
   L.end("cld_lambda");
   int rc = check("k_cloud_lambda");
   if (rc) return rc;
   L.begin(last ? "cld_deltap_vel" : "cld_deltap");
   if (last)
     launch(L, k_cloud_deltap<true>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut, totS, velS,
-                                                                        pl);
+                                                                        pl, packed);
   else
     launch(L, k_cloud_deltap<false>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut, totS,
-                                                                         velS, pl);
+                                                                         velS, pl, packed);
   L.end(last ? "cld_deltap_vel" : "cld_deltap");
   return check("k_cloud_deltap");
 }
@@ -606,15 +620,16 @@ int cloud_update_vel(const GridK& g, const FluidK& p, const float4* totS, uint32
 }
 
 int cloud_post(const GridK& g, const FluidK& p, const CloudK& c, const float4* pred, float4* velS, float4* vort,
-               const uint2* table, uint32_t n, const CloudState& s, const PairList& pl, Launcher& L) {
+               const uint2* table, uint32_t n, const CloudState& s, const PairList& pl, Launcher& L, float4* packed) {
   if (p.vorticity) {
     L.begin("cld_vorticity");
-    launch(L, k_cloud_vorticity, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, pred, velS, table, n, vort, pl);
+    launch(L, k_cloud_vorticity, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, pred, velS, table, n, vort, pl,
+           packed);
     L.end("cld_vorticity");
     int rc = check("k_cloud_vorticity");
     if (rc) return rc;
     L.begin("cld_confine");
-    launch(L, k_cloud_confine, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, pred, vort, table, n, velS, pl);
+    launch(L, k_cloud_confine, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, pred, vort, table, n, velS, pl, packed);
     L.end("cld_confine");
     rc = check("k_cloud_confine");
     if (rc) return rc;

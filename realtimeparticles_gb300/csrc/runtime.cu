@@ -683,13 +683,14 @@ int record_clouds_step(Handle* h, Launcher& L) {
   RTP_TRY(launch_sort_passes(plan, h->ss.keysA, h->cellId, h->ss, gl, L));
   RTP_TRY(launch_cell_table(g, h->cellId, n, h->table, L, nullptr, true));
   // Clouds.cpp:554-567.
-  if (ck.smoothing) RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, h->pairs, L));
+  if (ck.smoothing)
+    RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, h->pairs, L, h->predLam));
   // Clouds.cpp:570-590.
   float4* cur = h->predA;
   float4* nxt = h->predB;
   for (uint32_t it = 0; it < h->iters; ++it) {
     RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == h->iters,
-                            h->velS, h->pairs, L));
+                            h->velS, h->pairs, L, h->predLam));
     std::swap(cur, nxt);
   }
   if (h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
@@ -708,7 +709,7 @@ int record_clouds_step(Handle* h, Launcher& L) {
   s.buoyS = h->buoyS;
   s.ids = h->ids;
   s.idsS = h->idsS;
-  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, h->pairs, L);
+  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, h->pairs, L, h->predLam);
 }
 
 // ---- Model::reset: reference defaults + the case's initial particles ------------------
