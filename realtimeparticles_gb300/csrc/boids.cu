@@ -48,6 +48,11 @@ __global__ void __launch_bounds__(kKeyThreads) k_boids_keys(GridK g, float4* __r
   th.store(hist0);
 }
 
+// A neighbour's position and velocity, loaded ahead of use.
+struct PosVel {
+  float4 x, v;
+};
+
 __device__ __forceinline__ float4 fnorm(float4 a) {
   const float d = dot4(a, a);
   if (d == 0.0f) return a;
@@ -167,10 +172,18 @@ __global__ void __launch_bounds__(128) k_boids_rules_update(GridK g, BoidsK p, c
     if (inline_sums) {
       rows(add);
     } else {
-      for (int k = 0; k < nh; ++k) {
-        const uint32_t j = hits[k];
-        add(j, ld4(posS + j));
-      }
+      // The recorded boids, four at a time: their positions and velocities loaded together.
+      visit_list_x4(
+          0u, (uint32_t)nh, 1u, [&](uint32_t k) { return hits[k]; },
+          [&](uint32_t j) { return PosVel{ld4(posS + j), ld4(velS + j)}; },
+          [&](uint32_t, PosVel a) {
+            const float4 v = xi - a.x;
+            const float sq = dot4(v, v);
+            sp = sp + a.x;
+            sv = sv + fnorm(a.v);
+            sr = sr + v * (1.0f / sq);
+            ++count;
+          });
     }
   }
   float4 a = f4(0.f, 0.f, 0.f, 0.f);
