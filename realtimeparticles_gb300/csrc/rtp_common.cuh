@@ -14,7 +14,8 @@ constexpr int kSortTile = 2048;            // keys per sort tile
 constexpr int kSortWarps = 8;              // warps of a scatter-pass block at large tile counts
 constexpr int kSortItems = kSortTile / (32 * kSortWarps);  // keys per lane
 constexpr int kSortThreads = kSortWarps * 32;
-constexpr int kKeyThreads = 512;           // threads of the key-producing kernels (one tile each)
+constexpr int kKeyThreads = 1024;          // threads of the key-producing kernels (one tile each;
+                                           // 64 tiles at 131k occupy 64 SMs, so more warps per tile)
 constexpr int kKeyItems = kSortTile / kKeyThreads;
 constexpr int kMaxRadixBits = 9;
 constexpr int kMaxBins = 1 << kMaxRadixBits;
