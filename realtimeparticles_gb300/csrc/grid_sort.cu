@@ -104,11 +104,17 @@ __global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, 
   __shared__ uint32_t s_part[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int d = blockIdx.x * 32 + lane;
-  const uint32_t chunk = (tiles + 7) / 8;
+  const uint32_t chunk = (tiles + 7) / 8;  // at most kScanChunk (tiles <= kScanTilesPerGroup)
   const uint32_t t0 = min(tiles, warp * chunk), t1 = min(tiles, t0 + chunk);
+  // The warp's column slice, loaded once (all loads in flight) and kept for the rewrite.
+  constexpr int kScanChunk = (int)kScanTilesPerGroup / 8;
+  uint32_t v[kScanChunk];
   uint32_t sum = 0;
-  if (d < bins)
-    for (uint32_t t = t0; t < t1; ++t) sum += hist[(size_t)t * kMaxBins + d];
+#pragma unroll
+  for (int u = 0; u < kScanChunk; ++u) {
+    v[u] = (d < bins && t0 + u < t1) ? hist[(size_t)(t0 + u) * kMaxBins + d] : 0u;
+    sum += v[u];
+  }
   s_part[warp][lane] = sum;
   __syncthreads();
   if (warp == 0) {
@@ -124,11 +130,10 @@ __global__ void __launch_bounds__(256) k_sort_scan(uint32_t* __restrict__ hist, 
   __syncthreads();
   if (d < bins) {
     uint32_t run = s_part[warp][lane];
-    for (uint32_t t = t0; t < t1; ++t) {
-      const size_t at = (size_t)t * kMaxBins + d;
-      const uint32_t v = hist[at];
-      hist[at] = run;
-      run += v;
+#pragma unroll
+    for (int u = 0; u < kScanChunk; ++u) {
+      if (t0 + u < t1) hist[(size_t)(t0 + u) * kMaxBins + d] = run;
+      run += v[u];
     }
   }
 }
