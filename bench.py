@@ -321,7 +321,8 @@ def run_reference(args):
             "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
             "ms_per_step": 1000.0 * el / k, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
-            "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0},
+            "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0,
+                       "parallelism": "single"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
                              "sample": sample},
@@ -593,6 +594,7 @@ def run_ours(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": args.workload, "particles": n, "jacobi_iterations": w.get("iters"),
+                       **({"substep_dt": 1 / 240.0} if w["kind"] in ("fluids", "batch") else {}),
                        "l2": "flushed before every timed step (256 MiB write)",
                        "parallelism": ("scenes by rank" if w["kind"] == "batch" else "replicas") if ws > 1
                        else "single"},
