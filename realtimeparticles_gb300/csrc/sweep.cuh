@@ -124,8 +124,15 @@ __device__ __forceinline__ void filter_range_x8(uint32_t b, uint32_t e, G&& g, H
     }
     j += 4;
   }
-  for (; j < e; ++j)
-    if (hit(g(j))) add(j);
+  if (j < e) {  // 1-3 left: one round (past the end re-load e - 1 and do not count)
+    const uint32_t last = e - 1u;
+    const auto a0 = g(j), a1 = g(min(j + 1u, last)), a2 = g(min(j + 2u, last));
+    uint32_t m = (hit(a0) ? 1u : 0u) | (j + 1u < e && hit(a1) ? 2u : 0u) | (j + 2u < e && hit(a2) ? 4u : 0u);
+    while (m) {
+      add(j + (uint32_t)(__ffs(m) - 1));
+      m &= m - 1u;
+    }
+  }
 }
 
 // Walks list entries begin, begin + step, ... < end in order, four at a time: the four

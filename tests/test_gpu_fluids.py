@@ -85,6 +85,15 @@ def test_dam_break_131k_first_step_parity():
         _step_and_compare(m, c, sc["fluid_params"], 3, steps=2)
 
 
+def test_dam_break_1m_first_step_parity():
+    """2^20 particles: the full sweeps record their hits through the bit-mask filter (the path
+    from 1M particles on)."""
+    sc = scenes.dam_break(lattice=(64, 128, 128), box=2.0)
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    with fluids_model(sc, 3) as m:
+        _step_and_compare(m, c, sc["fluid_params"], 3, steps=1)
+
+
 def test_long_run_statistics_16k():
     """500 independent steps on each side (config 0): density error, kinetic energy
     and the neighbour-count histogram must agree (the trajectories themselves diverge)."""
