@@ -17,8 +17,8 @@ from helpers import REL_BOX, assert_close_by_id, random_net
 pytestmark = pytest.mark.gpu
 
 
-def _batch(count=6, seed=3, n_range=(700, 3000), iters=2):
-    sc = scenes.batched_dam_breaks(count=count, seed=seed, n_range=n_range)
+def _batch(count=6, seed=3, n_range=(700, 3000), iters=2, **kw):
+    sc = scenes.batched_dam_breaks(count=count, seed=seed, n_range=n_range, **kw)
     m = model.FluidsBatch(sc["scenes"], sc["h"])
     m.setFluidParams(sc["fluid_params"])
     m.setJacobiIterations(iters)
@@ -80,6 +80,21 @@ def test_large_batch_matches_the_oracle_per_scene():
                 oracle.fluids_step(c, fp, 2, st)
             m.update(1)
             _compare(m, sc, before, fp)
+
+
+def test_batch_over_1m_particles_matches_the_oracle_per_scene():
+    """A batch of more than 2^20 particles: its full sweeps record hits through the bit-mask
+    filter."""
+    # Wide scenes (x extent 2): their lattices stay below 0.7 of the box height.
+    sc, m = _batch(count=6, seed=13, n_range=(180000, 220000), aspect_range=(2.0, 2.0))
+    with m:
+        assert m.nbParticles() >= 1 << 20
+        fp = sc["fluid_params"]
+        before = _scene_states(m, sc)
+        for c, off, cnt, st in before:
+            oracle.fluids_step(c, fp, 2, st)
+        m.update(1)
+        _compare(m, sc, before, fp)
 
 
 def test_batch_scene_equals_the_same_scene_alone():
