@@ -318,6 +318,21 @@ int rtp_radix_sort_scratch_bytes(uint32_t n, uint32_t keyBits, size_t* bytes);
 int rtp_radix_sort(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits,
                    uint32_t* d_keys_out, uint32_t* d_perm_out,
                    void* d_scratch, size_t scratch_bytes, void* stream);
+/* One stable scatter pass of the LSD radix sort with caller-supplied digit offsets (the pass
+ * RadixSort::sort runs per digit, radixSort.cl:147-168 `reorder`, with the histogram and scan of
+ * radixSort.cl:19-141 done by the caller).  Keys are split in tiles of RTP_SORT_TILE; digit
+ * d = (key >> shift) & (2^bits - 1), bits 1..9.  d_tile_offsets[t * RTP_SORT_BINS + d] = number of
+ * keys with digit d in tiles < t; d_digit_totals[d] = number of keys with digit d.  Keys go to
+ * keys_out in digit order, stable, perm_out (optional) receives their input indices.  Offsets
+ * inconsistent with the keys would place an element outside [0, n): such an element is not
+ * written and 1 is ORed into *d_fault (device memory).  Inside a model step the same guard raises
+ * the handle's fault word, which rtp_synchronize, rtp_download, rtp_update_host and
+ * rtp_time_steps report as RTP_ERR_CUDA. */
+#define RTP_SORT_TILE 2048u
+#define RTP_SORT_BINS 512u
+int rtp_radix_sort_pass(const uint32_t* d_keys_in, uint32_t n, uint32_t shift, uint32_t bits,
+                        const uint32_t* d_tile_offsets, const uint32_t* d_digit_totals, uint32_t* d_keys_out,
+                        uint32_t* d_perm_out, uint32_t* d_fault, void* stream);
 /* Cell table from n sorted keys, in the reference's format: uint2 per cell,
  * (start, end) inclusive, empty = (1, 0), capped at maxPartsInCell. */
 int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_keys,
@@ -333,8 +348,9 @@ int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_k
  *  - at most RTP_NOALLOC_SORT_MAX_KEYS keys; more returns RTP_ERR_CAPACITY, nothing runs;
  *  - the array (RTP_NOALLOC_SORT_SCRATCH_BYTES) is held by every GPU that loads the library
  *    until the process exits;
- *  - the first call on a device looks up the array's address on that device (make that
- *    first call before any stream capture);
+ *  - the first call in each CUDA context (per device; again after cudaDeviceReset re-creates
+ *    the primary context, or from another context on the same device) looks up the array's
+ *    address in that context: make that call before any stream capture;
  *  - every call shares the array, so calls that overlap on the GPU race: order them on one
  *    stream or synchronise between them. */
 #define RTP_NOALLOC_SORT_MAX_KEYS 262144u

@@ -74,6 +74,7 @@ _SIGS = {
     "rtp_radix_sort": [P, U32, U32, P, P, P, C.c_size_t, P],
     "rtp_build_cell_table": [C.POINTER(abi.GridConstants), P, U32, P, P],
     "rtp_radix_sort_noalloc": [P, U32, U32, P, P, P],
+    "rtp_radix_sort_pass": [P, U32, U32, U32, P, P, P, P, P, P],
     "rtp_set_warm_start": [P, C.POINTER(abi.Mlp), C.POINTER(abi.WarmStartConfig)],
     "rtp_enable_solver_stats": [P, C.c_int],
     "rtp_get_solver_stats": [P, C.POINTER(abi.SolverStats)],

@@ -351,9 +351,11 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
       src = ks.y;
       pos = s_base[(kk >> shift) & mask] + j;  // wraps back into [0, n) for a consistent histogram
     }
-    // A consistent histogram gives pos < n; the guard keeps an inconsistent one (a bug)
-    // from writing out of bounds: the element is dropped and the parity tests fail.
+    // A consistent histogram gives pos < n.  An inconsistent one (a bug, or offsets supplied
+    // from outside) must not write out of bounds: the element is not written and the fault
+    // word is raised, which the handle reports at its next synchronisation.
     const bool ok = valid && pos < n;
+    if (valid && !ok && g.fault) atomicOr(g.fault, 1u);
     if (ok) {
       keys_out[pos] = kk;
       if (!LAST) {
@@ -456,6 +458,21 @@ int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L) {
   RTP_CUDA(cudaMemsetAsync(s.hist + per, 0, sizeof(uint32_t) * per * (p.passes - 1), L.stream));
   L.end("sort_clear");
   return RTP_OK;
+}
+
+static_assert(RTP_SORT_TILE == kSortTile && RTP_SORT_BINS == kMaxBins, "keep rtp.h in step with the sort tiles");
+
+int launch_sort_one_pass(const uint32_t* keys_in, uint32_t n, int shift, int bits, const uint32_t* hist,
+                         const uint32_t* totals, uint32_t* keys_out, const GatherList& g, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+  if (tiles <= kWidePassTiles)
+    launch(L, k_sort_pass<true, 16>, dim3(tiles), dim3(512), keys_in, (const uint32_t*)nullptr, n, shift, bits, hist,
+           totals, keys_out, (uint32_t*)nullptr, (uint32_t*)nullptr, 0, 0, g);
+  else
+    launch(L, k_sort_pass<true, 8>, dim3(tiles), dim3(256), keys_in, (const uint32_t*)nullptr, n, shift, bits, hist,
+           totals, keys_out, (uint32_t*)nullptr, (uint32_t*)nullptr, 0, 0, g);
+  return check_launch("k_sort_pass");
 }
 
 int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* keys_out, const SortScratch& s,
@@ -572,6 +589,22 @@ int rtp_radix_sort(const uint32_t* d_keys_in, uint32_t n, uint32_t keyBits, uint
   GatherList g;
   g.perm = d_perm_out;
   return launch_sort_passes(p, d_keys_in, d_keys_out, s, g, L);
+}
+
+int rtp_radix_sort_pass(const uint32_t* d_keys_in, uint32_t n, uint32_t shift, uint32_t bits,
+                        const uint32_t* d_tile_offsets, const uint32_t* d_digit_totals, uint32_t* d_keys_out,
+                        uint32_t* d_perm_out, uint32_t* d_fault, void* stream) {
+  if (bits < 1 || bits > (uint32_t)kMaxRadixBits || shift > 31)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort_pass: bits must be 1..9 and shift < 32");
+  if (n == 0) return RTP_OK;
+  if (!d_keys_in || !d_keys_out || !d_tile_offsets || !d_digit_totals || !d_fault)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_radix_sort_pass: null pointer");
+  Launcher L;
+  L.stream = (cudaStream_t)stream;
+  GatherList g;
+  g.perm = d_perm_out;
+  g.fault = d_fault;
+  return launch_sort_one_pass(d_keys_in, n, (int)shift, (int)bits, d_tile_offsets, d_digit_totals, d_keys_out, g, L);
 }
 
 int rtp_build_cell_table(const rtp_grid_constants* c, const uint32_t* d_sorted_keys, uint32_t n, uint32_t* d_table2,

@@ -88,6 +88,9 @@ struct GatherList {
   int n4 = 0;
   int n1 = 0;
   uint32_t* perm = nullptr;  // optional: write the permutation
+  // Optional fault word: a pass that computes a position outside [0, n) for an element (a digit
+  // offset table inconsistent with the keys) does not write it and ORs 1 into *fault instead.
+  uint32_t* fault = nullptr;
 };
 
 // Histogram of digit 0 of `keys` per tile (used when keys come from outside a model step).
@@ -98,6 +101,10 @@ int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* key
                        const GatherList& g, Launcher& L);
 // Zero the histogram area (the first pass reads it after the producer kernel filled it).
 int launch_sort_clear(const SortPlan& p, const SortScratch& s, Launcher& L);
+// One scatter pass over all tiles with caller-supplied digit offsets: hist = exclusive prefix
+// over tiles per digit ([tile][kMaxBins]), totals = per-digit totals (kMaxBins).
+int launch_sort_one_pass(const uint32_t* keys_in, uint32_t n, int shift, int bits, const uint32_t* hist,
+                         const uint32_t* totals, uint32_t* keys_out, const GatherList& g, Launcher& L);
 
 // Cell table in the internal [begin, endExcl) encoding from sorted keys (sceneOf: the scene
 // of every slot of a batch, or nullptr).

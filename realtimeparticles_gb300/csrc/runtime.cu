@@ -159,6 +159,10 @@ struct Handle {
   uint32_t* mHist = nullptr;
   PairList pairs{};
   std::vector<void*> allocs;
+  // Sort fault word in mapped pinned memory: the sort passes raise it (never in a correct
+  // run); the calls that synchronise with the stream read it and report it.
+  uint32_t* faultHost = nullptr;
+  uint32_t* faultDev = nullptr;
 
   // Graph executor.
   cudaGraphExec_t graph = nullptr;
@@ -304,6 +308,9 @@ static int alloc_buffers(Handle* h) {
   RTP_TRY(dalloc(h, &h->tableRef, h->gc.numCells));
   RTP_TRY(dalloc(h, &h->mAcc, 4));
   RTP_TRY(dalloc(h, &h->mHist, 80));
+  RTP_CUDA(cudaHostAlloc((void**)&h->faultHost, sizeof(uint32_t), cudaHostAllocMapped));
+  *h->faultHost = 0;
+  RTP_CUDA(cudaHostGetDevicePointer((void**)&h->faultDev, h->faultHost, 0));
   if (h->model == RTP_MODEL_BOIDS) {
     RTP_TRY(dalloc(h, &h->acc, M));
   } else {
@@ -363,6 +370,7 @@ static void free_handle(Handle* h) {
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->targetHost) cudaFreeHost(h->targetHost);
+  if (h->faultHost) cudaFreeHost(h->faultHost);
   if (h->targetUp) cudaEventDestroy(h->targetUp);
   delete h;
 }
@@ -414,6 +422,7 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
   const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
   RTP_TRY(fluid_presort(g, fk, h->pos, h->vel, n, h->predTmp, h->ss.keysA, plan, h->ss.hist, clampOut, L, zero, h->io));
   GatherList gl;
+  gl.fault = h->faultDev;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
   gl.src4[1] = h->vel;
@@ -596,6 +605,7 @@ static int record_boids_step(Handle* h, Launcher& L) {
   }
   RTP_TRY(boids_presort(g, h->pos, h->vel, n, h->ss.keysA, plan, h->ss.hist, L, zero, tk, h->io));
   GatherList gl;
+  gl.fault = h->faultDev;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
   gl.src4[1] = h->vel;
@@ -660,6 +670,7 @@ int record_clouds_step(Handle* h, Launcher& L) {
                         h->ss.keysA, plan, h->ss.hist, L, zero));
   // Clouds.cpp:543.
   GatherList gl;
+  gl.fault = h->faultDev;
   gl.src4[0] = h->pos;
   gl.dst4[0] = h->posS;
   gl.src4[1] = h->vel;
@@ -1163,6 +1174,18 @@ static int run_steps(Handle* h, uint32_t nsteps) {
 
 static Handle* H(void* p) { return reinterpret_cast<Handle*>(p); }
 
+// After a synchronisation with the handle's stream: a raised sort fault word becomes an error
+// (and is cleared).  No correct run raises it; it stands for state the sort could not write.
+static int check_fault(Handle* h) {
+  if (!h->faultHost) return RTP_OK;
+  volatile uint32_t* f = h->faultHost;
+  if (*f == 0) return RTP_OK;
+  *f = 0;
+  return fail(RTP_ERR_CUDA,
+              "radix sort: digit offsets inconsistent with the keys placed elements outside the sorted range; they "
+              "were not written and the model state is not valid");
+}
+
 }  // namespace rtp
 
 using namespace rtp;
@@ -1575,7 +1598,7 @@ int rtp_download(void* handle, int buffer, void* host, uint64_t count) {
   }
   RTP_CUDA(cudaMemcpyAsync(host, d, elem * count, cudaMemcpyDeviceToHost, h->stream));
   RTP_CUDA(cudaStreamSynchronize(h->stream));
-  return RTP_OK;
+  return check_fault(h);
   RTP_GUARD_END
 }
 
@@ -1618,7 +1641,7 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
       RTP_CUDA(cudaGraphLaunch(exec, h->stream));
       h->hasStep = true;
       RTP_CUDA(cudaStreamSynchronize(h->stream));
-      return RTP_OK;
+      return check_fault(h);
     }
   }
   if (posIn && bytes) {
@@ -1630,14 +1653,14 @@ int rtp_update_host(void* handle, const void* posIn, const void* velIn, uint64_t
   if (posOut && bytes) RTP_CUDA(cudaMemcpyAsync(posOut, h->pos, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (velOut && bytes) RTP_CUDA(cudaMemcpyAsync(velOut, h->vel, bytes, cudaMemcpyDeviceToHost, h->stream));
   RTP_CUDA(cudaStreamSynchronize(h->stream));
-  return RTP_OK;
+  return check_fault(h);
   RTP_GUARD_END
 }
 
 int rtp_synchronize(void* handle) {
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
   RTP_CUDA(cudaStreamSynchronize(H(handle)->stream));
-  return RTP_OK;
+  return check_fault(H(handle));
 }
 
 int rtp_enable_profiling(void* handle, int enable) {
@@ -1704,7 +1727,7 @@ int rtp_time_steps(void* handle, uint32_t nsteps, uint64_t flush_bytes, double* 
     if (h->graphProfiled) RTP_TRY(collect_profile(h));
   }
   h->hasStep = true;
-  return RTP_OK;
+  return check_fault(h);
   RTP_GUARD_END
 }
 
@@ -1891,6 +1914,7 @@ int rtp_fill_camera_order(void* handle, const float cameraPos[3]) {
   RTP_TRY(launch_sort_clear(plan, h->camSS, L));
   RTP_TRY(launch_sort_histogram(plan, h->camDist, h->camSS, L));
   GatherList gl;
+  gl.fault = h->faultDev;
   gl.perm = h->drawOrder;
   RTP_TRY(launch_sort_passes(plan, h->camDist, h->camSorted, h->camSS, gl, L));
   RTP_CUDA(cudaStreamSynchronize(h->stream));

@@ -13,6 +13,8 @@
 // GPU (different streams, or host threads without ordering) race and must be serialised
 // by the caller.  The array keeps the last call's contents; each call clears the
 // histogram area it accumulates into before using it.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "rtp_internal.hpp"
@@ -37,24 +39,74 @@ static_assert(kScratchBytes == RTP_NOALLOC_SORT_SCRATCH_BYTES, "keep rtp.h in st
 static __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 
 // Host code cannot use g_sort_scratch's name as a device address: the address is looked up
-// once per device, with that device current.
+// with the device current and cached per device together with the identity of the context it
+// was looked up in (cuCtxGetId: unique for the life of the process).  A call from another
+// context on that device, or after cudaDeviceReset re-created the primary context, finds a
+// different identity and looks the address up again (that call must not be under stream
+// capture).  The driver entry points are resolved through the runtime, so the library does
+// not link libcuda.
 constexpr int kMaxDevices = 128;
+struct ScratchAddress {
+  unsigned long long ctxId;
+  void* ptr;
+};
 std::mutex g_mutex;
-void* g_scratch_address[kMaxDevices] = {};
+ScratchAddress g_scratch_address[kMaxDevices] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+int resolve_driver_entry_points() {  // caller holds g_mutex
+  if (g_ctx_get_current && g_ctx_get_id) return RTP_OK;
+  void* f0 = nullptr;
+  void* f1 = nullptr;
+  cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = cudaDriverEntryPointSymbolNotFound;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDriverEntryPointByVersion(cuCtxGetCurrent)");
+  e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDriverEntryPointByVersion(cuCtxGetId)");
+  if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+    return fail(RTP_ERR_NOT_SUPPORTED, "rtp_radix_sort_noalloc: driver lacks cuCtxGetCurrent / cuCtxGetId");
+  g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+  g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+  return RTP_OK;
+}
+
+// Identity of the context current on the calling thread; with none current yet, the device's
+// primary context is made current first (cudaSetDevice initialises it).
+int current_context_id(int dev, unsigned long long* id) {  // caller holds g_mutex
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return fail(RTP_ERR_CUDA, "rtp_radix_sort_noalloc: cuCtxGetCurrent failed");
+  if (!ctx) {
+    RTP_CUDA(cudaSetDevice(dev));
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx)
+      return fail(RTP_ERR_CUDA, "rtp_radix_sort_noalloc: no CUDA context is current");
+  }
+  if (g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return fail(RTP_ERR_CUDA, "rtp_radix_sort_noalloc: cuCtxGetId failed");
+  return RTP_OK;
+}
 
 int scratch_on_current_device(void** out) {
   int dev = -1;
   RTP_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_radix_sort_noalloc: device ordinal too large");
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_address[dev]) {
+  int rc = resolve_driver_entry_points();
+  if (rc) return rc;
+  unsigned long long id = 0;
+  rc = current_context_id(dev, &id);
+  if (rc) return rc;
+  ScratchAddress& a = g_scratch_address[dev];
+  if (!a.ptr || a.ctxId != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_sort_scratch)");
     if (!p) return fail(RTP_ERR_CUDA, "rtp_radix_sort_noalloc: null scratch address");
-    g_scratch_address[dev] = p;
+    a.ptr = p;
+    a.ctxId = id;
   }
-  *out = g_scratch_address[dev];
+  *out = a.ptr;
   return RTP_OK;
 }
 

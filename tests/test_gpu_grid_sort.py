@@ -128,3 +128,63 @@ def test_cell_table_bit_exact(torch, oracle_mod, case):
     got = t.cpu().numpy().view(np.uint32)
     ref = oracle_mod.cell_table(c, sk)
     assert np.array_equal(got, ref)
+
+
+def _pass_offsets(keys, shift, bits, tile=2048, bins=512):
+    """Per-tile exclusive prefix of each digit over the tiles before it, and digit totals."""
+    n = keys.shape[0]
+    tiles = (n + tile - 1) // tile
+    d = (keys >> np.uint32(shift)) & np.uint32((1 << bits) - 1)
+    counts = np.zeros((tiles, bins), np.uint32)
+    for t in range(tiles):
+        counts[t, :] = np.bincount(d[t * tile:(t + 1) * tile], minlength=bins)[:bins]
+    prefix = np.zeros_like(counts)
+    prefix[1:] = np.cumsum(counts, axis=0)[:-1]
+    return prefix, counts.sum(axis=0).astype(np.uint32)
+
+
+def _run_pass(torch, keys, shift, bits, prefix, totals):
+    n = keys.shape[0]
+    kin = torch.from_numpy(keys.view(np.int32)).cuda()
+    kout = torch.full_like(kin, -1)
+    perm = torch.full_like(kin, -1)
+    hp = torch.from_numpy(prefix.view(np.int32).ravel().copy()).cuda()
+    ht = torch.from_numpy(totals.view(np.int32).copy()).cuda()
+    fault = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("rtp_radix_sort_pass", _ptr(kin), n, shift, bits, _ptr(hp), _ptr(ht), _ptr(kout), _ptr(perm),
+              _ptr(fault), None)
+    torch.cuda.synchronize()
+    return kout.cpu().numpy().view(np.uint32), perm.cpu().numpy().view(np.uint32), int(fault.item())
+
+
+def test_sort_pass_with_consistent_offsets(torch):
+    rng = np.random.default_rng(5)
+    keys = rng.integers(0, 1 << 20, 5000, dtype=np.uint64).astype(np.uint32)
+    prefix, totals = _pass_offsets(keys, 4, 9)
+    kout, perm, fault = _run_pass(torch, keys, 4, 9, prefix, totals)
+    ref = np.argsort((keys >> 4) & 511, kind="stable")
+    assert fault == 0
+    assert np.array_equal(perm, ref)
+    assert np.array_equal(kout, keys[ref])
+
+
+def test_sort_pass_flags_inconsistent_offsets(torch):
+    """Digit offsets that do not match the keys (a histogram built wrongly) would place elements
+    past the end: the pass writes none of them and raises the fault word instead of writing out
+    of bounds or dropping them silently (a model step reports the same word as RTP_ERR_CUDA)."""
+    rng = np.random.default_rng(6)
+    n = 5000
+    keys = rng.integers(0, 512, n, dtype=np.uint64).astype(np.uint32)
+    keys[-1] = 511  # the largest digit occurs in the last tile: its run ends the output
+    prefix, totals = _pass_offsets(keys, 0, 9)
+    bad = prefix.copy()
+    bad[-1, 511] += 1000  # the last tile's run of digit 511 now starts beyond n
+    kout, perm, fault = _run_pass(torch, keys, 0, 9, bad, totals)
+    assert fault == 1
+    in_last = int(np.count_nonzero(keys[2 * 2048:] == 511))
+    # exactly those elements were not written (their output slots keep the fill value); every
+    # other element is where the consistent pass puts it
+    unwritten = perm == 0xFFFFFFFF
+    assert int(np.count_nonzero(unwritten)) == in_last
+    ref = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm[~unwritten], ref[~unwritten])

@@ -39,10 +39,10 @@ def _sort_allocating(torch, kin, n, bits):
     return kout, perm
 
 
-def _sort_noalloc(torch, kin, n, bits):
+def _sort_noalloc(torch, kin, n, bits, with_perm=True):
     kout = torch.full_like(kin, -1)
-    perm = torch.full_like(kin, -1)
-    _lib.call("rtp_radix_sort_noalloc", _ptr(kin), n, bits, _ptr(kout), _ptr(perm), None)
+    perm = torch.full_like(kin, -1) if with_perm else None
+    _lib.call("rtp_radix_sort_noalloc", _ptr(kin), n, bits, _ptr(kout), _ptr(perm) if with_perm else None, None)
     return kout, perm
 
 
@@ -72,3 +72,20 @@ def test_noalloc_sort_rejects_sizes_beyond_its_limit(torch):
     assert rc == abi.ERR_CAPACITY
     assert "262144" in _lib.last_error()
     assert bool((kout == -1).all()), "nothing may run when the size is refused"
+
+
+@pytest.mark.parametrize("n,bits,with_perm", [(1000, 9, True), (1000, 9, False), (3, 0, False), (5000, 17, False)])
+def test_noalloc_sort_other_plans(torch, n, bits, with_perm):
+    """The single-pass plan (keyBits <= 9: nothing to clear), keyBits = 0 and calls without a
+    permutation output give the allocating sort's keys and a stable order."""
+    rng = np.random.default_rng(n + bits)
+    keys = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+    kin = torch.from_numpy(keys.view(np.int32)).cuda()
+    ka, pa = _sort_allocating(torch, kin, n, bits)
+    kb, pb = _sort_noalloc(torch, kin, n, bits, with_perm)
+    torch.cuda.synchronize()
+    assert torch.equal(ka, kb)
+    assert np.array_equal(kb.cpu().numpy().view(np.uint32), np.sort(keys, kind="stable"))
+    if with_perm:
+        assert torch.equal(pa, pb)
+        assert np.array_equal(pb.cpu().numpy().view(np.uint32), np.argsort(keys, kind="stable"))
