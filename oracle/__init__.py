@@ -366,6 +366,9 @@ def ref_lib():
         L.ref_fill_color_float.argtypes = [G, P, C.c_uint32, C.c_float, C.c_float, P]
         L.ref_fill_camera_dist.argtypes = [G, P, C.c_uint32, C.c_uint32, P, P]
         L.ref_fill_grid_detector.argtypes = [G, P, C.c_uint32, P]
+        if hasattr(L, "ref_generate_3d_grid"):
+            L.ref_generate_3d_grid.argtypes = [C.c_int, P, P, P, P]
+            L.ref_generate_2d_grid_yz.argtypes = [C.c_int, P, P, P, P]
         _REF = L
     return _REF
 
@@ -429,3 +432,27 @@ def ref_side_outputs(c, fp, density, q, vmin, vmax, pos, n, cam):
     det = np.empty((c.numCells, 8), np.float32)
     L.ref_fill_grid_detector(C.byref(c), _p(pos), int(n), _p(det))
     return col, colf, dist, det
+
+
+def ref_geometry_available():
+    return ref_available() and hasattr(ref_lib(), "ref_generate_3d_grid")
+
+
+def ref_generate_3d_grid(shape, res, start, end):
+    """The reference's Geometry::Generate3DGrid (uniform); shape "box" or "sphere"."""
+    res = np.ascontiguousarray(res, dtype=np.int32)
+    s = np.ascontiguousarray(start, dtype=np.float32)
+    e = np.ascontiguousarray(end, dtype=np.float32)
+    out = np.zeros((int(np.prod(res)), 3), np.float32)
+    k = ref_lib().ref_generate_3d_grid(1 if shape == "sphere" else 0, _p(res), _p(s), _p(e), _p(out))
+    return out[:k]
+
+
+def ref_generate_2d_grid_yz(shape, res, start, end):
+    """The reference's Geometry::Generate2DGrid in the YZ plane (uniform); shape "rect" or "circle"."""
+    res = np.ascontiguousarray(res, dtype=np.int32)
+    s = np.ascontiguousarray(start, dtype=np.float32)
+    e = np.ascontiguousarray(end, dtype=np.float32)
+    out = np.zeros((int(np.prod(res)), 3), np.float32)
+    k = ref_lib().ref_generate_2d_grid_yz(1 if shape == "circle" else 0, _p(res), _p(s), _p(e), _p(out))
+    return out[:k]

@@ -3,8 +3,8 @@
 of axoloto/RealTimeParticles) and its Perlin noise (physics/utils/PerlinNoise.cpp) compiled
 for the CPU, to check the oracle against them.
 
-TEST INFRASTRUCTURE ONLY.  When the reference checkout is present (REFERENCE_DIR, default
-/root/reference), each OpenCL program is assembled from its .cl files in the order the
+TEST INFRASTRUCTURE ONLY.  When the reference checkout is present (REFERENCE_DIR, default: a
+checkout named `reference` next to this repository), each OpenCL program is assembled from its .cl files in the order the
 reference's createProgram uses (Fluids.cpp:123, Boids.cpp:117, Clouds.cpp:157), the OpenCL
 vector literals "(float4)(a, b, ...)" are rewritten to "make_float4(a, b, ...)" (the only
 change: C++ would read them as comma expressions), and the result is written to
@@ -20,7 +20,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-REF = os.environ.get("REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("REFERENCE_DIR", os.path.join(os.path.dirname(os.path.dirname(ORACLE)), "reference"))
 KDIR = os.path.join(REF, "physics", "ocl", "kernels")
 
 PROGRAMS = {
@@ -77,6 +77,15 @@ def generate():
                 os.path.join(REF, "physics", "utils", "PerlinNoise.hpp"),
                 os.path.join(REF, "utils", "Math.hpp")):
         open(os.path.join(pdir, os.path.basename(src)), "w").write(open(src).read())
+    # Geometry's reset-case lattices (utils/Geometry.cpp) with the headers it includes, as they
+    # are, except Logging.hpp (spdlog, absent): a two-line stand-in that drops the log calls.
+    gdir = os.path.join(OUT, "geometry")
+    os.makedirs(gdir, exist_ok=True)
+    for src in (os.path.join(REF, "utils", "Geometry.cpp"), os.path.join(REF, "utils", "Geometry.hpp"),
+                os.path.join(REF, "utils", "Math.hpp")):
+        open(os.path.join(gdir, os.path.basename(src)), "w").write(open(src).read())
+    open(os.path.join(gdir, "Logging.hpp"), "w").write(
+        "#pragma once\n#define LOG_ERROR(...) ((void)0)\n")
 
 
 def compile_lib():
@@ -86,7 +95,8 @@ def compile_lib():
     out = os.path.join(OUT, "libref.so")
     # The driver includes the generated programs (one namespace each) into one unit.
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-w",
-           "-I", OUT, "-shared", "-o", out, os.path.join(HERE, "ref_driver.cpp")]
+           "-I", OUT, "-shared", "-o", out, os.path.join(HERE, "ref_driver.cpp"),
+           os.path.join(HERE, "ref_geometry.cpp")]
     subprocess.run(cmd, check=True)
     return True
 
