@@ -919,7 +919,11 @@ static int init_case(Handle* h) {
   if (n > h->maxN) return fail(RTP_ERR_CAPACITY, "rtp_reset: the case needs more than maxNbParticles");
   const float inf = INFINITY;
   std::vector<float4> pos(h->maxN, make_float4(inf, inf, inf, 0.0f)), vel(h->maxN, make_float4(0.f, 0.f, 0.f, 0.f));
-  for (size_t i = 0; i < verts.size() && i < n; ++i) pos[i] = make_float4(verts[i].x, verts[i].y, verts[i].z, 0.0f);
+  // Every generated vertex is written, as the reference's std::transform over gridVerts does
+  // (Fluids.cpp:383-386): the 2D Drop case generates 512 + 64 x 128 vertices but counts
+  // 512 + 4096 particles, so its buffer holds finite positions past the particle count.
+  for (size_t i = 0; i < verts.size() && i < h->maxN; ++i)
+    pos[i] = make_float4(verts[i].x, verts[i].y, verts[i].z, 0.0f);
   if (h->model == RTP_MODEL_BOIDS) vel = pos;  // Boids.cpp:317-318: vel initialised from the position buffer
   std::vector<uint32_t> id(h->maxN);
   for (size_t i = 0; i < id.size(); ++i) id[i] = (uint32_t)i;

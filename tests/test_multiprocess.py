@@ -37,7 +37,7 @@ def _worker(rank, world, port, out):
 def test_bench_replicas_take_max_over_ranks():
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
@@ -71,7 +71,7 @@ def test_batch_shards_by_scene():
     particles of all ranks (no collective on the data path, one all-reduce of the count)."""
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_batch_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
