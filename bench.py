@@ -331,8 +331,8 @@ def run_reference(args):
     return 0
 
 
-PLAIN_ITERS = (1, 2, 3, 4, 6, 8, 12, 16, 24)
-WARM_EXTRA = (0, 1, 2, 3)
+PLAIN_ITERS = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48)
+WARM_EXTRA = (0, 1, 2, 3, 5, 7, 11)
 
 
 def _timed_config(lattice, iters, net, extra, tol, steps, warmup):
@@ -365,45 +365,70 @@ def _plain_at(curve, err):
     return None
 
 
+WS_TRAIN_SEEDS = (1, 2, 3, 4)
+WS_TRAIN_STEPS = 300
+WS_EVAL_WARMUP = 100
+WS_EVAL_STEPS = 100
+
+
 def warm_start_study(w, steps, warmup):
-    from realtimeparticles_gb300 import warmstart
+    """The learned warm start against the plain solver at equal error.  The network is trained
+    through the solve on the rollouts of other seeded scenes (WS_TRAIN_STEPS steps each, warm
+    start + 1 extra iteration, one AdamW step per step); every configuration then runs the
+    seed-0 scene for WS_EVAL_STEPS device-timed steps after WS_EVAL_WARMUP warm-up steps (the
+    dam has collapsed by then: errors of the first steps say little), L2 flushed before every
+    step.  The plain solver's throughput at a configuration's error is log-log interpolated on
+    the measured plain curve."""
+    from realtimeparticles_gb300 import model, warmstart
     lattice = w["lattice"]
     n = int(np.prod(lattice))
     t0 = time.perf_counter()
-    feats, targets = warmstart.generate_samples(seeds=range(1, 9), lattice=lattice, steps=400, record_every=25,
-                                                stride=8, reference_iterations=8)
+    net, losses = None, []
+    for seed in WS_TRAIN_SEEDS:
+        sc = scenes.dam_break(lattice=lattice, seed=seed)
+        with model.Fluids(sc["model_params"]) as m:
+            m.setFluidParams(sc["fluid_params"])
+            m.setJacobiIterations(2)
+            m.upload(abi.BUF_POS, sc["pos"])
+            m.upload(abi.BUF_VEL, sc["vel"])
+            net, hist = warmstart.train_rollout(m, WS_TRAIN_STEPS, extra_iterations=1, net=net, seed=0)
+            losses += hist
     t1 = time.perf_counter()
-    net, hist = warmstart.train(feats, targets, epochs=16, batch=8192, learning_rate=2e-3, seed=0)
-    t2 = time.perf_counter()
-    out = {"training": {"samples": int(feats.shape[0]), "reference_iterations": 8, "runs": 8,
-                        "epochs": len(hist), "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
-                        "sample_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2)}}
-    del feats, targets
+    out = {"training": {"method": "through the solve on the model's own rollout (one AdamW step per step)",
+                        "scenes": len(WS_TRAIN_SEEDS), "steps": len(losses), "particles": n,
+                        "extra_iterations": 1, "train_seconds": round(t1 - t0, 2)},
+           "eval": {"warmup_steps": WS_EVAL_WARMUP, "timed_steps": WS_EVAL_STEPS}}
     plain, curve = [], []
     for it in PLAIN_ITERS:
-        ms, err, _ = _timed_config(lattice, it, None, 0, 0.0, steps, warmup)
+        ms, err, _ = _timed_config(lattice, it, None, 0, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
         v = n / (ms / 1000.0)
         plain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err})
         curve.append((err, v))
     learned = []
     for e in WARM_EXTRA:
-        ms, err, rr = _timed_config(lattice, 8, net, e, 0.0, steps, warmup)
+        ms, err, rr = _timed_config(lattice, 3, net, e, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
         v = n / (ms / 1000.0)
         ref = _plain_at(curve, err)
         learned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
                         "mean_density_error": err, "plain_at_equal_error": ref,
                         "speedup_at_equal_error": (v / ref) if ref else None})
-    # The guard: tolerance = the plain 3-iteration error; reruns use 3 iterations.
-    tol = next(p["mean_density_error"] for p in plain if p["iterations"] == 3)
-    ms, err, rr = _timed_config(lattice, 3, net, 1, tol, steps, warmup)
-    guarded = {"extra_iterations": 1, "guard_tolerance": tol, "plain_iterations": 3,
+    # The guard on the warm start + 2 extra iterations (three in all): a step whose
+    # solver-output error exceeds 1.25 x the plain 3-iteration mean reruns with the plain 3.
+    e3 = next(p["mean_density_error"] for p in plain if p["iterations"] == 3)
+    tol = 1.25 * e3
+    ms, err, rr = _timed_config(lattice, 3, net, 2, tol, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+    guarded = {"extra_iterations": 2, "guard_tolerance": tol, "plain_iterations": 3,
                "particle_steps_per_s": n / (ms / 1000.0), "mean_density_error": err, "reruns": rr,
-               "steps": steps}
-    speedups = [x["speedup_at_equal_error"] for x in learned if x["speedup_at_equal_error"]]
+               "steps": WS_EVAL_STEPS}
+
+    def best(cond):
+        v = [x["speedup_at_equal_error"] for x in learned if x["speedup_at_equal_error"] and cond(x)]
+        return max(v) if v else None
+
     out.update(plain=plain, learned=learned, guarded=guarded,
-               best_speedup_at_equal_error=max(speedups) if speedups else None,
-               note="speed-up < 1 or null: the warm start does not reach the plain solver's "
-                    "throughput at its own error on this workload")
+               best_speedup_at_equal_error=best(lambda x: True),
+               best_speedup_at_or_below_plain3_error=best(lambda x: x["mean_density_error"] <= e3),
+               best_speedup_at_error_le_1pct=best(lambda x: x["mean_density_error"] <= 0.01))
     return out
 
 

@@ -391,9 +391,13 @@ int rtp_fill_grid_detector(void* handle);
  *       with lo, hi the fld_applyBoundaryCondition bounds
  *   10 lambda_i of the plain first iteration
  *   11 |v_i| dt / h
- * Outputs: lambda_i, to use in place of the first iteration's lambda (trained on the sum of
- * lambda over the reference iterations), and a residual displacement r_i (3).  The first
- * correction is x_i += dp_i(lambda) + r_i, then `extraIterations` plain Jacobi iterations run.
+ * Output: the network's value y_i (output 0 times outScale[0]; outputs 1-3 are not used by the
+ * solve) sets a relaxation of the plain first-iteration lambda (feature 10):
+ *   omega_i = 1 + tanh(y_i) * (2 if y_i > 0 else 1), in (0, 3);  lambda_i <- omega_i lambda_i.
+ * y = 0 gives omega = 1 exactly, so a network whose output layer is zero is the plain solver bit
+ * for bit.  The first correction is x_i += dp_i(omega lambda) (fld_computeConstraintCorrection
+ * with the relaxed lambdas, Fluids.cpp:433-434), then `extraIterations` Jacobi iterations, plain
+ * or (relaxAllIterations) relaxed by the same omega.
  * Guard: the solver output's mean |rho_i/rho0 - 1| is measured in the vorticity sweep; a
  * step above `guardTolerance` reruns from the same predicted positions with the plain
  * iteration count (rtp_set_jacobi_iterations) before vorticity confinement and XSPH. */
@@ -416,7 +420,8 @@ typedef struct rtp_warm_start_config {
   uint32_t enabled;         /* 0: plain solver */
   uint32_t extraIterations; /* plain Jacobi iterations after the warm-started one */
   float guardTolerance;     /* mean |rho/rho0 - 1| that triggers a plain rerun; <= 0: no guard */
-  uint32_t reserved;
+  uint32_t relaxAllIterations; /* != 0: the extra iterations' lambdas are relaxed by the same
+                                  per-particle omega (set once per step by the network) */
 } rtp_warm_start_config;
 
 typedef struct rtp_solver_stats {
@@ -434,7 +439,7 @@ int rtp_enable_solver_stats(void* handle, int enable);
 int rtp_get_solver_stats(void* handle, rtp_solver_stats* out);
 int rtp_reset_solver_stats(void* handle);
 
-/* Training data: runs one plain step with `referenceIterations` Jacobi iterations (the
+/* Regression data: runs one plain step with `referenceIterations` Jacobi iterations (the
  * simulation advances) and writes one sample for each cell-sorted particle index
  * phase, phase + stride, ... < n: its RTP_MLP_IN raw features (as above) into
  * d_features[k][RTP_MLP_IN] and its targets into d_targets[k][RTP_MLP_OUT]: the sum of
@@ -461,12 +466,37 @@ typedef struct rtp_train_config {
  * cfg->epochs floats, may be NULL) receives each epoch's mean loss. */
 int rtp_train_warm_start(const float* d_features, const float* d_targets, uint64_t n, const rtp_train_config* cfg,
                          rtp_mlp* net, float* loss_history, void* stream);
+/* Training through the solve.  The loss of a state is the mean squared density constraint after
+ * the warm-started correction:
+ *   x* = the step's predicted positions, clamped (fld_predictPosition, fld_applyBoundaryCondition),
+ *   x' = clamp(x* + dp(omega(y) lambda)) with y = network(features at x*),
+ *   L  = 1/n sum_i (rho_i(x') / rho0 - 1)^2, rho(x') over the 27 cells of the step's table.
+ * rtp_warm_start_loss_grad evaluates L and dL/dy for the handle's current state (it runs the next
+ * step's predict, sort and cell table; the model's positions and velocities are not changed):
+ * d_dy (device, optional) receives dL/dy_i at index = particle id (RTP_BUF_ID), n floats. */
+int rtp_warm_start_loss_grad(void* handle, const rtp_mlp* net, float* d_dy, double* loss);
+/* Trains `net` on the handle's own rollout: each of `steps` steps computes L and its gradient at
+ * that step's predicted positions (the backward sweeps dL/dx', dL/dy, then the network's backward
+ * kernels) and takes one AdamW step (cfg: learningRate cosine-decayed to learningRate *
+ * finalLrFraction over the steps, beta1, beta2, eps, weightDecay, seed; epochs, batch and
+ * lossWeights are not used), then advances the simulation one step with the updated network and
+ * `extraIterations` plain iterations, so it trains on the states the warm-started solver visits.
+ * init != 0 starts a new network: input normalisation from the first step's features,
+ * Xavier-uniform hidden layers (cfg->seed), a zero output layer (omega = 1) and unit output
+ * scales; init == 0 continues from *net.  loss_history (host, `steps` floats, may be NULL)
+ * receives each step's L before its update.  Single fluids scenes only. */
+int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint32_t steps, uint32_t extraIterations,
+                                 int init, rtp_mlp* net, float* loss_history);
 /* Loss and gradient of `net` over n samples (forward and backward kernels of the trainer):
  *   loss = 1/n sum_s sum_o lossWeights[o] * (y_so - t_so / outScale[o])^2,
  * y the network value.  grad gets d loss / d (w1, b1, w2, b2, w3, b3); its normalisation
  * fields are zero. */
 int rtp_mlp_loss_grad(const rtp_mlp* net, const float* lossWeights, const float* d_features, const float* d_targets,
                       uint64_t n, double* loss, rtp_mlp* grad, void* stream);
+/* Backward kernels of the trainer with a given output gradient: grad = d/d(w1, b1, w2, b2, w3, b3)
+ * of sum_s sum_o d_dy[s][o] * y_so (y in network units, rows of RTP_MLP_OUT). */
+int rtp_mlp_backward(const rtp_mlp* net, const float* d_features, const float* d_dy, uint64_t n, rtp_mlp* grad,
+                     void* stream);
 /* Inference kernel of the warm start on stand-alone features: d_out[s][o] = y_so * outScale[o]. */
 int rtp_mlp_forward(const rtp_mlp* net, const float* d_features, uint64_t n, float* d_out, void* stream);
 

@@ -69,7 +69,10 @@ def lib():
         L.or_mlp_loss_grad.argtypes = [C.POINTER(abi.Mlp), P, P, P, C.c_uint64, C.c_int, C.POINTER(C.c_double), P]
         L.or_ws_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.POINTER(abi.Mlp),
                                  C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, P, P, C.POINTER(C.c_double),
-                                 C.POINTER(C.c_int)]
+                                 C.POINTER(C.c_int), C.c_int]
+        L.or_mlp_backward.argtypes = [C.POINTER(abi.Mlp), P, P, C.c_uint64, C.c_int, P]
+        L.or_ws_loss_grad.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.POINTER(abi.Mlp),
+                                      C.c_int, C.c_uint32, P, C.POINTER(C.c_double), P, P]
         L.or_ws_record_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), C.c_uint32,
                                         C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, C.POINTER(C.c_uint32)]
         L.or_fill_fluid_color.argtypes = [P, C.c_uint32, C.c_float, P]
@@ -305,14 +308,44 @@ def mlp_loss_grad(net, loss_weights, feats, targets, emulate=True):
     return loss.value, out
 
 
-def ws_step(c, fp, net, extra_iters, guard_tol, plain_iters, st, lam_tot):
+def mlp_backward(net, feats, dy, emulate=True):
+    """{name: gradient} of sum_s sum_o dy_so y_so (double precision)."""
+    feats = np.ascontiguousarray(feats, dtype=np.float32)
+    dy = np.ascontiguousarray(dy, dtype=np.float32)
+    g = np.empty(5252, np.float64)
+    lib().or_mlp_backward(C.byref(net), _p(feats), _p(dy), feats.shape[0], 1 if emulate else 0, _p(g))
+    out, o = {}, 0
+    for name, shape in MLP_GRAD_SHAPES:
+        size = int(np.prod(shape))
+        out[name] = g[o:o + size].reshape(shape)
+        o += size
+    return out
+
+
+def ws_loss_grad(c, fp, net, st, emulate=True):
+    """(loss, dL/dy by particle id, omega by particle id) of the warm start through the solve at
+    the state st (advanced by the step's presort only)."""
+    n = st["pos"].shape[0]
+    s = _state(st)
+    loss = C.c_double()
+    dy = np.zeros(n, np.float64)
+    om = np.zeros(n, np.float64)
+    rc = lib().or_ws_loss_grad(C.byref(c), C.byref(fp), C.byref(net), 1 if emulate else 0, n, C.byref(s),
+                               C.byref(loss), _p(dy), _p(om))
+    if rc != 0:
+        raise ValueError("or_ws_loss_grad failed: %d" % rc)
+    return loss.value, dy, om
+
+
+def ws_step(c, fp, net, extra_iters, guard_tol, plain_iters, st, lam_tot, relax_all=False):
     """One warm-started step in place; returns (solver-output mean error, rerun flag)."""
     n = st["pos"].shape[0]
     s = _state(st)
     err = C.c_double()
     rr = C.c_int()
     rc = lib().or_ws_step(C.byref(c), C.byref(fp), C.byref(net), int(extra_iters), float(guard_tol),
-                          int(plain_iters), n, C.byref(s), _p(lam_tot), C.byref(err), C.byref(rr))
+                          int(plain_iters), n, C.byref(s), _p(lam_tot), C.byref(err), C.byref(rr),
+                          1 if relax_all else 0)
     if rc != 0:
         raise ValueError("or_ws_step failed: %d" % rc)
     return err.value, bool(rr.value)

@@ -430,7 +430,7 @@ struct Bounds {
 // of the iterations are added to it.
 void fluid_jacobi(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32_t iters, float* pred,
                   const uint32_t* table, uint32_t n, std::vector<float>& density, std::vector<float>& lambda,
-                  float* lamTot) {
+                  float* lamTot, const float* omega = nullptr) {
   const Grid g(c);
   const Bounds b(g);
   std::vector<float> corr(4 * (size_t)n);
@@ -440,6 +440,8 @@ void fluid_jacobi(const rtp_grid_constants* c, const rtp_fluid_params* p, uint32
     for (int64_t i = 0; i < (int64_t)n; ++i) st4(pred, i, clamp4(ld4(pred, i), b.lo, b.hi));
     or_fld_density(c, p, pred, table, n, density.data());
     or_fld_lambda(c, p, pred, density.data(), table, n, lambda.data());
+    if (omega)  // the warm start's relaxation in every iteration (warmstart.cu, relaxAllIterations)
+      for (uint32_t i = 0; i < n; ++i) lambda[i] *= omega[i];
     or_fld_correction(c, p, pred, lambda.data(), table, n, corr.data());
     // fld_correctPosition, fluids.cl:252-258.
     OR_PARALLEL_FOR
@@ -581,6 +583,42 @@ struct NetD {
   }
 };
 
+// The network's relaxation of the plain lambda (warmstart.cu ws_omega): 1 + tanh(y) * (2 for
+// y > 0, 1 otherwise), and its derivative.
+inline float ws_omega(float y) { return 1.0f + std::tanh(y) * (y > 0.0f ? 2.0f : 1.0f); }
+inline double ws_omega_d(double y) { return 1.0 + std::tanh(y) * (y > 0.0 ? 2.0 : 1.0); }
+inline double ws_omega_grad(double y) {
+  const double t = std::tanh(y);
+  return (1.0 - t * t) * (y > 0.0 ? 2.0 : 1.0);
+}
+
+// Backward of one sample through the network: G += d/dparams of sum_o dy[o] y_o (dy already
+// rounded as the GPU stores it when emulating).
+void mlp_backward_one(const NetD& d, const NetD::Act& a, const double dy[4], bool emu, std::vector<double>& G) {
+  const int W1 = 0, B1 = W1 + 768, W2 = B1 + 64, B2 = W2 + 4096, W3 = B2 + 64, B3 = W3 + 256;
+  double dz2[64], dz1[64];
+  for (int h = 0; h < 64; ++h) {
+    double v = 0.0;
+    for (int o = 0; o < 4; ++o) v += dy[o] * d.w3[o * 64 + h];
+    dz2[h] = q(v * gelu_grad(a.z2[h]), emu);
+  }
+  for (int h = 0; h < 64; ++h) {
+    double v = 0.0;
+    for (int o = 0; o < 64; ++o) v += dz2[o] * d.w2[o * 64 + h];
+    dz1[h] = q(v * gelu_grad(a.z1[h]), emu);
+  }
+  for (int o = 0; o < 4; ++o) {
+    for (int h = 0; h < 64; ++h) G[W3 + o * 64 + h] += dy[o] * a.h2[h];
+    G[B3 + o] += dy[o];
+  }
+  for (int o = 0; o < 64; ++o) {
+    for (int h = 0; h < 64; ++h) G[W2 + o * 64 + h] += dz2[o] * a.h1[h];
+    G[B2 + o] += dz2[o];
+    for (int k = 0; k < 12; ++k) G[W1 + o * 12 + k] += dz1[o] * a.x[k];
+    G[B1 + o] += dz1[o];
+  }
+}
+
 // Feature sums of particle i at x0 (warmstart.cu ws_sweep + k_ws_lambda), using the
 // reference's neighbour loop and kernels.
 void ws_features_one(const Grid& g, const Sph& k, const rtp_fluid_params* p, const float* x0, const float* vel,
@@ -666,7 +704,7 @@ void or_mlp_loss_grad(const rtp_mlp* net, const float* lossW, const float* feats
   // grad: w1 (64x12), b1 (64), w2 (64x64), b2 (64), w3 (4x64), b3 (4) = 5252 doubles.
   const bool emu = emulate != 0;
   const NetD d(net, emu);
-  const int W1 = 0, B1 = W1 + 768, W2 = B1 + 64, B2 = W2 + 4096, W3 = B2 + 64, B3 = W3 + 256, NP = B3 + 4;
+  const int NP = 5252;
   std::vector<double> G(NP, 0.0);
   double L = 0.0;
   const double invN = 1.0 / (double)n;
@@ -680,35 +718,137 @@ void or_mlp_loss_grad(const rtp_mlp* net, const float* lossW, const float* feats
       L += lossW[o] * e * e;
       dy[o] = q(2.0 * lossW[o] * e * invN, emu);
     }
-    double dz2[64], dz1[64];
-    for (int h = 0; h < 64; ++h) {
-      double v = 0.0;
-      for (int o = 0; o < 4; ++o) v += dy[o] * d.w3[o * 64 + h];
-      dz2[h] = q(v * gelu_grad(a.z2[h]), emu);
-    }
-    for (int h = 0; h < 64; ++h) {
-      double v = 0.0;
-      for (int o = 0; o < 64; ++o) v += dz2[o] * d.w2[o * 64 + h];
-      dz1[h] = q(v * gelu_grad(a.z1[h]), emu);
-    }
-    for (int o = 0; o < 4; ++o) {
-      for (int h = 0; h < 64; ++h) G[W3 + o * 64 + h] += dy[o] * a.h2[h];
-      G[B3 + o] += dy[o];
-    }
-    for (int o = 0; o < 64; ++o) {
-      for (int h = 0; h < 64; ++h) G[W2 + o * 64 + h] += dz2[o] * a.h1[h];
-      G[B2 + o] += dz2[o];
-      for (int k = 0; k < 12; ++k) G[W1 + o * 12 + k] += dz1[o] * a.x[k];
-      G[B1 + o] += dz1[o];
-    }
+    mlp_backward_one(d, a, dy, emu, G);
   }
   *loss = L * invN;
   std::memcpy(grad, G.data(), sizeof(double) * NP);
 }
 
+void or_mlp_backward(const rtp_mlp* net, const float* feats, const float* dy, uint64_t n, int emulate, double* grad) {
+  const bool emu = emulate != 0;
+  const NetD d(net, emu);
+  std::vector<double> G(5252, 0.0);
+  for (uint64_t s = 0; s < n; ++s) {
+    NetD::Act a;
+    d.forward(feats + 12 * s, a);
+    double g4[4];
+    for (int o = 0; o < 4; ++o) g4[o] = q((double)dy[4 * s + o], emu);
+    mlp_backward_one(d, a, g4, emu, G);
+  }
+  std::memcpy(grad, G.data(), sizeof(double) * G.size());
+}
+
+// Loss of the warm start through the solve and its gradient to the network's output
+// (warmstart.cu k_ws_loss_grad_x, k_ws_grad_y; runtime.cu ws_train_pass), in double:
+//   x* = clamp(predicted positions), sorted and tabled as the step does;
+//   y = network(features at x*) (BF16 operand rounding when emulating), omega = omega(y);
+//   x' = clamp(x* + dp(omega lambda)), dp as fld_computeConstraintCorrection;
+//   L = 1/n sum (rho(x') / rho0 - 1)^2, rho over the 27 cells of x*'s table around x';
+//   dL/dy_k = omega'(y_k) lambda_k / rho0 sum_j (g_k - g_j) . gradSpiky(x*_k - x*_j), with
+//   g = dL/dx' (2 / (n rho0) sum_j (C'_m + C'_j) gradPoly6(x'_m - x'_j)), zero on a clamped
+//   coordinate.  The state `s` is advanced by the presort only (sorted copies, ids).  dy and
+//   omega are written at index = particle id.
+int or_ws_loss_grad(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, int emulate,
+                    uint32_t n, or_state* s, double* loss, double* dyById, double* omegaById) {
+  if (!c || !p || !net || !s || !s->pos || !s->vel || !s->predPos || !s->id || !loss) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const Bounds b(g);
+  std::vector<uint32_t> table;
+  fluid_presort(c, p, n, s, table, nullptr);
+  std::vector<float> x0(4 * (size_t)n);
+  for (uint32_t i = 0; i < n; ++i) st4(x0.data(), i, clamp4(ld4(s->predPos, i), b.lo, b.hi));
+  std::vector<float> feats(12 * (size_t)n);
+  or_ws_features(c, p, x0.data(), s->vel, table.data(), n, feats.data());
+  const NetD d(net, emulate != 0);
+  std::vector<double> y(n), om(n), lamE(n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    NetD::Act a;
+    d.forward(feats.data() + 12 * i, a);
+    y[i] = a.y[0] * net->outScale[0];
+    om[i] = ws_omega_d(y[i]);
+    lamE[i] = om[i] * (double)feats[12 * i + 10];
+  }
+  const double rho0 = p->restDensity, h = k.h, h2 = h * h;
+  const double lo[3] = {b.lo.x, b.lo.y, b.lo.z}, hi[3] = {b.hi.x, b.hi.y, b.hi.z};
+  std::vector<double> xp(3 * (size_t)n);
+  std::vector<float> xpf(4 * (size_t)n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 xi = ld4(x0.data(), i);
+    double dp[3] = {0.0, 0.0, 0.0};
+    fluid_neighbours(g, table.data(), xi, [&](uint32_t e) {
+      const f4 v = xi - ld4(x0.data(), e);
+      const f4 gr = k.grad(v);
+      const double f = lamE[i] + lamE[e] + (double)k.artPressure(v, p);
+      dp[0] += f * gr.x;
+      dp[1] += f * gr.y;
+      dp[2] += f * gr.z;
+    });
+    const double xi3[3] = {xi.x, xi.y, xi.z};
+    for (int a = 0; a < 3; ++a) xp[3 * i + a] = std::min(std::max(xi3[a] + dp[a] / rho0, lo[a]), hi[a]);
+    st4(xpf.data(), i, mk((float)xp[3 * i], (float)xp[3 * i + 1], (float)xp[3 * i + 2], 0.0f));
+  }
+  // rho(x') and C'.
+  std::vector<double> C(n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    double rho = 0.0;
+    fluid_neighbours(g, table.data(), ld4(xpf.data(), i), [&](uint32_t e) {
+      double r2 = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        const double v = xp[3 * i + a] - xp[3 * e + a];
+        r2 += v * v;
+      }
+      if (r2 < h2) rho += (double)k.poly6c * (h2 - r2) * (h2 - r2) * (h2 - r2);
+    });
+    C[i] = rho / rho0 - 1.0;
+  }
+  double L = 0.0;
+  for (uint32_t i = 0; i < n; ++i) L += C[i] * C[i];
+  *loss = L / n;
+  // g = dL/dx'.
+  std::vector<double> gx(3 * (size_t)n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    fluid_neighbours(g, table.data(), ld4(xpf.data(), i), [&](uint32_t e) {
+      double v[3], r2 = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        v[a] = xp[3 * i + a] - xp[3 * e + a];
+        r2 += v[a] * v[a];
+      }
+      if (r2 < h2) {
+        const double f = (C[i] + C[e]) * (-6.0 * (double)k.poly6c * (h2 - r2) * (h2 - r2));
+        for (int a = 0; a < 3; ++a) acc[a] += f * v[a];
+      }
+    });
+    for (int a = 0; a < 3; ++a) {
+      const bool held = xp[3 * i + a] == lo[a] || xp[3 * i + a] == hi[a];
+      gx[3 * i + a] = held ? 0.0 : 2.0 / ((double)n * rho0) * acc[a];
+    }
+  }
+  // dL/dy.
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 xi = ld4(x0.data(), i);
+    double acc = 0.0;
+    fluid_neighbours(g, table.data(), xi, [&](uint32_t e) {
+      const f4 gr = k.grad(xi - ld4(x0.data(), e));
+      acc += (gx[3 * i] - gx[3 * e]) * gr.x + (gx[3 * i + 1] - gx[3 * e + 1]) * gr.y +
+             (gx[3 * i + 2] - gx[3 * e + 2]) * gr.z;
+    });
+    const uint32_t id = s->id[i];
+    if (dyById) dyById[id] = ws_omega_grad(y[i]) * (double)feats[12 * i + 10] / rho0 * acc;
+    if (omegaById) omegaById[id] = om[i];
+  }
+  return RTP_OK;
+}
+
 int or_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, uint32_t extraIters,
                float guardTol, uint32_t plainIters, uint32_t n, or_state* s, float* lamTot, double* solverErr,
-               int* rerun) {
+               int* rerun, int relaxAll) {
   if (!c || !p || !net || !s || !s->pos || !s->vel || !s->predPos || !lamTot) return RTP_ERR_INVALID_ARGUMENT;
   const Grid g(c);
   const Sph k(c);
@@ -723,16 +863,19 @@ int or_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp
   std::vector<float> feats(12 * (size_t)n), out(4 * (size_t)n);
   or_ws_features(c, p, x0.data(), s->vel, table.data(), n, feats.data());
   or_mlp_forward(net, feats.data(), n, 1, out.data());
-  std::vector<float> lam(n), corr(4 * (size_t)n), density(n), lambdaBuf(n);
-  for (uint32_t i = 0; i < n; ++i) lam[i] = out[4 * i];
-  // x1 = x0 + dp(lambda_net) + r_net; clamped when plain iterations follow.
+  std::vector<float> lam(n), corr(4 * (size_t)n), density(n), lambdaBuf(n), om(n);
+  // The network relaxes the plain first-iteration lambda (feature 10): lambda <- omega(y) lambda.
+  for (uint32_t i = 0; i < n; ++i) {
+    om[i] = ws_omega(out[4 * i]);
+    lam[i] = om[i] * feats[12 * (size_t)i + 10];
+  }
+  // x1 = x0 + dp(omega lambda); clamped when iterations follow (they start with the clamp).
   or_fld_correction(c, p, x0.data(), lam.data(), table.data(), n, corr.data());
   for (uint32_t i = 0; i < n; ++i) {
-    f4 x = ld4(x0.data(), i) + ld4(corr.data(), i) + mk(out[4 * i + 1], out[4 * i + 2], out[4 * i + 3], 0.0f);
-    st4(pred, i, x);
+    st4(pred, i, ld4(x0.data(), i) + ld4(corr.data(), i));
     lamTot[i] = lam[i];
   }
-  fluid_jacobi(c, p, extraIters, pred, table.data(), n, density, lambdaBuf, lamTot);
+  fluid_jacobi(c, p, extraIters, pred, table.data(), n, density, lambdaBuf, lamTot, relaxAll ? om.data() : nullptr);
   double err = mean_density_error(c, p, pred, table.data(), n);
   int rr = 0;
   if (guardTol > 0.0f && err > (double)guardTol) {

@@ -117,9 +117,16 @@ void or_mlp_forward(const rtp_mlp* net, const float* feats, uint64_t n, int emul
 void or_mlp_loss_grad(const rtp_mlp* net, const float* lossW, const float* feats, const float* targets, uint64_t n,
                       int emulate, double* loss, double* grad);
 /* One warm-started Fluids step; lamTot receives the multiplier totals (sorted order). */
+// Backward of the network with a given output gradient dy (rows of 4): 5252 doubles (w1, b1,
+// w2, b2, w3, b3) of d/dparams sum_s sum_o dy_so y_so.
+void or_mlp_backward(const rtp_mlp* net, const float* feats, const float* dy, uint64_t n, int emulate, double* grad);
+// Loss of the warm start through the solve (mean squared density constraint after the
+// omega-relaxed first correction) and dL/dy per particle id; see oracle.cpp.
+int or_ws_loss_grad(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, int emulate,
+                    uint32_t n, or_state* s, double* loss, double* dyById, double* omegaById);
 int or_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* p, const rtp_mlp* net, uint32_t extraIters,
                float guardTol, uint32_t plainIters, uint32_t n, or_state* s, float* lamTot, double* solverErr,
-               int* rerun);
+               int* rerun, int relaxAll);
 /* One plain step with `iters` iterations (lamTot receives the lambda sums) that also returns
  * the samples of particles
  * phase, phase + stride, ... (features and targets as rtp_record_warm_start_samples). */

@@ -83,6 +83,9 @@ _SIGS = {
     "rtp_train_warm_start": [P, P, U64, C.POINTER(abi.TrainConfig), C.POINTER(abi.Mlp), P, P],
     "rtp_mlp_loss_grad": [C.POINTER(abi.Mlp), P, P, P, U64, C.POINTER(C.c_double), C.POINTER(abi.Mlp), P],
     "rtp_mlp_forward": [C.POINTER(abi.Mlp), P, U64, P, P],
+    "rtp_mlp_backward": [C.POINTER(abi.Mlp), P, P, U64, C.POINTER(abi.Mlp), P],
+    "rtp_warm_start_loss_grad": [P, C.POINTER(abi.Mlp), P, C.POINTER(C.c_double)],
+    "rtp_train_warm_start_rollout": [P, C.POINTER(abi.TrainConfig), U32, U32, C.c_int, C.POINTER(abi.Mlp), P],
     "rtp_fill_fluid_color": [P],
     "rtp_fill_color_float": [P, C.c_int, C.c_float, C.c_float],
     "rtp_fill_camera_order": [P, C.POINTER(C.c_float)],

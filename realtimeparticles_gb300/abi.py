@@ -222,7 +222,7 @@ class WarmStartConfig(C.Structure):
         ("enabled", C.c_uint32),
         ("extraIterations", C.c_uint32),
         ("guardTolerance", C.c_float),
-        ("reserved", C.c_uint32),
+        ("relaxAllIterations", C.c_uint32),
     ]
 
 

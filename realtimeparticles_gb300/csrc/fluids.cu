@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
                                                                 float* __restrict__ lambda,
                                                                 float* __restrict__ density, PairList pl,
                                                                 float* __restrict__ lamTot, int totMode,
-                                                                float4* __restrict__ packed) {
+                                                                float4* __restrict__ packed,
+                                                                const float* __restrict__ omega) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -122,7 +123,8 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
-  const float lam = -C / (ssq + p.relaxCFM);
+  float lam = -C / (ssq + p.relaxCFM);
+  if (omega) lam *= __ldg(omega + i);  // warm start relaxing every iteration
   lambda[i] = lam;
   density[i] = rho;
   if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, c
                                                             const uint2* __restrict__ table, uint32_t n,
                                                             float* __restrict__ lambda, float* __restrict__ density,
                                                             PairList pl, float* __restrict__ lamTot, int totMode,
-                                                            float4* __restrict__ packed) {
+                                                            float4* __restrict__ packed, const float* __restrict__ omega) {
   pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, q = t % LW;
   if ((t & ~31u) / LW >= n) return;  // the whole warp is past the last particle
@@ -179,7 +181,8 @@ __global__ void __launch_bounds__(128) k_fluid_lambda_group(GridK g, FluidK p, c
   const float C = rho / p.rho0 - 1.0f;
   ssq += sgx * sgx + sgy * sgy + sgz * sgz;
   ssq *= p.invRho0Sq;
-  const float lam = -C / (ssq + p.relaxCFM);
+  float lam = -C / (ssq + p.relaxCFM);
+  if (omega) lam *= __ldg(omega + i);  // warm start relaxing every iteration
   lambda[i] = lam;
   density[i] = rho;
   if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
@@ -620,7 +623,15 @@ int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uin
 
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table, uint32_t n,
                     float* lambda, float* density, bool last, const float4* posS, float4* velS, const PairList& pl,
-                    Launcher& L, float* lamTot, int totMode, float4* packed) {
+                    Launcher& L, float* lamTot, int totMode, float4* packed, const float* omega) {
+  const int rc = fluid_lambda_sweep(g, p, predIn, table, n, lambda, density, pl, L, lamTot, totMode, packed, omega);
+  if (rc) return rc;
+  return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L, packed);
+}
+
+int fluid_lambda_sweep(const GridK& g, const FluidK& p, const float4* predIn, const uint2* table, uint32_t n,
+                       float* lambda, float* density, const PairList& pl, Launcher& L, float* lamTot, int totMode,
+                       float4* packed, const float* omega) {
   L.begin("fld_lambda");
   const dim3 nb(blocks(n, kSweepThreads)), nt(kSweepThreads);
   const bool mask = n >= kMaskFilterParticles;
@@ -629,24 +640,25 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
       const dim3 gb(blocks(n, 128 / LW)), gt(128);
       if (p.bt.scenes)
         launch(L, k_fluid_lambda_group<true, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode,
-               packed);
+               packed, omega);
       else
         launch(L, k_fluid_lambda_group<false, LW>, gb, gt, g, p, predIn, table, n, lambda, density, pl, lamTot,
-               totMode, packed);
+               totMode, packed, omega);
     });
   } else if (p.bt.scenes && mask)
-    launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
+    launch(L, k_fluid_lambda<true, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed,
+           omega);
   else if (p.bt.scenes)
-    launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
+    launch(L, k_fluid_lambda<true, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed,
+           omega);
   else if (mask)
-    launch(L, k_fluid_lambda<false, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed);
+    launch(L, k_fluid_lambda<false, true>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode, packed,
+           omega);
   else
     launch(L, k_fluid_lambda<false, false>, nb, nt, g, p, predIn, table, n, lambda, density, pl, lamTot, totMode,
-           packed);
+           packed, omega);
   L.end("fld_lambda");
-  int rc = check("k_fluid_lambda");
-  if (rc) return rc;
-  return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L, packed);
+  return check("k_fluid_lambda");
 }
 
 int fluid_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const float* lambda,

@@ -90,7 +90,13 @@ int fluid_presort(const GridK& g, const FluidK& p, float4* pos, float4* vel, uin
 int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, const uint2* table,
                     uint32_t n, float* lambda, float* density, bool last, const float4* posS, float4* velS,
                     const PairList& pl, Launcher& L, float* lamTot = nullptr, int totMode = kTotNone,
-                    float4* packed = nullptr);
+                    float4* packed = nullptr, const float* omega = nullptr);
+// The density / lambda sweep of one iteration alone (fld_applyBoundaryCondition is the
+// producer's; fld_computeDensity + fld_computeConstraintFactor), recording the pairs into pl.
+// With omega (per particle) the lambdas are relaxed by it (the warm start in every iteration).
+int fluid_lambda_sweep(const GridK& g, const FluidK& p, const float4* predIn, const uint2* table, uint32_t n,
+                       float* lambda, float* density, const PairList& pl, Launcher& L, float* lamTot = nullptr,
+                       int totMode = kTotNone, float4* packed = nullptr, const float* omega = nullptr);
 // Position correction alone with given lambdas (+ an optional residual displacement).  With
 // `packed` (x, y, z, lambda per particle, written by the lambda sweep) the neighbours' data
 // come from there.

@@ -157,11 +157,13 @@ __device__ __forceinline__ void d_to_a(const float (&z)[kMlpH8][4], uint32_t (&a
 
 // Minibatch rows [0, B) are samples perm[base + r] (or base + r without perm).  dY carries
 // the factor invTotal (1 / samples of the loss).  lossPart[tile] = sum of w_o (y - t)^2.
+// With dyIn (rows of kMlpOut) the output gradient is given instead of the regression loss's:
+// dY = dyIn, no loss.
 __global__ void __launch_bounds__(128) k_train_fwd_bwd(MlpDev m, const float* __restrict__ feats,
                                                        const float* __restrict__ targets,
                                                        const uint32_t* __restrict__ perm, uint64_t base, uint32_t B,
                                                        LossW lw, float invTotal, TrainAct act,
-                                                       float* __restrict__ lossPart) {
+                                                       float* __restrict__ lossPart, const float* __restrict__ dyIn) {
   const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
   const uint32_t s0 = tile * 16;
@@ -213,7 +215,9 @@ __global__ void __launch_bounds__(128) k_train_fwd_bwd(MlpDev m, const float* __
     for (int j = 0; j < 4; ++j) {
       const int o = 2 * c + (j & 1);
       const bool rowA = j < 2;
-      if (rowA ? vA : vB) {
+      if ((rowA ? vA : vB) && dyIn) {
+        dy[j] = dyIn[(rowA ? iA : iB) * kMlpOut + o];
+      } else if (rowA ? vA : vB) {
         const uint64_t idx = rowA ? iA : iB;
         const float t = targets[idx * kMlpOut + o] / __ldg(m.outScale + o);
         const float d = y[j] - t;
@@ -505,13 +509,14 @@ struct Trainer {
 
   int repack(cudaStream_t s) { return mlp_pack(master, norm, norm + 16, norm + 32, block, s); }
 
-  // Forward + backward + weight gradients of rows [base, base + B) (through perm).
+  // Forward + backward + weight gradients of rows [base, base + B) (through perm); with dyIn
+  // the output gradient is given (rows of kMlpOut) and targets are not read.
   int grads(const float* feats, const float* targets, const uint32_t* perm, uint64_t base, uint32_t B,
-            const LossW& lw, float invTotal, cudaStream_t s, uint32_t* nblkOut) {
+            const LossW& lw, float invTotal, cudaStream_t s, uint32_t* nblkOut, const float* dyIn = nullptr) {
     const uint32_t tiles = (B + 15) / 16;
     const uint32_t Bpad = tiles * 16;
     k_train_fwd_bwd<<<(tiles + 3) / 4, 128, 0, s>>>(mlp_dev(block), feats, targets, perm, base, B, lw, invTotal, act,
-                                                    lossPart);
+                                                    lossPart, dyIn);
     RTP_TRY2(check("k_train_fwd_bwd"));
     const uint32_t nblk = (Bpad + kWgradChunk - 1) / kWgradChunk;
     k_train_wgrad<<<nblk, kWgradThreads, 0, s>>>(act, kWgradChunk, Bpad, partials);
@@ -531,11 +536,131 @@ static uint64_t splitmix64(uint64_t& x) {
 }
 static double uniform01(uint64_t& x) { return (double)(splitmix64(x) >> 11) * (1.0 / 9007199254740992.0); }
 
+// ---- trainer for the runtime (training through the solve) ----------------------------------
+struct WsTrainer {
+  Trainer T;
+  uint64_t steps = 0;
+};
+
+int ws_trainer_create(uint32_t cap, WsTrainer** out) {
+  *out = nullptr;
+  WsTrainer* t = new WsTrainer();
+  const int rc = t->T.init(cap);
+  if (rc) {
+    delete t;
+    return rc;
+  }
+  *out = t;
+  return RTP_OK;
+}
+void ws_trainer_destroy(WsTrainer* t) { delete t; }
+const void* ws_trainer_block(const WsTrainer* t) { return t->T.block; }
+
+int ws_trainer_set_net(WsTrainer* t, const rtp_mlp& net, cudaStream_t s) {
+  RTP_CUDA(cudaMemsetAsync(t->T.mom, 0, kParams * sizeof(float), s));
+  RTP_CUDA(cudaMemsetAsync(t->T.var, 0, kParams * sizeof(float), s));
+  t->steps = 0;
+  return t->T.set_net(net, s);
+}
+
+int ws_trainer_get_net(WsTrainer* t, rtp_mlp& net, cudaStream_t s) {
+  std::vector<float> h(kParams);
+  RTP_CUDA(cudaMemcpyAsync(h.data(), t->T.master, kParams * sizeof(float), cudaMemcpyDeviceToHost, s));
+  RTP_CUDA(cudaStreamSynchronize(s));
+  master_to_net(h.data(), net);
+  return RTP_OK;
+}
+
+int ws_trainer_forward(WsTrainer* t, const float* feats, uint32_t n, float* y, cudaStream_t s) {
+  if (n == 0) return RTP_OK;
+  k_mlp_forward_rows<<<(n + 127) / 128, 128, 0, s>>>(mlp_dev(t->T.block), feats, n, y);
+  return check("k_mlp_forward_rows");
+}
+
+int ws_trainer_adam_step(WsTrainer* t, const float* feats, const float* dy, uint32_t n, const rtp_train_config& cfg,
+                         double lrScale, cudaStream_t s) {
+  if (n == 0) return RTP_OK;
+  LossW lw{};
+  uint32_t nblk = 0;
+  RTP_TRY2(t->T.grads(feats, nullptr, nullptr, 0, n, lw, 1.0f, s, &nblk, dy));
+  ++t->steps;
+  AdamStep st;
+  st.lr = (float)(cfg.learningRate * lrScale);
+  st.beta1 = cfg.beta1;
+  st.beta2 = cfg.beta2;
+  st.eps = cfg.eps;
+  st.wd = cfg.weightDecay;
+  st.bc1 = (float)(1.0 - std::pow((double)cfg.beta1, (double)t->steps));
+  st.bc2 = (float)(1.0 - std::pow((double)cfg.beta2, (double)t->steps));
+  k_train_adam<<<(kParams + 255) / 256, 256, 0, s>>>(t->T.partials, nblk, t->T.master, t->T.mom, t->T.var, st, nullptr);
+  RTP_TRY2(check("k_train_adam"));
+  return t->T.repack(s);
+}
+
+int ws_init_net(const float* feats, uint64_t n, uint64_t seed, rtp_mlp& net, cudaStream_t s) {
+  if (n == 0) return fail(RTP_ERR_INVALID_ARGUMENT, "no feature rows");
+  DevArena A;
+  const uint64_t per = 65536;
+  const uint32_t nb = (uint32_t)((n + per - 1) / per);
+  double* part = nullptr;
+  float* tz = nullptr;
+  RTP_TRY2(A.alloc(&part, (size_t)nb * kNormStats));
+  RTP_TRY2(A.alloc(&tz, (size_t)n * kMlpOut));
+  k_norm_partial<<<nb, 256, 0, s>>>(feats, tz, n, per, part);
+  RTP_TRY2(check("k_norm_partial"));
+  std::vector<double> h((size_t)nb * kNormStats);
+  RTP_CUDA(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RTP_CUDA(cudaStreamSynchronize(s));
+  double sum[kNormStats] = {0};
+  for (uint32_t b = 0; b < nb; ++b)
+    for (int q = 0; q < kNormStats; ++q) sum[q] += h[(size_t)b * kNormStats + q];
+  std::memset(&net, 0, sizeof(net));
+  for (int k = 0; k < kMlpIn; ++k) {
+    const double mu = sum[k] / (double)n;
+    const double sd = std::sqrt(std::max(0.0, sum[kMlpIn + k] / (double)n - mu * mu));
+    net.inMean[k] = (float)mu;
+    net.inScale[k] = sd > 1e-30 * (std::fabs(mu) + 1e-30) && sd > 0.0 ? (float)(1.0 / sd) : 1.0f;
+  }
+  for (int o = 0; o < kMlpOut; ++o) net.outScale[o] = 1.0f;
+  uint64_t rs = seed ^ 0x5DEECE66Dull;
+  auto fill = [&](float* w, int rows, int cols) {
+    const double a = std::sqrt(6.0 / (double)(rows + cols));
+    for (int i = 0; i < rows * cols; ++i) w[i] = (float)((2.0 * uniform01(rs) - 1.0) * a);
+  };
+  fill(&net.w1[0][0], kMlpHidden, kMlpIn);
+  fill(&net.w2[0][0], kMlpHidden, kMlpHidden);
+  return RTP_OK;
+}
+
 }  // namespace rtp
 
 using namespace rtp;
 
 extern "C" {
+
+int rtp_mlp_backward(const rtp_mlp* net, const float* d_features, const float* d_dy, uint64_t n, rtp_mlp* grad,
+                     void* stream) {
+  if (!net || !d_features || !d_dy || !grad) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
+  if (n == 0 || n > (1u << 24)) return fail(RTP_ERR_INVALID_ARGUMENT, "sample count must be in [1, 2^24]");
+  cudaStream_t s = (cudaStream_t)stream;
+  Trainer T;
+  RTP_TRY2(T.init((uint32_t)n));
+  RTP_TRY2(T.set_net(*net, s));
+  LossW lw{};
+  uint32_t nblk = 0;
+  RTP_TRY2(T.grads(d_features, nullptr, nullptr, 0, (uint32_t)n, lw, 1.0f, s, &nblk, d_dy));
+  float* g = nullptr;
+  RTP_TRY2(T.A.alloc(&g, kParams));
+  AdamStep st{};
+  k_train_adam<<<(kParams + 255) / 256, 256, 0, s>>>(T.partials, nblk, T.master, T.mom, T.var, st, g);
+  RTP_TRY2(check("k_train_adam(grad)"));
+  std::vector<float> h(kParams);
+  RTP_CUDA(cudaMemcpyAsync(h.data(), g, kParams * sizeof(float), cudaMemcpyDeviceToHost, s));
+  RTP_CUDA(cudaStreamSynchronize(s));
+  std::memset(grad, 0, sizeof(*grad));
+  master_to_net(h.data(), *grad);
+  return RTP_OK;
+}
 
 int rtp_mlp_forward(const rtp_mlp* net, const float* d_features, uint64_t n, float* d_out, void* stream) {
   if (!net || (!d_features && n) || (!d_out && n)) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");

@@ -198,12 +198,25 @@ struct Handle {
   // Learned warm start (fluids).
   bool wsOn = false;
   uint32_t wsExtra = 0;
+  bool wsRelaxAll = false;     // the network's omega relaxes every iteration, not the first only
+  float* wsOmega = nullptr;    // per-particle omega of the step (relaxAll)
   float wsTol = 0.0f;
   bool statsOn = false;        // solver statistics in plain steps
   void* mlpBlock = nullptr;    // packed network
   float* mlpTmp = nullptr;     // upload staging for the packer
   float* lamTot = nullptr;     // lambda summed over the last warm-started / recording step
-  float4* wsRes = nullptr;     // the network's residual displacements
+  // Training through the solve (allocated on first use): features and network outputs of
+  // every particle, dL/dy, dL/dx', the plain lambda, the corrected positions and their
+  // densities, per-block loss sums, and the trainer.
+  float* trFeats = nullptr;
+  float* trY = nullptr;
+  float* trDy = nullptr;
+  float4* trG = nullptr;
+  float* trLam = nullptr;
+  float4* trXp = nullptr;
+  float* trRho = nullptr;
+  float* trLoss = nullptr;
+  WsTrainer* trainer = nullptr;
   float* errPartial = nullptr; // per-block density-error sums
   SolverStatsDev* solverStats = nullptr;
   PairList pairsRec{};         // pairs at the predicted positions while recording samples
@@ -371,16 +384,17 @@ static void free_handle(Handle* h) {
   if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->targetHost) cudaFreeHost(h->targetHost);
   if (h->faultHost) cudaFreeHost(h->faultHost);
+  if (h->trainer) ws_trainer_destroy(h->trainer);
   if (h->targetUp) cudaEventDestroy(h->targetUp);
   delete h;
 }
 
 // Buffers of the warm start and of the solver statistics (allocated on first use).
 static int ws_alloc(Handle* h) {
-  if (h->wsRes) return RTP_OK;
+  if (h->errPartial) return RTP_OK;
   const size_t M = h->maxN;
-  RTP_TRY(dalloc(h, &h->wsRes, M));
   RTP_TRY(dalloc(h, &h->errPartial, ws_error_blocks((uint32_t)M)));
+  RTP_TRY(dalloc(h, &h->wsOmega, M));
   RTP_TRY(dalloc(h, &h->solverStats, 1));
   char* blk = nullptr;
   RTP_TRY(dalloc(h, &blk, MlpLayout::bytes));
@@ -399,6 +413,21 @@ static int ws_alloc_rec(Handle* h) {
   h->pairsRec.stride = (uint32_t)M;
   h->pairsRec.K = kPairListK;
   return RTP_OK;
+}
+
+static int ws_alloc_train(Handle* h) {
+  RTP_TRY(ws_alloc_rec(h));
+  if (h->trainer) return RTP_OK;
+  const size_t M = h->maxN;
+  RTP_TRY(dalloc(h, &h->trFeats, (size_t)kMlpIn * M));
+  RTP_TRY(dalloc(h, &h->trY, (size_t)kMlpOut * M));
+  RTP_TRY(dalloc(h, &h->trDy, (size_t)kMlpOut * M));
+  RTP_TRY(dalloc(h, &h->trG, M));
+  RTP_TRY(dalloc(h, &h->trLam, M));
+  RTP_TRY(dalloc(h, &h->trXp, M));
+  RTP_TRY(dalloc(h, &h->trRho, M));
+  RTP_TRY(dalloc(h, &h->trLoss, ws_loss_blocks((uint32_t)M)));
+  return ws_trainer_create((uint32_t)M, &h->trainer);
 }
 
 // A new state has no lambda totals yet.
@@ -440,15 +469,17 @@ static int fluids_presort(Handle* h, Launcher& L, const FluidK& fk, bool clampOu
 // `count` plain Jacobi iterations from `in`; the outputs alternate between dest and spare
 // so that the last lands in dest.  With trackTot the total lambda is accumulated (started
 // by the first iteration unless firstAdds).
+// With omega the lambdas of every iteration are relaxed by it (the warm start's relaxation kept
+// for the plain iterations after the first).
 static int plain_iterations(Handle* h, Launcher& L, const FluidK& fk, const float4* in, uint32_t count, float4* dest,
-                            float4* spare, bool trackTot, bool firstAdds) {
+                            float4* spare, bool trackTot, bool firstAdds, const float* omega = nullptr) {
   const uint32_t n = (uint32_t)h->curN;
   const float4* cur = in;
   for (uint32_t it = 0; it < count; ++it) {
     float4* out = ((count - it) % 2 == 1) ? dest : spare;
     const int mode = !trackTot ? kTotNone : ((it == 0 && !firstAdds) ? kTotWrite : kTotAdd);
     RTP_TRY(fluid_iteration(h->g, fk, cur, out, h->table, n, h->lambda, h->density, it + 1 == count, h->posS, h->velS,
-                            h->pairs, L, h->lamTot, mode, h->predLam));
+                            h->pairs, L, h->lamTot, mode, h->predLam, omega));
     cur = out;
   }
   return RTP_OK;
@@ -468,6 +499,52 @@ static int solver_error(Handle* h, Launcher& L, const FluidK& fk, const float4* 
 }
 
 static int record_fluids_ws_step(Handle* h, Launcher& L);
+
+// The warm-started first iteration from predA (the network `block` relaxes the plain lambda)
+// and E iterations after it, plain or (relaxAll) relaxed by the same per-particle omega; the
+// solver output lands in predB.
+static int ws_first_iteration(Handle* h, Launcher& L, const FluidK& fk, const void* block, uint32_t E, bool relaxAll) {
+  const uint32_t n = (uint32_t)h->curN;
+  RTP_TRY(ws_lambda_infer(h->g, fk, h->predA, h->velS, h->table, n, h->lambda, h->density, h->lamTot, h->pairs, block,
+                          h->predLam, relaxAll ? h->wsOmega : nullptr, L));
+  float4* warmOut = (E % 2 == 0) ? h->predB : h->predTmp;
+  RTP_TRY(fluid_deltap(h->g, fk, h->predA, warmOut, h->lambda, h->table, n, E == 0, h->posS, h->velS, h->pairs, nullptr,
+                       L, h->predLam));
+  return plain_iterations(h, L, fk, warmOut, E, h->predB, h->predTmp, true, true, relaxAll ? h->wsOmega : nullptr);
+}
+
+// Training through the solve, after the presort of a step (x* = predA): features and plain
+// lambda at x* (pairs P* in h->pairs), y = network(features) (the trainer's weights), the
+// correction x' = clamp(x* + dp(omega(y) lambda)), the density at x' (pairs P' in
+// h->pairsRec), then dL/dx' and dL/dy of L = 1/n sum C(x')^2 into trDy; per-block sums of
+// C(x')^2 in trLoss.  With skipFeatures the features of this presort are in trFeats already.
+static int ws_train_pass(Handle* h, Launcher& L, bool skipFeatures) {
+  const uint32_t n = (uint32_t)h->curN;
+  const GridK& g = h->g;
+  const FluidK fk = fluidk_of(h);
+  if (!skipFeatures)
+    RTP_TRY(ws_lambda_record(g, fk, h->predA, h->velS, h->table, n, h->trLam, h->density, h->lamTot, h->pairs, 1, 0,
+                             h->trFeats, n, L));
+  RTP_TRY(ws_trainer_forward(h->trainer, h->trFeats, n, h->trY, L.stream));
+  RTP_TRY(ws_apply_omega(h->predA, h->trLam, h->trY, n, h->lambda, h->predLam, L));
+  RTP_TRY(fluid_deltap(g, fk, h->predA, h->trXp, h->lambda, h->table, n, false, h->posS, h->velS, h->pairs, nullptr, L,
+                       h->predLam));
+  RTP_TRY(fluid_lambda_sweep(g, fk, h->trXp, h->table, n, h->lamTot, h->trRho, h->pairsRec, L));
+  RTP_TRY(ws_loss_grad_x(g, fk, h->trXp, h->trRho, h->table, n, h->pairsRec, h->trG, h->trLoss, L));
+  return ws_grad_y(g, fk, h->predA, h->trLam, h->trY, h->trG, h->table, n, h->pairs, h->trDy, L);
+}
+
+// Mean of C(x')^2 from the per-block sums (synchronises the stream).
+static int ws_train_loss(Handle* h, double* loss) {
+  const uint32_t n = (uint32_t)h->curN;
+  std::vector<float> part(ws_loss_blocks(n));
+  RTP_CUDA(cudaMemcpyAsync(part.data(), h->trLoss, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  double a = 0.0;
+  for (float v : part) a += (double)v;
+  *loss = n ? a / (double)n : 0.0;
+  return RTP_OK;
+}
 
 static int record_fluids_step(Handle* h, Launcher& L) {
   const uint32_t n = (uint32_t)h->curN;
@@ -505,12 +582,7 @@ static int record_fluids_ws_step(Handle* h, Launcher& L) {
   const GridK& g = h->g;
   const FluidK fk = fluidk_of(h);
   RTP_TRY(fluids_presort(h, L, fk, true));
-  RTP_TRY(ws_lambda_infer(g, fk, h->predA, h->velS, h->table, n, h->lambda, h->density, h->lamTot,
-                          h->pairs, h->mlpBlock, h->wsRes, L));
-  const uint32_t E = h->wsExtra;
-  float4* warmOut = (E % 2 == 0) ? h->predB : h->predTmp;
-  RTP_TRY(fluid_deltap(g, fk, h->predA, warmOut, h->lambda, h->table, n, E == 0, h->posS, h->velS, h->pairs, h->wsRes, L));
-  RTP_TRY(plain_iterations(h, L, fk, warmOut, E, h->predB, h->predTmp, true, true));
+  RTP_TRY(ws_first_iteration(h, L, fk, h->mlpBlock, h->wsExtra, h->wsRelaxAll));
   h->predFinal = h->predB;
   bool vortDone = false;
   RTP_TRY(solver_error(h, L, fk, h->predB, &vortDone));
@@ -1789,6 +1861,7 @@ int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_co
   RTP_TRY(mlp_upload_packed(*net, h->mlpTmp, h->mlpBlock, h->stream));
   h->wsOn = true;
   h->wsExtra = cfg->extraIterations;
+  h->wsRelaxAll = cfg->relaxAllIterations != 0;
   h->wsTol = cfg->guardTolerance;
   invalidate(h);
   return RTP_OK;
@@ -1859,6 +1932,77 @@ int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, ui
   h->hasStep = true;
   *written = count;
   return RTP_OK;
+  RTP_GUARD_END
+}
+
+static int check_trainable(Handle* h, const char* who) {
+  if (h->model != RTP_MODEL_FLUIDS || h->isBatch)
+    return fail(RTP_ERR_NOT_SUPPORTED, std::string(who) + ": single fluids scenes only");
+  if (h->curN == 0) return fail(RTP_ERR_STATE, std::string(who) + ": no particles");
+  if (h->paused) return fail(RTP_ERR_STATE, std::string(who) + ": the model is paused");
+  return RTP_OK;
+}
+
+int rtp_warm_start_loss_grad(void* handle, const rtp_mlp* net, float* d_dy, double* loss) {
+  RTP_GUARD_BEGIN
+  if (!handle || !net || !loss) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_warm_start_loss_grad: null argument");
+  Handle* h = H(handle);
+  RTP_TRY(check_trainable(h, "rtp_warm_start_loss_grad"));
+  const uint32_t n = (uint32_t)h->curN;
+  RTP_TRY(ws_alloc_train(h));
+  RTP_TRY(ws_trainer_set_net(h->trainer, *net, h->stream));
+  Launcher L;
+  L.stream = h->stream;
+  RTP_TRY(fluids_presort(h, L, fluidk_of(h), true));
+  RTP_TRY(ws_train_pass(h, L, false));
+  if (d_dy) RTP_TRY(ws_scatter_by_id(h->idsS, h->trDy, kMlpOut, n, d_dy, L));
+  RTP_TRY(ws_train_loss(h, loss));
+  return check_fault(h);
+  RTP_GUARD_END
+}
+
+int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint32_t steps, uint32_t extraIterations,
+                                 int init, rtp_mlp* net, float* loss_history) {
+  RTP_GUARD_BEGIN
+  if (!handle || !cfg || !net) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_train_warm_start_rollout: null argument");
+  Handle* h = H(handle);
+  RTP_TRY(check_trainable(h, "rtp_train_warm_start_rollout"));
+  if (extraIterations > 64) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_train_warm_start_rollout: extraIterations > 64");
+  const uint32_t n = (uint32_t)h->curN;
+  RTP_TRY(ws_alloc_train(h));
+  Launcher L;
+  L.stream = h->stream;
+  const FluidK fk = fluidk_of(h);
+  for (uint32_t s = 0; s < steps; ++s) {
+    RTP_TRY(fluids_presort(h, L, fk, true));
+    bool haveFeatures = false;
+    if (s == 0) {
+      if (init) {
+        RTP_TRY(ws_lambda_record(h->g, fk, h->predA, h->velS, h->table, n, h->trLam, h->density, h->lamTot, h->pairs,
+                                 1, 0, h->trFeats, n, L));
+        RTP_TRY(ws_init_net(h->trFeats, n, cfg->seed, *net, h->stream));
+        haveFeatures = true;
+      }
+      RTP_TRY(ws_trainer_set_net(h->trainer, *net, h->stream));
+    }
+    RTP_TRY(ws_train_pass(h, L, haveFeatures));
+    double loss = 0.0;
+    RTP_TRY(ws_train_loss(h, &loss));
+    if (loss_history) loss_history[s] = (float)loss;
+    const double frac = steps > 1 ? (double)s / (double)(steps - 1) : 0.0;
+    const double lrScale = cfg->finalLrFraction + (1.0 - cfg->finalLrFraction) * 0.5 * (1.0 + std::cos(M_PI * frac));
+    RTP_TRY(ws_trainer_adam_step(h->trainer, h->trFeats, h->trDy, n, *cfg, lrScale, h->stream));
+    // The simulation advances with the updated network (the states it trains on are the ones
+    // the warm-started solver itself produces).
+    RTP_TRY(ws_first_iteration(h, L, fk, ws_trainer_block(h->trainer), extraIterations, false));
+    h->predFinal = h->predB;
+    RTP_TRY(fluid_post(h->g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
+                       false, HostIO{}, h->predLam));
+    h->hasStep = true;
+  }
+  RTP_TRY(ws_trainer_get_net(h->trainer, *net, h->stream));
+  RTP_CUDA(cudaStreamSynchronize(h->stream));
+  return check_fault(h);
   RTP_GUARD_END
 }
 

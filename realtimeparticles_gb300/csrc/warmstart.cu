@@ -5,14 +5,21 @@
 //   k_ws_lambda<kInfer>   the first density / lambda sweep (fld_computeDensity +
 //                         fld_computeConstraintFactor at the predicted positions) also sums
 //                         the network's features, then each warp evaluates the MLP for its 32
-//                         particles on the tensor cores and writes lambda_i (the network's,
-//                         in place of the plain one) and a residual displacement r_i
-//   k_fluid_deltap        x_i += dp_i(lambda) + r_i, then the extra plain iterations
+//                         particles on the tensor cores.  The network's output y sets a
+//                         per-particle relaxation omega(y) in (0, 3) of the plain lambda:
+//                         lambda_i <- omega_i lambda_i (omega = 1 exactly at y = 0, so a
+//                         network whose last layer is zero is the plain solver)
+//   k_fluid_deltap        x_i += dp_i(omega lambda), then the extra plain iterations
 //   vorticity sweep       also sums |rho_i / rho0 - 1| per block at the solver output
 //   k_ws_guard            mean error -> statistics; sets the graph's conditional to rerun the
 //                         step's solve with the plain iteration count when above tolerance
-// Training samples come from plain steps: k_ws_lambda<kRecord> writes the features of the
-// sampled particles, k_ws_record_targets their targets once the plain solve has finished.
+// Training through the solve (rtp_train_warm_start_rollout): the loss is the mean squared
+// density constraint after the warm-started correction, L = 1/N sum_i C_i(x')^2 with
+// x' = clamp(x* + dp(omega lambda)); k_ws_loss_grad_x and k_ws_grad_y are its backward
+// sweeps (dL/dx', then dL/dy), and the trainer's kernels take dL/dy through the network.
+// Regression samples (features, converged lambda) come from plain steps:
+// k_ws_lambda<kRecord> writes the features of the sampled particles, k_ws_record_targets
+// their targets once the plain solve has finished.
 #include "warmstart.cuh"
 
 namespace rtp {
@@ -63,6 +70,14 @@ __device__ __forceinline__ void ws_sweep(const GridK& g, const uint2* __restrict
   pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
 }
 
+// The network's relaxation of the plain first-iteration lambda: omega = 1 + tanh(y) * (2 for
+// y > 0, 1 for y <= 0), in (0, 3); omega(0) = 1 exactly.
+__device__ __forceinline__ float ws_omega(float y) { return 1.0f + tanhf(y) * (y > 0.0f ? 2.0f : 1.0f); }
+__device__ __forceinline__ float ws_omega_grad(float y) {
+  const float t = tanhf(y);
+  return (1.0f - t * t) * (y > 0.0f ? 2.0f : 1.0f);
+}
+
 // Wall proximity along one axis: positive within 2h of the low wall, negative within 2h of
 // the high wall, 0 in between.
 __device__ __forceinline__ float wall_proximity(float x, float lo, float hi, float invH) {
@@ -71,13 +86,15 @@ __device__ __forceinline__ float wall_proximity(float x, float lo, float hi, flo
 
 // Inference holds the network's fragments after the sweep: 14 blocks of 64 threads per SM
 // (73 registers) still keep 131,072 particles in one wave on 152 SMs.
+// kInfer also writes (x, y, z, omega lambda) to `packed` for the correction sweep, and omega to
+// omegaOut when given.
 template <int MODE, bool BATCH>
 __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
     k_ws_lambda(GridK g, FluidK p, const float4* __restrict__ pred, const float4* __restrict__ velS,
                 const uint2* __restrict__ table, uint32_t n,
                 float* __restrict__ lambda, float* __restrict__ density, float* __restrict__ lamTot, PairList pl,
                 uint32_t stride, uint32_t phase, float* __restrict__ feats, uint32_t capacity, MlpDev m,
-                float4* __restrict__ res) {
+                float4* __restrict__ packed, float* __restrict__ omegaOut) {
   pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n;
@@ -85,9 +102,11 @@ __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
 #pragma unroll
   for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
   float lam = 0.0f;
+  float4 xi = f4(0.0f, 0.0f, 0.0f, 0.0f);
   if (active) {
     scene_of<BATCH>(i, g, p);
-    const float4 xi = ld4(pred + i), vi = ld4(velS + i);
+    xi = ld4(pred + i);
+    const float4 vi = ld4(velS + i);
     WsSums S;
     ws_sweep(g, table, pred, velS, i, xi, vi, pl, S);
     // fld_computeConstraintFactor, same operations as k_fluid_lambda.
@@ -131,11 +150,113 @@ __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
     float y[kMlpOut];
     mlp_warp_forward(m, x, y, s_stage[threadIdx.x >> 5]);
     if (!active) return;
-    const float lw = y[0] * __ldg(m.outScale + 0);
+    const float om = ws_omega(y[0] * __ldg(m.outScale + 0));
+    const float lw = om * lam;
+    if (omegaOut) omegaOut[i] = om;
     lambda[i] = lw;
     lamTot[i] = lw;
-    res[i] = f4(y[1] * __ldg(m.outScale + 1), y[2] * __ldg(m.outScale + 2), y[3] * __ldg(m.outScale + 3), 0.0f);
+    packed[i] = f4(xi.x, xi.y, xi.z, lw);
   }
+}
+
+// Training: lambda_i <- omega(y_i) lambda_i, with y the network's output 0 per particle
+// (rows of 4) and (x, y, z, omega lambda) into packed for the correction sweep.
+__global__ void k_ws_apply_omega(const float4* __restrict__ xs, const float* __restrict__ lam,
+                                 const float* __restrict__ y, uint32_t n, float* __restrict__ lamOut,
+                                 float4* __restrict__ packed) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 x = ld4(xs + i);
+  const float lw = ws_omega(__ldg(y + (size_t)i * kMlpOut)) * __ldg(lam + i);
+  lamOut[i] = lw;
+  packed[i] = f4(x.x, x.y, x.z, lw);
+}
+
+// Backward of the loss L = invN sum_m C'_m^2 to the corrected positions x' (the density sweep
+// at x' recorded its pairs in pl2 and rho' in rho2):
+//   g_m = 2 invN / rho0 sum_{j in P'(m)} (C'_m + C'_j) gradW_poly6(x'_m - x'_j),
+// with gradW_poly6(v) = -6 POLY6 (h^2 - r^2)^2 v, zeroed on a coordinate the clamp held (x'
+// on a bound of fld_applyBoundaryCondition).  lossPart[block] = sum of C'^2 over its particles.
+__global__ void __launch_bounds__(128) k_ws_loss_grad_x(GridK g, FluidK p, const float4* __restrict__ xp,
+                                                        const float* __restrict__ rho2, const uint2* __restrict__ table,
+                                                        uint32_t n, PairList pl2, float invN,
+                                                        float4* __restrict__ gOut, float* __restrict__ lossPart) {
+  __shared__ float s_loss[128 / kQuad];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;
+  const Sph k(g);
+  const float4 xi = ld4(xp + ii);
+  const float ci = __ldg(rho2 + ii) * p.invRho0 - 1.0f;
+  float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+  if (active) {
+    auto ld = [&](uint32_t j) { return Pair4{ld4(xp + j), __ldg(rho2 + j)}; };
+    quad_pairs(g, table, pl2, i, q, xi, ld, [&](uint32_t, Pair4 a) {
+      const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        const float d = k.h2 - r2;
+        const float f = (ci + (a.s * p.invRho0 - 1.0f)) * (-6.0f * k.poly6 * d * d);
+        gx += vx * f;
+        gy += vy * f;
+        gz += vz * f;
+      }
+    });
+  }
+  gx = quad_sum(gx);
+  gy = quad_sum(gy);
+  gz = quad_sum(gz);
+  const float sc = 2.0f * invN * p.invRho0;
+  if (q == 0) s_loss[threadIdx.x / kQuad] = active ? ci * ci : 0.0f;
+  if (active && q == 0)
+    gOut[i] = f4((xi.x == p.lo.x || xi.x == p.hi.x) ? 0.0f : gx * sc, (xi.y == p.lo.y || xi.y == p.hi.y) ? 0.0f : gy * sc,
+                 (xi.z == p.lo.z || xi.z == p.hi.z) ? 0.0f : gz * sc, 0.0f);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = 0.0f;
+    for (int u = 0; u < 128 / kQuad; ++u) a += s_loss[u];
+    lossPart[blockIdx.x] = a;
+  }
+}
+
+// dL/dy_k = omega'(y_k) lambda_k / rho0 sum_{j in P*(k)} (g_k - g_j) . gradSpiky(x*_k - x*_j)
+// over the pairs recorded at the predicted positions x* (the correction's own pairs).
+__global__ void __launch_bounds__(128) k_ws_grad_y(GridK g, FluidK p, const float4* __restrict__ xs,
+                                                   const float* __restrict__ lam, const float* __restrict__ y,
+                                                   const float4* __restrict__ gIn, const uint2* __restrict__ table,
+                                                   uint32_t n, PairList pl, float* __restrict__ dy) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;
+  const Sph k(g);
+  const float4 xi = ld4(xs + ii), gi = ld4(gIn + ii);
+  float acc = 0.0f;
+  if (active) {
+    auto ld = [&](uint32_t j) { return Pair44{ld4(xs + j), ld4(gIn + j)}; };
+    quad_pairs(g, table, pl, i, q, xi, ld, [&](uint32_t, Pair44 a) {
+      const float vx = xi.x - a.x.x, vy = xi.y - a.x.y, vz = xi.z - a.x.z;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        acc += ((gi.x - a.v.x) * vx + (gi.y - a.v.y) * vy + (gi.z - a.v.z) * vz) * s;
+      }
+    });
+  }
+  acc = quad_sum(acc);
+  if (!active || q != 0) return;
+  // Rows of kMlpOut: the gradient of output 0; outputs 1..3 are not used by the solve.
+  *reinterpret_cast<float4*>(dy + (size_t)i * kMlpOut) =
+      f4(ws_omega_grad(__ldg(y + (size_t)i * kMlpOut)) * __ldg(lam + i) * p.invRho0 * acc, 0.0f, 0.0f, 0.0f);
+}
+
+// dst[ids[i]] = src[i * stride]: sorted order -> particle ids.
+__global__ void k_scatter_by_id(const uint32_t* __restrict__ ids, const float* __restrict__ src, uint32_t stride,
+                                uint32_t n, float* __restrict__ dst) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[__ldg(ids + i)] = __ldg(src + (size_t)i * stride);
 }
 
 // Targets of sample s (particle i = phase + s * stride): (Lambda_i, xFinal_i - x0_i -
@@ -257,23 +378,53 @@ int ws_lambda_record(const GridK& g, const FluidK& p, const float4* pred, const 
   L.begin("ws_lambda_record");
   if (p.bt.scenes) return fail(RTP_ERR_NOT_SUPPORTED, "sample recording runs on single scenes");
   launch(L, k_ws_lambda<kRecord, false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
-      g, p, pred, velS, table, n, lambda, density, lamTot, pl, stride, phase, feats, capacity, m, nullptr);
+      g, p, pred, velS, table, n, lambda, density, lamTot, pl, stride, phase, feats, capacity, m, nullptr, nullptr);
   L.end("ws_lambda_record");
   return check("k_ws_lambda<record>");
 }
 
 int ws_lambda_infer(const GridK& g, const FluidK& p, const float4* pred, const float4* velS, const uint2* table, uint32_t n, float* lambda, float* density, float* lamTot, const PairList& pl,
-                    const void* mlpBlock, float4* res, Launcher& L) {
+                    const void* mlpBlock, float4* packed, float* omegaOut, Launcher& L) {
   const MlpDev m = mlp_dev(mlpBlock);
   L.begin("ws_lambda_mlp");
   if (p.bt.scenes)
     launch(L, k_ws_lambda<kInfer, true>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
-        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
+        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, packed, omegaOut);
   else
     launch(L, k_ws_lambda<kInfer, false>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads),
-        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, res);
+        g, p, pred, velS, table, n, lambda, density, lamTot, pl, 1, 0, nullptr, 0, m, packed, omegaOut);
   L.end("ws_lambda_mlp");
   return check("k_ws_lambda<infer>");
+}
+
+int ws_apply_omega(const float4* xs, const float* lam, const float* y, uint32_t n, float* lamOut, float4* packed,
+                   Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_ws_apply_omega, dim3(blocks(n, 256)), dim3(256), xs, lam, y, n, lamOut, packed);
+  return check("k_ws_apply_omega");
+}
+
+uint32_t ws_loss_blocks(uint32_t n) { return blocks(n * kQuad, 128); }
+
+int ws_loss_grad_x(const GridK& g, const FluidK& p, const float4* xp, const float* rho2, const uint2* table, uint32_t n,
+                   const PairList& pl2, float4* gOut, float* lossPart, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_ws_loss_grad_x, dim3(ws_loss_blocks(n)), dim3(128), g, p, xp, rho2, table, n, pl2,
+         (float)(1.0 / (double)n), gOut, lossPart);
+  return check("k_ws_loss_grad_x");
+}
+
+int ws_grad_y(const GridK& g, const FluidK& p, const float4* xs, const float* lam, const float* y, const float4* gIn,
+              const uint2* table, uint32_t n, const PairList& pl, float* dy, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_ws_grad_y, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, xs, lam, y, gIn, table, n, pl, dy);
+  return check("k_ws_grad_y");
+}
+
+int ws_scatter_by_id(const uint32_t* ids, const float* src, uint32_t stride, uint32_t n, float* dst, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_scatter_by_id, dim3(blocks(n, 256)), dim3(256), ids, src, stride, n, dst);
+  return check("k_scatter_by_id");
 }
 
 int ws_record_targets(const GridK& g, const FluidK& p, const float4* x0, const float* lamTot, const uint2* table,

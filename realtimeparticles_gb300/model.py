@@ -347,12 +347,14 @@ class Fluids(Model):
         return (int(r.best.lanes), float(r.best.cellFactor)), cands
 
     # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
-    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):
-        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off."""
+    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0, relax_all=False):
+        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off.
+        relax_all: the network's per-particle relaxation also applies to the extra iterations."""
         cfg = abi.WarmStartConfig()
         cfg.enabled = 0 if net is None else 1
         cfg.extraIterations = int(extra_iterations)
         cfg.guardTolerance = float(guard_tolerance)
+        cfg.relaxAllIterations = 1 if relax_all else 0
         call("rtp_set_warm_start", self._h, None if net is None else C.byref(net), C.byref(cfg))
 
     def enableSolverStats(self, enable=True):
@@ -510,12 +512,14 @@ class Clouds(Model):
         return (int(r.best.lanes), float(r.best.cellFactor)), cands
 
     # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
-    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0):
-        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off."""
+    def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0, relax_all=False):
+        """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off.
+        relax_all: the network's per-particle relaxation also applies to the extra iterations."""
         cfg = abi.WarmStartConfig()
         cfg.enabled = 0 if net is None else 1
         cfg.extraIterations = int(extra_iterations)
         cfg.guardTolerance = float(guard_tolerance)
+        cfg.relaxAllIterations = 1 if relax_all else 0
         call("rtp_set_warm_start", self._h, None if net is None else C.byref(net), C.byref(cfg))
 
     def enableSolverStats(self, enable=True):

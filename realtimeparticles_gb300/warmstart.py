@@ -1,9 +1,12 @@
-"""Learned warm start of the PBF constraint solve: training samples from plain runs, the
-network trained by the library's own GPU kernels, and the network file format.
+"""Learned warm start of the PBF constraint solve: the network trained through the solve on the
+model's own rollout by the library's GPU kernels, regression samples from plain runs, and the
+network file format.
 
-The C entry points are rtp_record_warm_start_samples, rtp_train_warm_start and
-rtp_set_warm_start (include/rtp.h).  PyTorch only provides the device buffers the samples
-live in; every computation is a library kernel.
+The network relaxes the plain first-iteration lambda per particle, lambda <- omega(y) lambda
+with omega = 1 + tanh(y) (2 for y > 0, 1 otherwise); a zero output layer is the plain solver.
+The C entry points are rtp_train_warm_start_rollout, rtp_warm_start_loss_grad,
+rtp_set_warm_start, and for regression rtp_record_warm_start_samples / rtp_train_warm_start
+(include/rtp.h).  PyTorch only provides device buffers; every computation is a library kernel.
 """
 import ctypes as C
 
@@ -102,6 +105,50 @@ def train(feats, targets, **kw):
         if cfg.lossWeights[o] == 0.0:
             net.outScale[o] = 0.0
     return net, [float(v) for v in hist]
+
+
+ROLLOUT_TRAIN = dict(learning_rate=2e-3, final_lr_fraction=0.05, beta1=0.9, beta2=0.999, eps=1e-8,
+                     weight_decay=0.0, seed=0)
+
+
+def omega(y):
+    """The relaxation the network's output y sets (numpy)."""
+    y = np.asarray(y, np.float64)
+    return 1.0 + np.tanh(y) * np.where(y > 0, 2.0, 1.0)
+
+
+def train_rollout(model, steps, extra_iterations=0, net=None, **kw):
+    """Trains the warm-start network through the solve on `model`'s own rollout (the model
+    advances `steps` steps under the warm-started solver).  net=None starts a new network.
+    Returns (abi.Mlp, per-step losses)."""
+    d = dict(ROLLOUT_TRAIN)
+    d.update(kw)
+    cfg = train_config(epochs=1, batch=16, loss_weights=(1.0, 0.0, 0.0, 0.0), **d)
+    init = net is None
+    net = abi.Mlp() if init else net
+    hist = (C.c_float * max(1, steps))()
+    call("rtp_train_warm_start_rollout", model.handle, C.byref(cfg), int(steps), int(extra_iterations),
+         1 if init else 0, C.byref(net), hist)
+    return net, [float(v) for v in hist[:steps]]
+
+
+def loss_grad_solve(model, net):
+    """(loss, dL/dy by particle id as a CUDA tensor) of the warm start through the solve at the
+    model's current state (the model is not advanced)."""
+    torch = _torch()
+    n = model.nbParticles()
+    dy = torch.zeros(n, dtype=torch.float32, device="cuda")
+    loss = C.c_double()
+    call("rtp_warm_start_loss_grad", model.handle, C.byref(net), C.c_void_p(dy.data_ptr()), C.byref(loss))
+    return loss.value, dy
+
+
+def backward(net, feats, dy):
+    """Parameter gradient (abi.Mlp) of sum dy * y for CUDA rows (the trainer's kernels)."""
+    grad = abi.Mlp()
+    call("rtp_mlp_backward", C.byref(net), C.c_void_p(feats.data_ptr()), C.c_void_p(dy.data_ptr()),
+         int(feats.shape[0]), C.byref(grad), None)
+    return grad
 
 
 def r2(pred, target):

@@ -3,11 +3,15 @@
 - inference kernel and the trainer's loss / gradient against the oracle's double-precision
   restatement, both with the GPU's BF16 operand rounding emulated (tight) and without it;
 - the trainer lowers the loss and is deterministic;
-- training samples (features and targets) recorded by the library against the oracle's;
-- warm-started steps (network + 0 or 1 extra iterations) against the oracle within the
-  step tolerance 1e-5 x box;
+- regression samples (features and targets) recorded by the library against the oracle's;
+- the loss through the solve and its gradient dL/dy, and the network's backward with a given
+  output gradient, against the oracle (whose gradient is pinned by finite differences);
+- warm-started steps (network + 0, 1 or 2 extra iterations, relaxed or plain) against the
+  oracle within the step tolerance 1e-5 x box; an untrained network (zero output layer) is the
+  plain solver bit for bit;
 - the guard: a step above tolerance reruns as the plain solver, bit for bit;
-- what a trained network gains over the same solver without it.
+- what a network trained through the solve gains over the same solver without it, on a
+  held-out scene.
 """
 import numpy as np
 import pytest
@@ -112,25 +116,42 @@ def test_recorded_samples_match_oracle():
         assert np.abs(t[:, 1:] - t_o[:, 1:]).max() <= REL_BOX * 1.0
 
 
-def _small_net(rng, lam_scale, res_scale):
-    return random_net(rng, out_scale=np.array([lam_scale, res_scale, res_scale, res_scale], np.float32))
+# Typical magnitudes of the 12 features on the dam break (the inputs' normalisation).
+FEATURE_SCALE = np.array([30.0, 0.05, 1.0, 1.0, 1.0, 5.0, 0.05, 1.0, 1.0, 1.0, 1e-5, 0.1], np.float32)
 
 
-@pytest.mark.parametrize("extra", [0, 1])
-def test_warm_started_steps_match_oracle(extra):
+def _omega_net(rng, out=0.3):
+    """A random network with normalised inputs whose relaxation omega spans about 0.6-1.8."""
+    net = random_net(rng, out_scale=np.array([1.0, 1.0, 1.0, 1.0], np.float32))
+    a = abi.mlp_to_arrays(net)
+    a["inMean"][:] = 0.0
+    a["inScale"][:] = 1.0 / FEATURE_SCALE
+    a["w3"][:] *= out / max(1e-6, float(np.abs(a["w3"]).max()))
+    a["b3"][:] = 0.0
+    return abi.mlp_from_arrays(a)
+
+
+def _zero_output(net):
+    a = abi.mlp_to_arrays(net)
+    a["w3"][:] = 0.0
+    a["b3"][:] = 0.0
+    return abi.mlp_from_arrays(a)
+
+
+@pytest.mark.parametrize("extra,relax_all", [(0, False), (1, False), (2, True)])
+def test_warm_started_steps_match_oracle(extra, relax_all):
     sc = scenes.dam_break(lattice=(8, 16, 16))
     c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
     fp = sc["fluid_params"]
     L = box_size(sc["model_params"])
     rng = np.random.default_rng(9)
-    # lambda of the plain first iteration is ~1e-6 here; residuals a fraction of a spacing
-    net = _small_net(rng, 2e-7, 2e-5)
+    net = _omega_net(rng)
     with fluids_model(sc, 3) as m:
-        m.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0)
+        m.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0, relax_all=relax_all)
         for step in range(4):
             st = gpu_state(m, abi.FLUIDS)
             lam = np.zeros(st["pos"].shape[0], np.float32)
-            err_o, rerun = oracle.ws_step(c, fp, net, extra, 0.0, 3, st, lam)
+            err_o, rerun = oracle.ws_step(c, fp, net, extra, 0.0, 3, st, lam, relax_all=relax_all)
             assert not rerun
             m.update(1)
             g = gpu_state(m, abi.FLUIDS)
@@ -138,15 +159,67 @@ def test_warm_started_steps_match_oracle(extra):
             assert_close_by_id(g["id"], g["pos"], st["id"], st["pos"], REL_BOX * L, "pos step %d" % step)
             assert_close_by_id(g["id"], g["vel"], st["id"], st["vel"], REL_BOX * L / fp.timeStep, "vel")
             lam_g = m.download(abi.BUF_LAMBDA_TOTAL)
-            assert np.abs(lam_g - lam).max() <= 1e-3 * np.abs(lam).max() + 1e-12
+            # omega comes from the BF16 network (within 0.5 % of the oracle's BF16 emulation)
+            assert np.abs(lam_g - lam).max() <= 1e-2 * np.abs(lam).max() + 1e-12
         stats = m.solverStats()
         assert stats["steps"] == 4 and stats["reruns"] == 0
+
+
+@pytest.mark.parametrize("extra", [0, 2])
+def test_untrained_network_is_the_plain_solver(extra):
+    """A zero output layer sets omega = 1: the warm-started step with `extra` plain iterations
+    after it equals the plain solver with extra + 1 iterations bit for bit (65,536 particles:
+    the plain sweeps run one lane per particle, as the warm start's feature sweep does)."""
+    sc = scenes.dam_break(lattice=(32, 64, 32))
+    net = _zero_output(_omega_net(np.random.default_rng(4)))
+    with fluids_model(sc, extra + 1) as plain, fluids_model(sc, 3) as warm:
+        warm.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0)
+        for _ in range(3):
+            plain.update(1)
+            warm.update(1)
+        a, b = gpu_state(plain, abi.FLUIDS), gpu_state(warm, abi.FLUIDS)
+        assert np.array_equal(a["id"], b["id"])
+        assert np.array_equal(a["pos"], b["pos"])
+        assert np.array_equal(a["vel"], b["vel"])
+
+
+@pytest.mark.parametrize("lattice,steps", [((8, 16, 16), 3), ((16, 32, 32), 30)])
+def test_loss_and_gradient_through_the_solve_match_oracle(lattice, steps):
+    sc = scenes.dam_break(lattice=lattice)
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    fp = sc["fluid_params"]
+    net = _omega_net(np.random.default_rng(7))
+    with fluids_model(sc, 2) as m:
+        m.update(steps)
+        st = gpu_state(m, abi.FLUIDS)
+        pos0 = m.download(abi.BUF_POS)
+        loss, dy = warmstart.loss_grad_solve(m, net)
+        assert np.array_equal(m.download(abi.BUF_POS), pos0), "the state must not advance"
+    dy = dy.cpu().numpy().astype(np.float64)
+    l_o, dy_o, om = oracle.ws_loss_grad(c, fp, net, st, emulate=True)
+    assert om.std() > 0.05  # the network does relax lambda
+    assert abs(loss - l_o) <= 2e-3 * l_o, (loss, l_o)
+    rel = np.linalg.norm(dy - dy_o) / np.linalg.norm(dy_o)
+    assert rel <= 2e-2, rel
+
+
+def test_backward_with_given_output_gradient_matches_oracle():
+    rng = np.random.default_rng(12)
+    net = random_net(rng)
+    n = 3001
+    feats = rng.normal(0, 1, (n, 12)).astype(np.float32)
+    dy = rng.normal(0, 1e-3, (n, 4)).astype(np.float32)
+    grad = abi.mlp_to_arrays(warmstart.backward(net, _cuda(feats), _cuda(dy)))
+    g_o = oracle.mlp_backward(net, feats, dy, emulate=True)
+    for name in abi.MLP_TRAINABLE:
+        rel = np.linalg.norm(grad[name] - g_o[name]) / np.linalg.norm(g_o[name])
+        assert rel <= 1e-2, (name, rel)
 
 
 def test_guard_reruns_as_the_plain_solver():
     sc = scenes.dam_break(lattice=(8, 16, 16))
     rng = np.random.default_rng(1)
-    net = _small_net(rng, 2e-7, 2e-5)
+    net = _omega_net(rng)
     with fluids_model(sc, 3) as plain, fluids_model(sc, 3) as guarded:
         guarded.setWarmStart(net, extra_iterations=0, guard_tolerance=1e-12)
         for _ in range(3):
@@ -161,40 +234,29 @@ def test_guard_reruns_as_the_plain_solver():
         assert s["mean"] > 0.0 and s["mean_first"] > 0.0
 
 
-def test_trained_network_gain_over_the_plain_first_iteration():
-    """Train on plain 8-iteration dam-break runs (2 seeded scenes), evaluate on a third.
+def _solver_error(sc, iters, net=None, extra=0, steps=160):
+    with fluids_model(sc, iters) as m:
+        m.enableSolverStats(True)
+        if net is not None:
+            m.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0)
+        m.update(steps)
+        return m.solverStats()["mean"]
 
-    The network's multiplier replaces the plain solver's first-iteration lambda; its target
-    is the converged one (lambda summed over the 8 reference iterations).  Gain: on held-out
-    samples the network explains the target better (R^2) than the plain first-iteration
-    lambda does under its best linear scaling.  The step-level outcome (solver-output mean
-    density error of the warm start + 1 iteration against plain 2 and 8 iterations, same
-    held-out scene) is printed, not asserted: on this workload a local network's multiplier
-    errors, amplified by the correction's kernel gradients, cost about what it saves."""
+
+def test_network_trained_through_the_solve_beats_the_plain_first_iteration():
+    """Train on the rollout of one seeded dam break (16,384 particles) under the warm start with
+    no extra iteration, evaluate on a held-out seed: the solver-output mean density error of the
+    warm start with no extra iteration must be below the plain solver's with one iteration (the
+    solve the warm start replaces), and the training loss must fall.  The comparison with more
+    iterations is printed."""
     lattice = (16, 32, 32)
-    feats, targets = warmstart.generate_samples(seeds=(1, 2), lattice=lattice, steps=160, record_every=10,
-                                                stride=4, reference_iterations=8)
-    assert feats.shape[0] == 2 * 16 * 4096
-    net, hist = warmstart.train(feats, targets, epochs=16, batch=4096, learning_rate=2e-3, seed=1)
-    assert hist[-1] < 0.7 * hist[0], hist
-    fe, te = warmstart.generate_samples(seeds=(3,), lattice=lattice, steps=160, record_every=20, stride=4,
-                                        reference_iterations=8)
-    pred = warmstart.forward(net, fe).cpu().numpy()
-    t = te.cpu().numpy()[:, 0]
-    lam0 = fe.cpu().numpy()[:, 10].astype(np.float64)
-    a = float(lam0 @ t / (lam0 @ lam0))
-    r2_net = float(warmstart.r2(pred[:, 0], t))
-    r2_plain = float(warmstart.r2(a * lam0, t))
-    assert not np.any(pred[:, 1:]), "residual outputs are off by default"
-    errs = {}
-    sc = scenes.dam_break(lattice=lattice, seed=3)
-    for name, iters, extra in (("plain2", 2, None), ("plain8", 8, None), ("learned+1", 8, 1)):
-        with fluids_model(sc, iters) as m:
-            m.enableSolverStats(True)
-            if extra is not None:
-                m.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0)
-            m.update(160)
-            errs[name] = round(m.solverStats()["mean"], 5)
-    print("R2 of the converged multiplier: network %.3f, plain first iteration %.3f; "
-          "solver-output density error %s" % (r2_net, r2_plain, errs))
-    assert r2_net > r2_plain + 0.1, (r2_net, r2_plain)
+    sc = scenes.dam_break(lattice=lattice, seed=1)
+    with fluids_model(sc, 2) as m:
+        net, hist = warmstart.train_rollout(m, 300, extra_iterations=0, seed=1)
+    assert np.all(np.isfinite(hist))
+    assert np.mean(hist[-30:]) < np.mean(hist[:30]), (hist[:5], hist[-5:])
+    test = scenes.dam_break(lattice=lattice, seed=3)
+    errs = {"plain1": _solver_error(test, 1), "plain2": _solver_error(test, 2), "plain3": _solver_error(test, 3),
+            "learned+0": _solver_error(test, 3, net, 0), "learned+1": _solver_error(test, 3, net, 1)}
+    print("solver-output mean |rho/rho0 - 1| on a held-out scene: %s" % {k: round(v, 5) for k, v in errs.items()})
+    assert errs["learned+0"] < errs["plain1"], errs
