@@ -1,0 +1,178 @@
+"""Parity at the benchmark configurations' own sizes and lengths.
+
+* Clouds at 131,072 particles (the clouds benchmark workload): three steps against the oracle,
+  with the value-noise ground temperature (Clouds::update, physics/ocl/Clouds.cpp:503-627).
+* The exact 48-scene batch the batched benchmark steps (`batched_dam_breaks(count=48, seed=0)`,
+  1,134,509 particles, 4,127-65,031 per scene, aspect 0.5-2): one step, every scene against
+  the oracle run on that scene alone (Fluids::update, Fluids.cpp:400-457, once per scene).
+* Long runs judged on statistics, since independent trajectories of a chaotic system diverge
+  after a few hundred steps: boids, 131,072 particles over 1,000 steps (Boids::update,
+  Boids.cpp:323-384), and clouds over 4,000 steps.  The clouds run uses 8,192 particles (the
+  same box, grid and per-particle density law as the 131k workload): 4,000 oracle steps at
+  131,072 particles would take over an hour of CPU time.
+
+The tolerances of the long runs come from the spread of the oracle against itself: the same
+run from positions perturbed by 1e-6 .. 5e-6 (rounding-sized changes).  Boids (1,000 steps):
+kinetic energy within 1e-5, polarisation within 2e-4, mean neighbour count within 0.4 %,
+neighbour-histogram total variation 0.016-0.020.  Clouds (4,000 steps, a convecting, condensing
+column): mean temperature 290.1-291.6 K, kinetic energy within 5 %, mean vapour within 3 %,
+mean cloud water within 6 %, mean height within 0.02, density error within 7 %, neighbours
+within 0.5 %, 1 % temperature quantile within 3.1 K, 99 % quantile within 0.06 K, 99 % cloud-water
+quantile within 2 %.  Each bound is about twice that spread; extremes (hottest, coldest particle)
+are compared through those quantiles, since single particles differ between runs.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from realtimeparticles_gb300 import abi, model, scenes
+
+from helpers import REL_BOX, assert_close_by_id, boids_model, clouds_model, gpu_state
+from test_gpu_clouds import _compare as _clouds_compare
+
+pytestmark = pytest.mark.gpu
+
+
+def test_clouds_131k_steps_match_the_oracle():
+    sc = scenes.clouds_cumulus(n=131072, noise=True)
+    with clouds_model(sc, iters=1) as m:
+        _clouds_compare(m, sc, 1, steps=3)
+
+
+def test_batched_48_scene_set_matches_the_oracle_per_scene():
+    sc = scenes.batched_dam_breaks(count=48, seed=0)
+    fp = sc["fluid_params"]
+    iters = 3
+    with model.FluidsBatch(sc["scenes"], sc["h"]) as m:
+        m.setFluidParams(fp)
+        m.setJacobiIterations(iters)
+        m.upload(abi.BUF_POS, sc["pos"])
+        m.upload(abi.BUF_VEL, sc["vel"])
+        assert m.numScenes() == 48
+        assert m.nbParticles() == sum(n for n, _ in sc["scenes"])
+        before = []
+        for s in range(48):
+            off, cnt = m.sceneRange(s)
+            c = m.sceneConstants(s)
+            st = oracle.new_state(cnt, c)
+            st["pos"][:] = sc["pos"][off:off + cnt]
+            st["vel"][:] = sc["vel"][off:off + cnt]
+            oracle.fluids_step(c, fp, iters, st)
+            before.append((off, cnt, st))
+        m.update(1)
+        pos, vel, ids = m.download(abi.BUF_POS), m.download(abi.BUF_VEL), m.download(abi.BUF_ID)
+        keys = m.download(abi.BUF_CELL_ID)
+        for s, (off, cnt, st) in enumerate(before):
+            box = max(sc["scenes"][s][1])
+            gid = ids[off:off + cnt] - off
+            assert np.array_equal(gid, st["id"]), "scene %d: sorted order" % s
+            assert np.array_equal(keys[off:off + cnt] - m.sceneKeyBase(s), st["cellId"]), "scene %d: keys" % s
+            assert_close_by_id(gid, pos[off:off + cnt], st["id"], st["pos"], REL_BOX * box, "scene %d pos" % s)
+            assert_close_by_id(gid, vel[off:off + cnt], st["id"], st["vel"], REL_BOX * box / fp.timeStep,
+                               "scene %d vel" % s)
+
+
+# ---- long runs ---------------------------------------------------------------------------
+def _fmt(d):
+    return {k: round(float(v), 5) for k, v in d.items() if not isinstance(v, np.ndarray)}
+
+
+def boids_statistics(pos, vel, radius=0.05):
+    """Kinetic energy, speed range, polarisation |mean of unit velocities| (the flocking order
+    the alignment rule builds) and the histogram of boids within the neighbour radius (the
+    rules' own 1e-8 < r^2 < R^2 test, no periodic images: boids.cl:84-101)."""
+    from scipy.spatial import cKDTree
+    x = pos[:, :3].astype(np.float64)
+    v = vel[:, :3].astype(np.float64)
+    speed = np.linalg.norm(v, axis=1)
+    pairs = cKDTree(x).query_pairs(radius, output_type="ndarray")
+    cnt = np.bincount(pairs.ravel(), minlength=len(x))
+    hist = np.bincount(np.minimum(cnt, 31), minlength=32).astype(np.float64)
+    return {"ke": 0.5 * float((speed ** 2).sum()), "smin": float(speed.min()), "smax": float(speed.max()),
+            "polar": float(np.linalg.norm((v / np.maximum(speed, 1e-12)[:, None]).mean(axis=0))),
+            "mean_nbr": float(cnt.mean()), "hist": hist / hist.sum()}
+
+
+def test_boids_131k_long_run_statistics():
+    pytest.importorskip("scipy")
+    sc = scenes.boids_cloud(n=131072)
+    bp = sc["boids_params"]
+    steps = 1000
+    c = oracle.derive_constants(abi.BOIDS, sc["model_params"])
+    st = oracle.new_state(131072, c, abi.BOIDS)
+    st["pos"][:] = sc["pos"]
+    st["vel"][:] = sc["vel"]
+    for _ in range(steps):
+        oracle.boids_step(c, bp, 0.01, abi.CYCLIC_WALL, st)
+    so = boids_statistics(st["pos"], st["vel"])
+    with boids_model(sc, dt=0.01, boundary=abi.CYCLIC_WALL) as m:
+        m.update(steps)
+        g = gpu_state(m, abi.BOIDS)
+    sg = boids_statistics(g["pos"], g["vel"])
+    print("boids after %d steps: gpu %s oracle %s" % (steps, _fmt(sg), _fmt(so)))
+    assert np.all(np.isfinite(g["pos"])) and np.all(np.abs(g["pos"][:, :3]) <= 1.0)
+    # bd_updateVel clamps speeds to [0.2 v, v] (boids.cl:246-259)
+    assert sg["smin"] >= 0.2 * bp.velocityScale * (1 - 1e-5) and sg["smax"] <= bp.velocityScale * (1 + 1e-5)
+    assert sg["ke"] == pytest.approx(so["ke"], rel=1e-3)
+    assert sg["polar"] == pytest.approx(so["polar"], abs=5e-3)
+    assert sg["mean_nbr"] == pytest.approx(so["mean_nbr"], rel=0.01)
+    tv = 0.5 * np.abs(sg["hist"] - so["hist"]).sum()
+    assert tv < 0.05, tv
+
+
+def clouds_statistics(st, c, rho0):
+    """Means and quantiles of temperature, vapour and cloud water, kinetic energy, mean height,
+    and the mean |rho / rho0 - 1| and neighbour count of the final positions under poly6 with
+    the clouds' periodic images in x and z and walls in y (clouds.cl:305-360)."""
+    from scipy.spatial import cKDTree
+    t, qv, qc = st["temp"].astype(np.float64), st["vapor"].astype(np.float64), st["cloud"].astype(np.float64)
+    v = st["vel"][:, :3].astype(np.float64)
+    W = np.array(c.absWall[:3], np.float64)
+    x = st["pos"][:, :3].astype(np.float64) + W
+    period = np.array([2 * W[0], 1e9, 2 * W[2]])
+    x = np.mod(x, period)
+    h = float(c.effectRadius)
+    pairs = cKDTree(x, boxsize=period).query_pairs(h, output_type="ndarray")
+    d = x[pairs[:, 0]] - x[pairs[:, 1]]
+    d -= period * np.round(d / period)
+    w = float(c.poly6Coeff) * (h * h - (d * d).sum(axis=1)) ** 3
+    rho = np.full(len(x), float(c.poly6Coeff) * h ** 6)
+    np.add.at(rho, pairs[:, 0], w)
+    np.add.at(rho, pairs[:, 1], w)
+    cnt = np.bincount(pairs.ravel(), minlength=len(x))
+    return {"err": float(np.abs(rho / rho0 - 1).mean()), "ke": 0.5 * float((v ** 2).sum()), "t_mean": t.mean(),
+            "t_p01": float(np.quantile(t, 0.01)), "t_p99": float(np.quantile(t, 0.99)), "qv_mean": qv.mean(),
+            "qc_mean": qc.mean(), "qc_p99": float(np.quantile(qc, 0.99)), "y_mean": float(st["pos"][:, 1].mean()),
+            "nbr": float(cnt.mean())}
+
+
+def test_clouds_long_run_statistics():
+    pytest.importorskip("scipy")
+    n, steps = 8192, 4000
+    sc = scenes.clouds_cumulus(n=n, noise=True)
+    fp, cp = sc["fluid_params"], sc["cloud_params"]
+    c = oracle.derive_constants(abi.CLOUDS, sc["model_params"])
+    st = oracle.new_state(n, c, abi.CLOUDS)
+    st["pos"][:] = sc["pos"]
+    st["vel"][:] = sc["vel"]
+    oracle.clouds_init(c, cp, sc["env"], sc["ground"], st)
+    for _ in range(steps):
+        oracle.clouds_step(c, fp, cp, sc["env"], sc["ground"], 1, st)
+    so = clouds_statistics(st, c, fp.restDensity)
+    with clouds_model(sc, iters=1) as m:
+        m.update(steps)
+        g = gpu_state(m, abi.CLOUDS)
+    sg = clouds_statistics(g, c, fp.restDensity)
+    print("clouds after %d steps: gpu %s oracle %s" % (steps, _fmt(sg), _fmt(so)))
+    assert np.all(np.isfinite(g["pos"])) and np.all(np.isfinite(g["temp"]))
+    assert g["cloud"].min() >= 0 and g["vapor"].min() >= 0
+    assert sg["t_mean"] == pytest.approx(so["t_mean"], abs=1.5)
+    assert sg["t_p01"] == pytest.approx(so["t_p01"], abs=6.0)
+    assert sg["t_p99"] == pytest.approx(so["t_p99"], abs=0.5)
+    assert sg["qv_mean"] == pytest.approx(so["qv_mean"], rel=0.06)
+    assert sg["qc_mean"] == pytest.approx(so["qc_mean"], rel=0.12)
+    assert sg["qc_p99"] == pytest.approx(so["qc_p99"], rel=0.05)
+    assert sg["y_mean"] == pytest.approx(so["y_mean"], abs=0.04)
+    assert sg["err"] == pytest.approx(so["err"], rel=0.15)
+    assert sg["ke"] == pytest.approx(so["ke"], rel=0.15)
+    assert sg["nbr"] == pytest.approx(so["nbr"], rel=0.03)
