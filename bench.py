@@ -31,6 +31,9 @@ Metric: particle-steps/s.
   statistics on; the speed-up at equal error compares each warm-started configuration with
   the plain solver's Pareto front interpolated (log-log) at its error, and at_error_le_1pct
   the fastest configurations of each whose mean error is at most 1 % of rho0.
+* warm_start (clouds_131k): the same study on the clouds solve: a network trained through the
+  clouds solve on the rollouts of seeds 1-2 (300 steps each, no extra iteration), then the
+  plain clouds solver (1-8 iterations) and the warm start (+0-3) on the seed-0 column.
 * --impl reference: that CPU implementation alone (rank 0), same metric and config.
 Under torchrun (N > 1) each rank runs an independent replica of the workload on its
 own GPU (one scene does not shard; a batch shards by scene: rank r steps its own seeded
@@ -104,17 +107,38 @@ def make_model(w, rank=0):
         m.setTimeStep(0.01)
         m.setBoundary(abi.CYCLIC_WALL)
     else:
-        sc = scenes.clouds_cumulus(n=w["n"])
-        m = model.Clouds(sc["model_params"])
-        m.setFluidParams(sc["fluid_params"])
-        m.setCloudParams(sc["cloud_params"])
-        m.setEnvironment(sc["env"], sc["ground"])
-        m.setJacobiIterations(w["iters"])
+        return clouds_model(w["n"], 0, w["iters"]), w["n"]
     m.upload(abi.BUF_POS, sc["pos"])
     m.upload(abi.BUF_VEL, sc["vel"])
-    if w["kind"] == "clouds":
-        m.initThermo()
     return m, sc["pos"].shape[0]
+
+
+def fluids_model(lattice, seed, iters):
+    """A dam break (scenes.dam_break) of `lattice` with its inputs uploaded."""
+    from realtimeparticles_gb300 import model
+    sc = scenes.dam_break(lattice=lattice, seed=seed)
+    m = model.Fluids(sc["model_params"])
+    m.setFluidParams(sc["fluid_params"])
+    m.setJacobiIterations(iters)
+    m.upload(abi.BUF_POS, sc["pos"])
+    m.upload(abi.BUF_VEL, sc["vel"])
+    return m
+
+
+def clouds_model(n, seed, iters):
+    """A cumulus column (scenes.clouds_cumulus) of n particles with its inputs uploaded and
+    its thermodynamic state initialised."""
+    from realtimeparticles_gb300 import model
+    sc = scenes.clouds_cumulus(n=n, seed=seed)
+    m = model.Clouds(sc["model_params"])
+    m.setFluidParams(sc["fluid_params"])
+    m.setCloudParams(sc["cloud_params"])
+    m.setEnvironment(sc["env"], sc["ground"])
+    m.setJacobiIterations(iters)
+    m.upload(abi.BUF_POS, sc["pos"])
+    m.upload(abi.BUF_VEL, sc["vel"])
+    m.initThermo()
+    return m
 
 # Algorithmic bytes per particle of each kernel of the PBF substep (minimal dataflow of
 # the fused kernels: every array a kernel must read or write once).
@@ -323,6 +347,7 @@ def run_reference(args):
             "ms_per_step": 1000.0 * el / k, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": WORKLOAD, "particles": n, "jacobi_iterations": iters, "substep_dt": 1 / 240.0,
+                       "l2": "host run: no GPU L2 flush; the state stays in host memory and caches between steps",
                        "parallelism": "single"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
@@ -336,15 +361,10 @@ PLAIN_ITERS = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48)
 WARM_EXTRA = (0, 1, 2, 3, 5, 7, 8, 9, 11)
 
 
-def _timed_config(lattice, iters, net, extra, tol, steps, warmup):
-    """(ms per step, mean solver-output density error, reruns) of one configuration."""
-    from realtimeparticles_gb300 import model
-    sc = scenes.dam_break(lattice=lattice)
-    with model.Fluids(sc["model_params"]) as m:
-        m.setFluidParams(sc["fluid_params"])
-        m.setJacobiIterations(iters)
-        m.upload(abi.BUF_POS, sc["pos"])
-        m.upload(abi.BUF_VEL, sc["vel"])
+def _timed_config(open_model, iters, net, extra, tol, steps, warmup):
+    """(ms per step, mean solver-output density error, reruns) of one configuration;
+    open_model(iters) makes the seed-0 model."""
+    with open_model(iters) as m:
         m.enableSolverStats(True)
         if net is not None:
             m.setWarmStart(net, extra_iterations=extra, guard_tolerance=tol)
@@ -405,18 +425,17 @@ def warm_start_study(w, steps, warmup):
     step.  The plain solver's throughput at a configuration's error is log-log interpolated on
     the Pareto front of the measured plain points; `at_error_le_1pct` compares the fastest
     configurations of each whose mean error is at most 1 % of rho0."""
-    from realtimeparticles_gb300 import model, warmstart
+    from realtimeparticles_gb300 import warmstart
     lattice = w["lattice"]
+
+    def open_model(iters):
+        return fluids_model(lattice, 0, iters)
+
     n = int(np.prod(lattice))
     t0 = time.perf_counter()
     net, losses = None, []
     for seed in WS_TRAIN_SEEDS:
-        sc = scenes.dam_break(lattice=lattice, seed=seed)
-        with model.Fluids(sc["model_params"]) as m:
-            m.setFluidParams(sc["fluid_params"])
-            m.setJacobiIterations(2)
-            m.upload(abi.BUF_POS, sc["pos"])
-            m.upload(abi.BUF_VEL, sc["vel"])
+        with fluids_model(lattice, seed, 2) as m:
             net, hist = warmstart.train_rollout(m, WS_TRAIN_STEPS, extra_iterations=1, net=net, seed=0)
             losses += hist
     t1 = time.perf_counter()
@@ -426,13 +445,13 @@ def warm_start_study(w, steps, warmup):
            "eval": {"warmup_steps": WS_EVAL_WARMUP, "timed_steps": WS_EVAL_STEPS}}
     plain, curve = [], []
     for it in PLAIN_ITERS:
-        ms, err, _ = _timed_config(lattice, it, None, 0, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+        ms, err, _ = _timed_config(open_model, it, None, 0, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
         v = n / (ms / 1000.0)
         plain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err})
         curve.append((err, v))
     learned = []
     for e in WARM_EXTRA:
-        ms, err, rr = _timed_config(lattice, 3, net, e, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+        ms, err, rr = _timed_config(open_model, 3, net, e, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
         v = n / (ms / 1000.0)
         ref = _plain_at(curve, err)
         learned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
@@ -442,7 +461,7 @@ def warm_start_study(w, steps, warmup):
     # solver-output error exceeds 1.25 x the plain 3-iteration mean reruns with the plain 3.
     e3 = next(p["mean_density_error"] for p in plain if p["iterations"] == 3)
     tol = 1.25 * e3
-    ms, err, rr = _timed_config(lattice, 3, net, 2, tol, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+    ms, err, rr = _timed_config(open_model, 3, net, 2, tol, WS_EVAL_STEPS, WS_EVAL_WARMUP)
     guarded = {"extra_iterations": 2, "guard_tolerance": tol, "plain_iterations": 3,
                "particle_steps_per_s": n / (ms / 1000.0), "mean_density_error": err, "reruns": rr,
                "steps": WS_EVAL_STEPS}
@@ -456,6 +475,58 @@ def warm_start_study(w, steps, warmup):
                best_speedup_at_or_below_plain3_error=best(lambda x: x["mean_density_error"] <= e3),
                at_error_le_1pct=_at_threshold(plain, learned, 0.01),
                at_error_le_plain3=_at_threshold(plain, learned, e3))
+    return out
+
+
+CLOUD_PLAIN_ITERS = (1, 2, 3, 4, 6, 8)
+CLOUD_WARM_EXTRA = (0, 1, 2, 3)
+CLOUD_WS_TRAIN_SEEDS = (1, 2)
+
+
+def clouds_warm_start_study(w):
+    """The learned warm start of the clouds solve against the plain clouds solver at equal
+    error, as warm_start_study: a network trained through the clouds solve on the rollouts of
+    other seeded columns (CLOUD_WS_TRAIN_SEEDS, WS_TRAIN_STEPS steps each, no extra iteration:
+    the workload's own solve is one iteration), then the seed-0 column for WS_EVAL_STEPS
+    device-timed steps after WS_EVAL_WARMUP warm-up steps per configuration.
+    `at_error_le_plain1` compares the fastest configurations of each whose mean error is at
+    most the plain one-iteration solver's."""
+    from realtimeparticles_gb300 import warmstart
+    n = w["n"]
+
+    def open_model(iters):
+        return clouds_model(n, 0, iters)
+
+    t0 = time.perf_counter()
+    net, losses = None, []
+    for seed in CLOUD_WS_TRAIN_SEEDS:
+        with clouds_model(n, seed, 1) as m:
+            net, hist = warmstart.train_rollout(m, WS_TRAIN_STEPS, extra_iterations=0, net=net, seed=0)
+            losses += hist
+    t1 = time.perf_counter()
+    out = {"training": {"method": "through the solve on the model's own rollout (one AdamW step per step)",
+                        "scenes": len(CLOUD_WS_TRAIN_SEEDS), "steps": len(losses), "particles": n,
+                        "extra_iterations": 0, "train_seconds": round(t1 - t0, 2),
+                        "loss_first_30": float(np.mean(losses[:30])), "loss_last_30": float(np.mean(losses[-30:]))},
+           "eval": {"warmup_steps": WS_EVAL_WARMUP, "timed_steps": WS_EVAL_STEPS}}
+    plain, curve = [], []
+    for it in CLOUD_PLAIN_ITERS:
+        ms, err, _ = _timed_config(open_model, it, None, 0, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+        v = n / (ms / 1000.0)
+        plain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err})
+        curve.append((err, v))
+    learned = []
+    for e in CLOUD_WARM_EXTRA:
+        ms, err, _ = _timed_config(open_model, 1, net, e, 0.0, WS_EVAL_STEPS, WS_EVAL_WARMUP)
+        v = n / (ms / 1000.0)
+        ref = _plain_at(curve, err)
+        learned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
+                        "mean_density_error": err, "plain_at_equal_error": ref,
+                        "speedup_at_equal_error": (v / ref) if ref else None})
+    e1 = plain[0]["mean_density_error"]
+    v = [x["speedup_at_equal_error"] for x in learned if x["speedup_at_equal_error"]]
+    out.update(plain=plain, learned=learned, best_speedup_at_equal_error=max(v) if v else None,
+               at_error_le_plain1=_at_threshold(plain, learned, e1))
     return out
 
 
@@ -678,6 +749,8 @@ def run_ours(args):
             out["cpu_baseline"] = cb
         if w["kind"] == "fluids" and args.workload == WORKLOAD and not args.no_warm_start:
             out["warm_start"] = warm_start_study(w, args.steps, max(3, args.warmup))
+        if w["kind"] == "clouds" and not args.no_warm_start:
+            out["warm_start"] = clouds_warm_start_study(w)
         print(json.dumps(out))
     if ws > 1:
         import torch.distributed as dist

@@ -53,6 +53,12 @@ def lib():
         L.or_clouds_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
                                      C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P, C.c_uint32,
                                      C.c_uint32, P]
+        L.or_clouds_ws_step.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
+                                        C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P,
+                                        C.POINTER(abi.Mlp), C.c_uint32, C.c_uint32, P, P, P]
+        L.or_clouds_ws_loss.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams),
+                                        C.POINTER(abi.CloudParams), C.POINTER(abi.CloudEnv), P,
+                                        C.POINTER(abi.Mlp), C.c_int, C.c_uint32, P, C.POINTER(C.c_double), P]
         L.or_clouds_init.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.CloudParams),
                                      C.POINTER(abi.CloudEnv), P, C.c_uint32, P]
         L.or_fld_density.argtypes = [C.POINTER(abi.GridConstants), C.POINTER(abi.FluidParams), P, P,
@@ -211,6 +217,36 @@ def clouds_step(c, fp, cp, env, ground, iters, st):
                               C.byref(s))
     if rc != 0:
         raise ValueError("or_clouds_step failed: %d" % rc)
+
+
+def clouds_ws_step(c, fp, cp, env, ground, net, extra_iters, st):
+    """One warm-started clouds step in place; returns (features [n, 12], omega [n]) by sorted
+    index (the order of st after the step)."""
+    n = st["pos"].shape[0]
+    s = _state(st)
+    g = None if ground is None else np.ascontiguousarray(ground, dtype=np.float32)
+    feats = np.zeros((n, 12), np.float32)
+    om = np.zeros(n, np.float32)
+    rc = lib().or_clouds_ws_step(C.byref(c), C.byref(fp), C.byref(cp), C.byref(env), _p(g), C.byref(net),
+                                 int(extra_iters), n, C.byref(s), _p(feats), _p(om))
+    if rc != 0:
+        raise ValueError("or_clouds_ws_step failed: %d" % rc)
+    return feats, om
+
+
+def clouds_ws_loss(c, fp, cp, env, ground, net, st, emulate=False):
+    """(loss, features [n, 12]) of the clouds warm start at state st, which advances through
+    the step's presort (sorted order and thermodynamics)."""
+    n = st["pos"].shape[0]
+    s = _state(st)
+    g = None if ground is None else np.ascontiguousarray(ground, dtype=np.float32)
+    feats = np.zeros((n, 12), np.float32)
+    loss = C.c_double()
+    rc = lib().or_clouds_ws_loss(C.byref(c), C.byref(fp), C.byref(cp), C.byref(env), _p(g), C.byref(net),
+                                 1 if emulate else 0, n, C.byref(s), C.byref(loss), _p(feats))
+    if rc != 0:
+        raise ValueError("or_clouds_ws_loss failed: %d" % rc)
+    return loss.value, feats
 
 
 def fld_density(c, fp, pred, table):

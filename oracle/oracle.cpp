@@ -1241,15 +1241,21 @@ void or_clouds_init(const rtp_grid_constants* c, const rtp_cloud_params* cp, con
   }
 }
 
-int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
-                   const rtp_cloud_env* env, const float* ground, uint32_t iters, uint32_t n,
-                   or_state* s) {
-  if (!c || !fp || !cp || !env || !s || !s->pos || !s->vel || !s->predPos || !s->totCorrPos ||
-      !s->temp || !s->vapor || !s->cloud || !s->buoyancy)
-    return RTP_ERR_INVALID_ARGUMENT;
+}  // extern "C"
+
+namespace {
+
+bool clouds_state_ok(const or_state* s) {
+  return s && s->pos && s->vel && s->predPos && s->totCorrPos && s->temp && s->vapor && s->cloud && s->buoyancy;
+}
+
+// Clouds.cpp:516-567: thermodynamics, predicted positions under the mixed boundary, the sort
+// of every particle array by cell and the temperature smoothing.  `table` is the step's cell
+// table.
+void clouds_presort(const rtp_grid_constants* c, const rtp_cloud_params* cp, const CloudEnv& E, uint32_t n,
+                    or_state* s, std::vector<uint32_t>& table) {
   const Grid g(c);
   const Sph k(c);
-  const CloudEnv E(c, env, ground);
   float* pos = s->pos;
   float* vel = s->vel;
   float* pred = s->predPos;
@@ -1259,7 +1265,6 @@ int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, cons
   float* cloud = s->cloud;
   float* buoy = s->buoyancy;
   const float dt = cp->timeStep;
-  const float fdt = fp->timeStep;
 
   // Thermodynamics, Clouds.cpp:516-529.
   std::vector<float> tempIn(temp, temp + n), cloudGen(n);
@@ -1293,7 +1298,7 @@ int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, cons
   // cloud, partID} (Clouds.cpp:541-543), table (:545-550).
   std::vector<uint32_t> keys(n), perm;
   or_fill_cell_ids(c, pred, n, keys.data());
-  std::vector<uint32_t> table(2 * (size_t)c->numCells);
+  table.assign(2 * (size_t)c->numCells, 0u);
   sort_and_table(c, n, keys, perm, s->cellId, table.data());
   gather4(pos, perm, n);
   gather4(vel, perm, n);
@@ -1353,57 +1358,80 @@ int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, cons
     }
     for (uint32_t i = 0; i < n; ++i) temp[i] += 0.3f * corrT[i];
   }
+}
 
-  std::vector<float> density(n), lambda(n), corr(4 * (size_t)n);
-  for (uint32_t it = 0; it < iters; ++it) {  // Clouds.cpp:570-587
-    // cld_computeDensity, clouds.cl:305-360.
-    OR_PARALLEL_FOR
-    for (int64_t i = 0; i < (int64_t)n; ++i) {
-      const f4 x = ld4(pred, i);
-      float rho = 0.0f;
-      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) { rho += k.poly6(x - ld4(pred, e) - sh); });
-      density[i] = rho;
-    }
-    // cld_computeConstraintFactor, clouds.cl:365-436.
-    OR_PARALLEL_FOR
-    for (int64_t i = 0; i < (int64_t)n; ++i) {
-      const f4 x = ld4(pred, i);
-      const float densityC = density[i] / fp->restDensity - 1.0f;
-      f4 sg = splat(0.0f);
-      float sq = 0.0f;
-      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
-        const f4 gr = k.grad(x - ld4(pred, e) - sh);
-        sg = sg + gr;
-        sq += dot(gr, gr);
-      });
-      sq += dot(sg, sg);
-      sq /= fp->restDensity * fp->restDensity;
-      lambda[i] = -densityC / (sq + fp->relaxCFM);
-    }
-    // cld_computeConstraintCorrection, clouds.cl:441-502.
-    OR_PARALLEL_FOR
-    for (int64_t i = 0; i < (int64_t)n; ++i) {
-      const f4 x = ld4(pred, i);
-      const float li = lambda[i];
-      f4 a = splat(0.0f);
-      cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
-        const f4 vec = x - ld4(pred, e) - sh;
-        a = a + (li + lambda[e] + k.artPressure(vec, fp)) * k.grad(vec);
-      });
-      st4(corr.data(), i, a / fp->restDensity);
-    }
-    // cld_correctPosition on predPos and totCorrPos, then the BC (Clouds.cpp:579-586).
-    OR_PARALLEL_FOR
-    for (int64_t i = 0; i < (int64_t)n; ++i) {
-      const f4 cr = ld4(corr.data(), i);
-      st4(pred, i, ld4(pred, i) + cr);
-      st4(tot, i, ld4(tot, i) + cr);
-      st4(pred, i, mixed_bc(g, ld4(pred, i)));
-    }
+// cld_computeDensity (clouds.cl:305-360) and cld_computeConstraintFactor (:365-436) at pred.
+void cloud_lambda(const Grid& g, const Sph& k, const rtp_fluid_params* fp, const float* pred, const uint32_t* T,
+                  uint32_t n, float* density, float* lambda) {
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 x = ld4(pred, i);
+    float rho = 0.0f;
+    cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) { rho += k.poly6(x - ld4(pred, e) - sh); });
+    density[i] = rho;
   }
-  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
-  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 x = ld4(pred, i);
+    const float densityC = density[i] / fp->restDensity - 1.0f;
+    f4 sg = splat(0.0f);
+    float sq = 0.0f;
+    cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+      const f4 gr = k.grad(x - ld4(pred, e) - sh);
+      sg = sg + gr;
+      sq += dot(gr, gr);
+    });
+    sq += dot(sg, sg);
+    sq /= fp->restDensity * fp->restDensity;
+    lambda[i] = -densityC / (sq + fp->relaxCFM);
+  }
+}
 
+// cld_computeConstraintCorrection (clouds.cl:441-502), then cld_correctPosition on predPos
+// and totCorrPos and the mixed boundary (Clouds.cpp:579-586).
+void cloud_correct(const Grid& g, const Sph& k, const rtp_fluid_params* fp, float* pred, float* tot,
+                   const float* lambda, const uint32_t* T, uint32_t n, float* corr) {
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 x = ld4(pred, i);
+    const float li = lambda[i];
+    f4 a = splat(0.0f);
+    cloud_neighbours(g, T, x, [&](uint32_t e, f4 sh) {
+      const f4 vec = x - ld4(pred, e) - sh;
+      a = a + (li + lambda[e] + k.artPressure(vec, fp)) * k.grad(vec);
+    });
+    st4(corr, i, a / fp->restDensity);
+  }
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const f4 cr = ld4(corr, i);
+    st4(pred, i, ld4(pred, i) + cr);
+    st4(tot, i, ld4(tot, i) + cr);
+    st4(pred, i, mixed_bc(g, ld4(pred, i)));
+  }
+}
+
+// The Jacobi loop of Clouds.cpp:570-587; density and lambda keep the last sweep's values.
+void cloud_jacobi(const Grid& g, const Sph& k, const rtp_fluid_params* fp, uint32_t iters, float* pred, float* tot,
+                  const uint32_t* T, uint32_t n, std::vector<float>& density, std::vector<float>& lambda) {
+  std::vector<float> corr(4 * (size_t)n);
+  for (uint32_t it = 0; it < iters; ++it) {
+    cloud_lambda(g, k, fp, pred, T, n, density.data(), lambda.data());
+    cloud_correct(g, k, fp, pred, tot, lambda.data(), T, n, corr.data());
+  }
+}
+
+// Clouds.cpp:590-610: velocities from the total correction, vorticity confinement and XSPH
+// viscosity, the wind drift into the new positions.
+void clouds_post(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                 const CloudEnv& E, uint32_t n, or_state* s, const uint32_t* T) {
+  const Grid g(c);
+  const Sph k(c);
+  float* pos = s->pos;
+  float* vel = s->vel;
+  const float* pred = s->predPos;
+  const float* tot = s->totCorrPos;
+  const float fdt = fp->timeStep;
   // cld_updateVel, clouds.cl:958-966.
   OR_PARALLEL_FOR
   for (int64_t i = 0; i < (int64_t)n; ++i)
@@ -1453,6 +1481,138 @@ int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, cons
     p.z += (1 - std::exp(-alt * E.windZ)) * 0.7f * cp->windCoeff * cp->timeStep;
     st4(pos, i, p);
   }
+}
+
+// Feature sums of the clouds warm start for particle i at x0 (clouds.cu k_cloud_ws_lambda):
+// the neighbour count (self excluded, periodic images included), C, h/rho0 sum gradW,
+// (h/rho0)^2 sum |gradW|^2, dt/rho0 sum (v_j - v_i).gradW, the buoyancy's displacement
+// b dt^2 / h, the y-wall proximity, (T - T_env) / 10, the plain lambda and |v| dt / h.
+void cloud_ws_features_one(const Grid& g, const Sph& k, const rtp_fluid_params* p, const CloudEnv& E,
+                           const float* x0, const float* vel, const float* temp, const float* buoy,
+                           const uint32_t* T, int64_t i, float* f) {
+  const f4 pos = ld4(x0, i), vi = ld4(vel, i);
+  float rho = 0.0f, ssq = 0.0f, div = 0.0f;
+  f4 sg = splat(0.0f);
+  uint32_t cnt = 0;
+  const float h2 = k.h * k.h;
+  cloud_neighbours(g, T, pos, [&](uint32_t e, f4 sh) {
+    const f4 v = pos - ld4(x0, e) - sh;
+    rho += k.poly6(v);
+    const f4 gr = k.grad(v);
+    sg = sg + gr;
+    ssq += dot(gr, gr);
+    const float r2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (((int64_t)e != i || sh.x != 0.0f || sh.z != 0.0f) && r2 < h2) {
+      ++cnt;
+      const f4 dv = ld4(vel, e) - vi;
+      div += dv.x * gr.x + dv.y * gr.y + dv.z * gr.z;
+    }
+  });
+  const float C = rho / p->restDensity - 1.0f;
+  float sq = ssq + dot(sg, sg);
+  sq /= p->restDensity * p->restDensity;
+  const float hr = k.h / p->restDensity, invH = 1.0f / k.h;
+  f[0] = (float)cnt;
+  f[1] = C;
+  f[2] = sg.x * hr;
+  f[3] = sg.y * hr;
+  f[4] = sg.z * hr;
+  f[5] = ssq * hr * hr;
+  f[6] = div * (p->timeStep / p->restDensity);
+  f[7] = buoy[i] * p->timeStep * p->timeStep * invH;
+  f[8] = std::fmin(std::fmax(2.0f - (pos.y + g.W[1]) * invH, 0.0f), 2.0f) -
+         std::fmin(std::fmax(2.0f - (g.W[1] - pos.y) * invH, 0.0f), 2.0f);
+  f[9] = (temp[i] - E.envTemp(pos)) * 0.1f;
+  f[10] = -C / (sq + p->relaxCFM);
+  f[11] = std::sqrt(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * p->timeStep * invH;
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                   const rtp_cloud_env* env, const float* ground, uint32_t iters, uint32_t n,
+                   or_state* s) {
+  if (!c || !fp || !cp || !env || !clouds_state_ok(s)) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const CloudEnv E(c, env, ground);
+  std::vector<uint32_t> table;
+  clouds_presort(c, cp, E, n, s, table);
+  std::vector<float> density(n), lambda(n);
+  cloud_jacobi(g, k, fp, iters, s->predPos, s->totCorrPos, table.data(), n, density, lambda);
+  if (s->density) std::memcpy(s->density, density.data(), sizeof(float) * n);
+  if (s->lambda) std::memcpy(s->lambda, lambda.data(), sizeof(float) * n);
+  clouds_post(c, fp, cp, E, n, s, table.data());
+  return RTP_OK;
+}
+
+void or_clouds_ws_features(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_env* env,
+                           const float* ground, const float* x0, const float* vel, const float* temp,
+                           const float* buoy, const uint32_t* table, uint32_t n, float* feats) {
+  const Grid g(c);
+  const Sph k(c);
+  const CloudEnv E(c, env, ground);
+  OR_PARALLEL_FOR
+  for (int64_t i = 0; i < (int64_t)n; ++i)
+    cloud_ws_features_one(g, k, fp, E, x0, vel, temp, buoy, table, i, feats + 12 * i);
+}
+
+// The training loss of the clouds warm start (runtime.cu cloud_train_pass): after the step's
+// presort, L = mean (rho(x') / rho0 - 1)^2 at x' = the relaxed first correction of x* under
+// the mixed boundary, with the step's cell table.  s advances through the presort.
+int or_clouds_ws_loss(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                      const rtp_cloud_env* env, const float* ground, const rtp_mlp* net, int emulate, uint32_t n,
+                      or_state* s, double* loss, float* featsOut) {
+  if (!c || !fp || !cp || !env || !net || !loss || !clouds_state_ok(s)) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const CloudEnv E(c, env, ground);
+  std::vector<uint32_t> table;
+  clouds_presort(c, cp, E, n, s, table);
+  std::vector<float> feats(12 * (size_t)n), out(4 * (size_t)n), lam(n), corr(4 * (size_t)n), rho(n), lamOut(n);
+  or_clouds_ws_features(c, fp, env, ground, s->predPos, s->vel, s->temp, s->buoyancy, table.data(), n, feats.data());
+  or_mlp_forward(net, feats.data(), n, emulate, out.data());
+  for (uint32_t i = 0; i < n; ++i) lam[i] = ws_omega(out[4 * (size_t)i]) * feats[12 * (size_t)i + 10];
+  cloud_correct(g, k, fp, s->predPos, s->totCorrPos, lam.data(), table.data(), n, corr.data());
+  cloud_lambda(g, k, fp, s->predPos, table.data(), n, rho.data(), lamOut.data());
+  double acc = 0.0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double C = (double)(rho[i] / fp->restDensity - 1.0f);
+    acc += C * C;
+  }
+  *loss = n ? acc / n : 0.0;
+  if (featsOut) std::memcpy(featsOut, feats.data(), sizeof(float) * feats.size());
+  return RTP_OK;
+}
+
+// The warm-started clouds step (runtime.cu clouds_solve_post with a network): the network
+// relaxes the plain first-iteration lambda, lambda <- omega(y) lambda, then extraIters plain
+// iterations follow.  feats/omega (optional, rows by sorted index) return the network's
+// inputs and relaxations.
+int or_clouds_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                      const rtp_cloud_env* env, const float* ground, const rtp_mlp* net, uint32_t extraIters,
+                      uint32_t n, or_state* s, float* featsOut, float* omegaOut) {
+  if (!c || !fp || !cp || !env || !net || !clouds_state_ok(s)) return RTP_ERR_INVALID_ARGUMENT;
+  const Grid g(c);
+  const Sph k(c);
+  const CloudEnv E(c, env, ground);
+  std::vector<uint32_t> table;
+  clouds_presort(c, cp, E, n, s, table);
+  std::vector<float> feats(12 * (size_t)n), out(4 * (size_t)n), lam(n), corr(4 * (size_t)n);
+  or_clouds_ws_features(c, fp, env, ground, s->predPos, s->vel, s->temp, s->buoyancy, table.data(), n, feats.data());
+  or_mlp_forward(net, feats.data(), n, 1, out.data());
+  for (uint32_t i = 0; i < n; ++i) {
+    const float om = ws_omega(out[4 * (size_t)i]);
+    lam[i] = om * feats[12 * (size_t)i + 10];
+    if (omegaOut) omegaOut[i] = om;
+  }
+  if (featsOut) std::memcpy(featsOut, feats.data(), sizeof(float) * feats.size());
+  cloud_correct(g, k, fp, s->predPos, s->totCorrPos, lam.data(), table.data(), n, corr.data());
+  std::vector<float> density(n), lambda(n);
+  cloud_jacobi(g, k, fp, extraIters, s->predPos, s->totCorrPos, table.data(), n, density, lambda);
+  clouds_post(c, fp, cp, E, n, s, table.data());
   return RTP_OK;
 }
 

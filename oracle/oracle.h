@@ -80,6 +80,24 @@ void or_target_trajectory(float boxWidth, int dim, float particlesVel, uint32_t 
 int or_clouds_step(const rtp_grid_constants* c, const rtp_fluid_params* fp,
                    const rtp_cloud_params* cp, const rtp_cloud_env* env, const float* ground,
                    uint32_t iters, uint32_t n, or_state* s);
+/* The clouds warm-start features at sorted positions x0 (rows of 12: the neighbour count,
+ * C, h/rho0 sum gradW (3), (h/rho0)^2 sum |gradW|^2, dt/rho0 sum (v_j - v_i).gradW,
+ * b dt^2 / h, the y-wall proximity, (T - T_env) / 10, the plain lambda, |v| dt / h). */
+void or_clouds_ws_features(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_env* env,
+                           const float* ground, const float* x0, const float* vel, const float* temp,
+                           const float* buoy, const uint32_t* table, uint32_t n, float* feats);
+/* One warm-started Clouds::update: the network relaxes the first iteration's lambda by
+ * omega(y) (BF16 operand rounding as on the GPU), then extraIters plain iterations.
+ * featsOut (12 n) and omegaOut (n), rows by sorted index, may be NULL. */
+int or_clouds_ws_step(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                      const rtp_cloud_env* env, const float* ground, const rtp_mlp* net, uint32_t extraIters,
+                      uint32_t n, or_state* s, float* featsOut, float* omegaOut);
+/* The clouds warm start's training loss: after the step's presort (s advances through it),
+ * mean (rho(x')/rho0 - 1)^2 at the relaxed first correction x' (emulate = the GPU's BF16
+ * operand rounding in the network).  featsOut (12 n, sorted rows) may be NULL. */
+int or_clouds_ws_loss(const rtp_grid_constants* c, const rtp_fluid_params* fp, const rtp_cloud_params* cp,
+                      const rtp_cloud_env* env, const float* ground, const rtp_mlp* net, int emulate, uint32_t n,
+                      or_state* s, double* loss, float* featsOut);
 /* cld_initTemperature + cld_initVaporDensity (clouds.cl:116-135), cloud = 0. */
 void or_clouds_init(const rtp_grid_constants* c, const rtp_cloud_params* cp,
                     const rtp_cloud_env* env, const float* ground, uint32_t n, or_state* s);

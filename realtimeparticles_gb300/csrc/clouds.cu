@@ -17,6 +17,7 @@
 // within h (entry = particle index | image code << 28) for the sweeps that follow at the
 // same positions, which give 4 lanes to each particle.
 #include "clouds.cuh"
+#include "mlp.cuh"
 
 namespace rtp {
 
@@ -360,6 +361,222 @@ __global__ void __launch_bounds__(kSweepThreads, 16) k_cloud_lambda(GridK g, Flu
   packed[i] = f4(xi.x, xi.y, xi.z, lam);
 }
 
+// ---- learned warm start of the clouds solve (new: the reference's Jacobi loop,
+// Clouds.cpp:570-587, starts every substep from a zero correction) -----------------------
+// The fluids method (warmstart.cu) on the clouds sweep: the first density / lambda sweep of a
+// substep also sums the network's features (layout in rtp.h: the fluids features with the x
+// and z wall proximities, always 0 under the periodic boundary, replaced by the buoyant
+// displacement of the step and the temperature above the environment), then each warp
+// evaluates the network and relaxes lambda by omega(y) in (0, 3), omega(0) = 1 exactly.
+constexpr int kCwsRecord = 0, kCwsInfer = 1;
+
+__device__ __forceinline__ float cws_omega(float y) { return 1.0f + tanhf(y) * (y > 0.0f ? 2.0f : 1.0f); }
+__device__ __forceinline__ float cws_omega_grad(float y) {
+  const float t = tanhf(y);
+  return (1.0f - t * t) * (y > 0.0f ? 2.0f : 1.0f);
+}
+
+// kCwsRecord: plain lambda into lambda, (x, y, z, lambda) into packed, the features of every
+// particle into feats (rows of kMlpIn).  kCwsInfer: omega(network) lambda into lambda and packed.
+// Both record the pairs within h (entries with image codes) into pl.
+template <int MODE>
+__global__ void __launch_bounds__(kSweepThreads, MODE == kCwsRecord ? 16 : 14)
+    k_cloud_ws_lambda(GridK g, FluidK p, CloudK c, const float4* __restrict__ pred, const float4* __restrict__ velS,
+                      const float* __restrict__ tempS, const float* __restrict__ buoyS,
+                      const uint2* __restrict__ table, uint32_t n, float* __restrict__ lambda,
+                      float* __restrict__ density, PairList pl, float4* __restrict__ packed,
+                      float* __restrict__ feats, MlpDev m) {
+  pdl_enter();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  float f[kMlpIn];
+#pragma unroll
+  for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+  float lam = 0.0f;
+  float4 xi = f4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    const Sph k(g);
+    xi = ld4(pred + i);
+    const float4 vi = ld4(velS + i);
+    ListWriter lw(pl, i);
+    filter_cloud_neighbours(g, table, pred, xi, k.h2, lw);
+    float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f, div = 0.0f;
+    uint32_t cnt = 0;
+    auto body_at = [&](uint32_t j, float4 xj, float4 vj, float shx, float shz) {
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        rho += k.w(r2);
+        float r;
+        const float s = k.gs(r2, r);
+        const float a = vx * s, b = vy * s, cc = vz * s;
+        sgx += a;
+        sgy += b;
+        sgz += cc;
+        ssq += a * a + b * b + cc * cc;
+        if (j != i || shx != 0.0f || shz != 0.0f) {
+          ++cnt;
+          div += (vj.x - vi.x) * a + (vj.y - vi.y) * b + (vj.z - vi.z) * cc;
+        }
+      }
+    };
+    if (lw.ok())
+      visit_list_x4(0, lw.n, 1, [&](uint32_t kk) { return lw.at(kk); },
+                    [&](uint32_t e) { return Pair44{ld4(pred + (e & 0x0FFFFFFFu)), ld4(velS + (e & 0x0FFFFFFFu))}; },
+                    [&](uint32_t e, Pair44 a) {
+                      float shx, shz;
+                      image_shift(g, e >> 28, shx, shz);
+                      body_at(e & 0x0FFFFFFFu, a.x, a.v, shx, shz);
+                    });
+    else
+      for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+        body_at(j, ld4(pred + j), ld4(velS + j), shx, shz);
+      });
+    pl.count[i] = lw.ok() ? lw.n : kListOverflow;
+    // cld_computeConstraintFactor, same operations as k_cloud_lambda.
+    const float C = rho / p.rho0 - 1.0f;
+    const float ssqRaw = ssq;
+    ssq += sgx * sgx + sgy * sgy + sgz * sgz;
+    ssq *= p.invRho0Sq;
+    lam = -C / (ssq + p.relaxCFM);
+    density[i] = rho;
+    const float hr = g.h * p.invRho0, invH = 1.0f / g.h;
+    f[0] = (float)cnt;
+    f[1] = C;
+    f[2] = sgx * hr;
+    f[3] = sgy * hr;
+    f[4] = sgz * hr;
+    f[5] = ssqRaw * hr * hr;
+    f[6] = div * (p.dt * p.invRho0);
+    f[7] = __ldg(buoyS + i) * p.dt * p.dt * invH;
+    f[8] = fminf(fmaxf(2.0f - (xi.y + g.W[1]) * invH, 0.0f), 2.0f) - fminf(fmaxf(2.0f - (g.W[1] - xi.y) * invH, 0.0f), 2.0f);
+    f[9] = (__ldg(tempS + i) - env_temp(c, g, xi)) * 0.1f;
+    f[10] = lam;
+    f[11] = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * p.dt * invH;
+  }
+  if constexpr (MODE == kCwsRecord) {
+    if (!active) return;
+    lambda[i] = lam;
+    packed[i] = f4(xi.x, xi.y, xi.z, lam);
+    float* o = feats + (size_t)i * kMlpIn;
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) o[k] = f[k];
+  } else {
+    __shared__ uint32_t s_stage[kSweepThreads / 32][32 * 9];
+    float x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) x[k] = active ? (f[k] - __ldg(m.inMean + k)) * __ldg(m.inScale + k) : 0.0f;
+    __syncwarp();
+    float y[kMlpOut];
+    mlp_warp_forward(m, x, y, s_stage[threadIdx.x >> 5]);
+    if (!active) return;
+    const float lw = cws_omega(y[0] * __ldg(m.outScale + 0)) * lam;
+    lambda[i] = lw;
+    packed[i] = f4(xi.x, xi.y, xi.z, lw);
+  }
+}
+
+// Backward of L = invN sum C'^2 to the corrected positions x' (the clouds density sweep at x'
+// recorded pl2 and rho2): g_m = 2 invN / rho0 sum_j (C'_m + C'_j) gradW_poly6(x'_m - x'_j -
+// image shift), zero in y where the mixed boundary held x' on a y wall.  lossPart[block] = sum
+// of C'^2 over its particles.
+__global__ void __launch_bounds__(128) k_cloud_ws_loss_grad_x(GridK g, FluidK p, const float4* __restrict__ xp,
+                                                              const float* __restrict__ rho2,
+                                                              const uint2* __restrict__ table, uint32_t n, PairList pl2,
+                                                              float invN, float4* __restrict__ gOut,
+                                                              float* __restrict__ lossPart) {
+  __shared__ float s_loss[128 / kQuad];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;
+  const Sph k(g);
+  const float4 xi = ld4(xp + ii);
+  const float ci = __ldg(rho2 + ii) * p.invRho0 - 1.0f;
+  float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+  if (active)
+    quad_cloud_pairs(g, table, pl2, i, q, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(xp + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        const float d = k.h2 - r2;
+        const float f = (ci + (__ldg(rho2 + j) * p.invRho0 - 1.0f)) * (-6.0f * k.poly6 * d * d);
+        gx += vx * f;
+        gy += vy * f;
+        gz += vz * f;
+      }
+    });
+  gx = quad_sum(gx);
+  gy = quad_sum(gy);
+  gz = quad_sum(gz);
+  const float sc = 2.0f * invN * p.invRho0;
+  if (q == 0) s_loss[threadIdx.x / kQuad] = active ? ci * ci : 0.0f;
+  if (active && q == 0) {
+    const bool held = fabsf(xi.y) >= g.W[1];
+    gOut[i] = f4(gx * sc, held ? 0.0f : gy * sc, gz * sc, 0.0f);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = 0.0f;
+    for (int u = 0; u < 128 / kQuad; ++u) a += s_loss[u];
+    lossPart[blockIdx.x] = a;
+  }
+}
+
+// dL/dy_k = omega'(y_k) lambda_k / rho0 sum_j (g_k - g_j) . gradSpiky(x*_k - x*_j - image shift),
+// rows of kMlpOut (output 0).
+__global__ void __launch_bounds__(128) k_cloud_ws_grad_y(GridK g, FluidK p, const float4* __restrict__ xs,
+                                                         const float* __restrict__ lam, const float* __restrict__ y,
+                                                         const float4* __restrict__ gIn,
+                                                         const uint2* __restrict__ table, uint32_t n, PairList pl,
+                                                         float* __restrict__ dy) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / kQuad, q = t % kQuad;
+  const bool active = i < n;
+  const uint32_t ii = active ? i : n - 1u;
+  const Sph k(g);
+  const float4 xi = ld4(xs + ii), gi = ld4(gIn + ii);
+  float acc = 0.0f;
+  if (active)
+    quad_cloud_pairs(g, table, pl, i, q, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(xs + j), gj = ld4(gIn + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) {
+        float r;
+        const float s = k.gs(r2, r);
+        acc += ((gi.x - gj.x) * vx + (gi.y - gj.y) * vy + (gi.z - gj.z) * vz) * s;
+      }
+    });
+  acc = quad_sum(acc);
+  if (!active || q != 0) return;
+  *reinterpret_cast<float4*>(dy + (size_t)i * kMlpOut) =
+      f4(cws_omega_grad(__ldg(y + (size_t)i * kMlpOut)) * __ldg(lam + i) * p.invRho0 * acc, 0.0f, 0.0f, 0.0f);
+}
+
+// Per-block sums of |rho_i / rho0 - 1| at pos (the solver statistics of a clouds step).
+__global__ void __launch_bounds__(kSweepThreads) k_cloud_density_error(GridK g, FluidK p, const float4* __restrict__ pos,
+                                                                       const uint2* __restrict__ table, uint32_t n,
+                                                                       float* __restrict__ errPartial) {
+  pdl_enter();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float err = 0.0f;
+  if (i < n) {
+    const Sph k(g);
+    const float4 xi = ld4(pos + i);
+    float rho = 0.0f;
+    for_each_cloud_neighbour(g, table, xi, [&](uint32_t j, float shx, float shz) {
+      const float4 xj = ld4(pos + j);
+      const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
+      const float r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < k.h2) rho += k.w(r2);
+    });
+    err = fabsf(rho / p.rho0 - 1.0f);
+  }
+  block_error_partial(err, errPartial);
+}
+
 // cld_computeConstraintCorrection, cld_correctPosition x2 and the mixed boundary
 // (Clouds.cpp:577-586); LAST adds cld_updateVel (clouds.cl:958-966).  kQuad lanes.
 template <bool LAST>
@@ -610,6 +827,73 @@ int cloud_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
                                                                          velS, pl, packed);
   L.end(last ? "cld_deltap_vel" : "cld_deltap");
   return check("k_cloud_deltap");
+}
+
+int cloud_ws_lambda(const GridK& g, const FluidK& p, const CloudK& c, const float4* pred, const float4* velS,
+                    const float* tempS, const float* buoyS, const uint2* table, uint32_t n, float* lambda,
+                    float* density, const PairList& pl, float4* packed, float* feats, const void* mlpBlock,
+                    Launcher& L) {
+  if (n == 0) return RTP_OK;
+  if (feats) {
+    MlpDev m{};
+    L.begin("cld_ws_features");
+    launch(L, k_cloud_ws_lambda<kCwsRecord>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, c, pred, velS,
+           tempS, buoyS, table, n, lambda, density, pl, packed, feats, m);
+    L.end("cld_ws_features");
+  } else {
+    L.begin("cld_ws_lambda_mlp");
+    launch(L, k_cloud_ws_lambda<kCwsInfer>, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, c, pred, velS,
+           tempS, buoyS, table, n, lambda, density, pl, packed, (float*)nullptr, mlp_dev(mlpBlock));
+    L.end("cld_ws_lambda_mlp");
+  }
+  return check("k_cloud_ws_lambda");
+}
+
+int cloud_deltap(const GridK& g, const FluidK& p, const float4* predIn, float4* predOut, float4* totS,
+                 const float* lambda, const uint2* table, uint32_t n, bool last, float4* velS, const PairList& pl,
+                 Launcher& L, const float4* packed) {
+  L.begin(last ? "cld_deltap_vel" : "cld_deltap");
+  if (last)
+    launch(L, k_cloud_deltap<true>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut,
+           totS, velS, pl, packed);
+  else
+    launch(L, k_cloud_deltap<false>, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, predIn, lambda, table, n, predOut,
+           totS, velS, pl, packed);
+  L.end(last ? "cld_deltap_vel" : "cld_deltap");
+  return check("k_cloud_deltap");
+}
+
+int cloud_density(const GridK& g, const FluidK& p, const float4* pred, const uint2* table, uint32_t n, float* lambda,
+                  float* density, const PairList& pl, float4* packed, Launcher& L) {
+  L.begin("cld_lambda");
+  launch(L, k_cloud_lambda, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, pred, table, n, lambda, density,
+         pl, packed);
+  L.end("cld_lambda");
+  return check("k_cloud_lambda");
+}
+
+int cloud_ws_loss_grad_x(const GridK& g, const FluidK& p, const float4* xp, const float* rho2, const uint2* table,
+                         uint32_t n, const PairList& pl2, float4* gOut, float* lossPart, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_cloud_ws_loss_grad_x, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, xp, rho2, table, n, pl2,
+         (float)(1.0 / (double)n), gOut, lossPart);
+  return check("k_cloud_ws_loss_grad_x");
+}
+
+int cloud_ws_grad_y(const GridK& g, const FluidK& p, const float4* xs, const float* lam, const float* y,
+                    const float4* gIn, const uint2* table, uint32_t n, const PairList& pl, float* dy, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  launch(L, k_cloud_ws_grad_y, dim3(blocks(n * kQuad, 128)), dim3(128), g, p, xs, lam, y, gIn, table, n, pl, dy);
+  return check("k_cloud_ws_grad_y");
+}
+
+int cloud_density_error(const GridK& g, const FluidK& p, const float4* pos, const uint2* table, uint32_t n,
+                        float* errPartial, Launcher& L) {
+  if (n == 0) return RTP_OK;
+  L.begin("cld_density_error");
+  launch(L, k_cloud_density_error, dim3(blocks(n, kSweepThreads)), dim3(kSweepThreads), g, p, pos, table, n, errPartial);
+  L.end("cld_density_error");
+  return check("k_cloud_density_error");
 }
 
 int cloud_update_vel(const GridK& g, const FluidK& p, const float4* totS, uint32_t n, float4* velS, Launcher& L) {

@@ -728,12 +728,11 @@ static CloudK make_cloudk(const Handle* h) {
   return c;
 }
 
-// Clouds::update (Clouds.cpp:503-610).
-int record_clouds_step(Handle* h, Launcher& L) {
+// Clouds.cpp:516-567: thermodynamics, predict, mixed boundary, cell ids, the sort, the cell
+// table and the temperature smoothing.
+static int clouds_presort(Handle* h, Launcher& L) {
   const uint32_t n = (uint32_t)h->curN;
-  if (n == 0) return RTP_OK;
   const GridK& g = h->g;
-  const FluidK fk = fluidk_of(h);
   const CloudK ck = make_cloudk(h);
   const SortPlan plan = make_sort_plan(n, h->gc.keyBits);
   const ZeroJob zero = step_zero_job(plan, h->ss, h->table, h->gc.numCells);
@@ -768,16 +767,39 @@ int record_clouds_step(Handle* h, Launcher& L) {
   // Clouds.cpp:554-567.
   if (ck.smoothing)
     RTP_TRY(cloud_temperature(g, ck, h->posS, h->tempS, h->lamT, h->table, n, h->pairs, L, h->predLam));
-  // Clouds.cpp:570-590.
+  return RTP_OK;
+}
+
+// Clouds.cpp:570-590 from predA: the plain Jacobi loop, or with `block` the warm-started first
+// iteration (the network relaxes the plain lambda) and E plain iterations; then (statistics)
+// the solver output's density error, then Clouds.cpp:592-605.
+static int clouds_solve_post(Handle* h, Launcher& L, const void* block, uint32_t E) {
+  const uint32_t n = (uint32_t)h->curN;
+  const GridK& g = h->g;
+  const FluidK fk = fluidk_of(h);
+  const CloudK ck = make_cloudk(h);
   float4* cur = h->predA;
   float4* nxt = h->predB;
-  for (uint32_t it = 0; it < h->iters; ++it) {
-    RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == h->iters,
+  uint32_t iters = h->iters;
+  if (block) {
+    RTP_TRY(cloud_ws_lambda(g, fk, ck, h->predA, h->velS, h->tempS, h->buoyS, h->table, n, h->lambda, h->density,
+                            h->pairs, h->predLam, nullptr, block, L));
+    RTP_TRY(cloud_deltap(g, fk, cur, nxt, h->totCorrS, h->lambda, h->table, n, E == 0, h->velS, h->pairs, L,
+                         h->predLam));
+    std::swap(cur, nxt);
+    iters = E;
+  }
+  for (uint32_t it = 0; it < iters; ++it) {
+    RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == iters,
                             h->velS, h->pairs, L, h->predLam));
     std::swap(cur, nxt);
   }
-  if (h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
+  if (!block && h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
   h->predFinal = cur;
+  if (h->statsOn) {
+    RTP_TRY(cloud_density_error(g, fk, cur, h->table, n, h->errPartial, L));
+    RTP_TRY(ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, false, L));
+  }
   // Clouds.cpp:592-605.
   CloudState s;
   s.pos = h->pos;
@@ -793,6 +815,49 @@ int record_clouds_step(Handle* h, Launcher& L) {
   s.ids = h->ids;
   s.idsS = h->idsS;
   return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, h->pairs, L, h->predLam);
+}
+
+// clouds_presort for rtp_warm_start_loss_grad: the thermodynamics it runs change temp, vapor,
+// cloud and buoyancy in place, so they are saved first and put back after (the sorted copies
+// the training pass reads are kept).
+static int clouds_presort_keep_state(Handle* h, Launcher& L) {
+  const size_t b = sizeof(float) * h->curN;
+  float* save[4] = {h->temp, h->vapor, h->cloud, h->buoy};
+  // Scratch: the network-output rows (4 floats a particle), written only after the restore.
+  for (int k = 0; k < 4; ++k)
+    RTP_CUDA(cudaMemcpyAsync(h->trY + (size_t)k * h->curN, save[k], b, cudaMemcpyDeviceToDevice, L.stream));
+  RTP_TRY(clouds_presort(h, L));
+  for (int k = 0; k < 4; ++k)
+    RTP_CUDA(cudaMemcpyAsync(save[k], h->trY + (size_t)k * h->curN, b, cudaMemcpyDeviceToDevice, L.stream));
+  return RTP_OK;
+}
+
+// Clouds::update (Clouds.cpp:503-610).
+int record_clouds_step(Handle* h, Launcher& L) {
+  if (h->curN == 0) return RTP_OK;
+  RTP_TRY(clouds_presort(h, L));
+  return clouds_solve_post(h, L, h->wsOn ? h->mlpBlock : nullptr, h->wsExtra);
+}
+
+// Training through the clouds solve after clouds_presort (x* = predA): as ws_train_pass, with
+// the clouds sweeps (periodic images in x and z, the mixed boundary) and the step's total
+// correction left untouched (the correction is applied to a copy of it).
+static int cloud_train_pass(Handle* h, Launcher& L, bool skipFeatures) {
+  const uint32_t n = (uint32_t)h->curN;
+  const GridK& g = h->g;
+  const FluidK fk = fluidk_of(h);
+  const CloudK ck = make_cloudk(h);
+  if (!skipFeatures)
+    RTP_TRY(cloud_ws_lambda(g, fk, ck, h->predA, h->velS, h->tempS, h->buoyS, h->table, n, h->trLam, h->density,
+                            h->pairs, h->predLam, h->trFeats, nullptr, L));
+  RTP_TRY(ws_trainer_forward(h->trainer, h->trFeats, n, h->trY, L.stream));
+  RTP_TRY(ws_apply_omega(h->predA, h->trLam, h->trY, n, h->lambda, h->predLam, L));
+  RTP_CUDA(cudaMemcpyAsync(h->vort, h->totCorrS, sizeof(float4) * n, cudaMemcpyDeviceToDevice, L.stream));
+  RTP_TRY(cloud_deltap(g, fk, h->predA, h->trXp, h->vort, h->lambda, h->table, n, false, h->velS, h->pairs, L,
+                       h->predLam));
+  RTP_TRY(cloud_density(g, fk, h->trXp, h->table, n, h->lamT, h->trRho, h->pairsRec, h->predLam, L));
+  RTP_TRY(cloud_ws_loss_grad_x(g, fk, h->trXp, h->trRho, h->table, n, h->pairsRec, h->trG, h->trLoss, L));
+  return cloud_ws_grad_y(g, fk, h->predA, h->trLam, h->trY, h->trG, h->table, n, h->pairs, h->trDy, L);
 }
 
 // ---- Model::reset: reference defaults + the case's initial particles ------------------
@@ -1845,7 +1910,9 @@ int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_co
   RTP_GUARD_BEGIN
   if (!handle || !cfg) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: null argument");
   Handle* h = H(handle);
-  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: fluids only");
+  if (h->model == RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: fluids and clouds only");
+  if (h->model == RTP_MODEL_CLOUDS && cfg->enabled && (cfg->guardTolerance > 0.0f || cfg->relaxAllIterations))
+    return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: clouds take no guard and no relaxation of every iteration");
   if (!cfg->enabled) {
     h->wsOn = false;
     invalidate(h);
@@ -1872,7 +1939,7 @@ int rtp_enable_solver_stats(void* handle, int enable) {
   RTP_GUARD_BEGIN
   if (!handle) return fail(RTP_ERR_INVALID_ARGUMENT, "null handle");
   Handle* h = H(handle);
-  if (h->model != RTP_MODEL_FLUIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_enable_solver_stats: fluids only");
+  if (h->model == RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_enable_solver_stats: fluids and clouds only");
   if (enable) RTP_TRY(ws_alloc(h));
   h->statsOn = enable != 0;
   invalidate(h);
@@ -1936,8 +2003,8 @@ int rtp_record_warm_start_samples(void* handle, uint32_t referenceIterations, ui
 }
 
 static int check_trainable(Handle* h, const char* who) {
-  if (h->model != RTP_MODEL_FLUIDS || h->isBatch)
-    return fail(RTP_ERR_NOT_SUPPORTED, std::string(who) + ": single fluids scenes only");
+  if (h->model == RTP_MODEL_BOIDS || h->isBatch)
+    return fail(RTP_ERR_NOT_SUPPORTED, std::string(who) + ": single fluids or clouds scenes only");
   if (h->curN == 0) return fail(RTP_ERR_STATE, std::string(who) + ": no particles");
   if (h->paused) return fail(RTP_ERR_STATE, std::string(who) + ": the model is paused");
   return RTP_OK;
@@ -1953,8 +2020,15 @@ int rtp_warm_start_loss_grad(void* handle, const rtp_mlp* net, float* d_dy, doub
   RTP_TRY(ws_trainer_set_net(h->trainer, *net, h->stream));
   Launcher L;
   L.stream = h->stream;
-  RTP_TRY(fluids_presort(h, L, fluidk_of(h), true));
-  RTP_TRY(ws_train_pass(h, L, false));
+  const bool clouds = h->model == RTP_MODEL_CLOUDS;
+  if (clouds) {
+    // The clouds presort advances the thermodynamic state: run it on a copy of it.
+    RTP_TRY(clouds_presort_keep_state(h, L));
+    RTP_TRY(cloud_train_pass(h, L, false));
+  } else {
+    RTP_TRY(fluids_presort(h, L, fluidk_of(h), true));
+    RTP_TRY(ws_train_pass(h, L, false));
+  }
   if (d_dy) RTP_TRY(ws_scatter_by_id(h->idsS, h->trDy, kMlpOut, n, d_dy, L));
   RTP_TRY(ws_train_loss(h, loss));
   return check_fault(h);
@@ -1973,19 +2047,26 @@ int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint
   Launcher L;
   L.stream = h->stream;
   const FluidK fk = fluidk_of(h);
+  const bool clouds = h->model == RTP_MODEL_CLOUDS;
   for (uint32_t s = 0; s < steps; ++s) {
-    RTP_TRY(fluids_presort(h, L, fk, true));
+    if (clouds) RTP_TRY(clouds_presort(h, L));
+    else RTP_TRY(fluids_presort(h, L, fk, true));
     bool haveFeatures = false;
     if (s == 0) {
       if (init) {
-        RTP_TRY(ws_lambda_record(h->g, fk, h->predA, h->velS, h->table, n, h->trLam, h->density, h->lamTot, h->pairs,
-                                 1, 0, h->trFeats, n, L));
+        if (clouds)
+          RTP_TRY(cloud_ws_lambda(h->g, fk, make_cloudk(h), h->predA, h->velS, h->tempS, h->buoyS, h->table, n,
+                                  h->trLam, h->density, h->pairs, h->predLam, h->trFeats, nullptr, L));
+        else
+          RTP_TRY(ws_lambda_record(h->g, fk, h->predA, h->velS, h->table, n, h->trLam, h->density, h->lamTot, h->pairs,
+                                   1, 0, h->trFeats, n, L));
         RTP_TRY(ws_init_net(h->trFeats, n, cfg->seed, *net, h->stream));
         haveFeatures = true;
       }
       RTP_TRY(ws_trainer_set_net(h->trainer, *net, h->stream));
     }
-    RTP_TRY(ws_train_pass(h, L, haveFeatures));
+    if (clouds) RTP_TRY(cloud_train_pass(h, L, haveFeatures));
+    else RTP_TRY(ws_train_pass(h, L, haveFeatures));
     double loss = 0.0;
     RTP_TRY(ws_train_loss(h, &loss));
     if (loss_history) loss_history[s] = (float)loss;
@@ -1994,10 +2075,14 @@ int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint
     RTP_TRY(ws_trainer_adam_step(h->trainer, h->trFeats, h->trDy, n, *cfg, lrScale, h->stream));
     // The simulation advances with the updated network (the states it trains on are the ones
     // the warm-started solver itself produces).
-    RTP_TRY(ws_first_iteration(h, L, fk, ws_trainer_block(h->trainer), extraIterations, false));
-    h->predFinal = h->predB;
-    RTP_TRY(fluid_post(h->g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
-                       false, HostIO{}, h->predLam));
+    if (clouds) {
+      RTP_TRY(clouds_solve_post(h, L, ws_trainer_block(h->trainer), extraIterations));
+    } else {
+      RTP_TRY(ws_first_iteration(h, L, fk, ws_trainer_block(h->trainer), extraIterations, false));
+      h->predFinal = h->predB;
+      RTP_TRY(fluid_post(h->g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs,
+                         L, false, HostIO{}, h->predLam));
+    }
     h->hasStep = true;
   }
   RTP_TRY(ws_trainer_get_net(h->trainer, *net, h->stream));

@@ -1,0 +1,173 @@
+"""Learned warm start of the clouds solve on the GPU against the oracle.
+
+The clouds Jacobi loop (Clouds.cpp:570-587) starts every step from a zero correction as the
+fluids one does; the network relaxes the first iteration's lambda by omega(y) in (0, 3), with
+features that see the clouds' periodic images in x and z, their y walls, the step's buoyancy
+and the temperature above the environment (clouds.cu k_cloud_ws_lambda).
+
+- warm-started steps (network + 0 or 1 extra iteration) against the oracle's restatement
+  (oracle.clouds_ws_step) within the clouds step tolerances;
+- an untrained network (zero output layer) is the plain clouds solver bit for bit;
+- the loss through the solve and its gradient dL/dy against the oracle, with the state left
+  where it was;
+- a network trained through the clouds solve on one seeded column lowers the solver-output
+  density error of the warm start with no extra iteration below the plain one-iteration
+  solver's (the clouds configuration's own iteration count) on a held-out seed.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from realtimeparticles_gb300 import abi, scenes, warmstart
+
+from helpers import REL_BOX, assert_close_by_id, box_size, clouds_model, gpu_state, random_net
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _copy(st):
+    return {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
+
+
+def _features(sc, st):
+    """The oracle's warm-start features of state st (a copy advances one step to get them)."""
+    c = oracle.derive_constants(abi.CLOUDS, sc["model_params"])
+    z = abi.mlp_to_arrays(abi.Mlp())
+    z["inScale"][:] = 1.0
+    f, _ = oracle.clouds_ws_step(c, sc["fluid_params"], sc["cloud_params"], sc["env"], sc["ground"],
+                                 abi.mlp_from_arrays(z), 0, _copy(st))
+    return f
+
+
+def _omega_net(rng, feats, out=0.3):
+    """A random network normalised on the scene's own features whose omega spans about 0.6-1.8."""
+    net = random_net(rng, out_scale=np.array([1.0, 1.0, 1.0, 1.0], np.float32))
+    a = abi.mlp_to_arrays(net)
+    mu, sd = feats.mean(axis=0), feats.std(axis=0)
+    a["inMean"][:] = mu
+    a["inScale"][:] = 1.0 / np.maximum(sd, 1e-6 * np.abs(mu) + 1e-30)
+    a["w3"][:] *= out / max(1e-6, float(np.abs(a["w3"]).max()))
+    a["b3"][:] = 0.0
+    return abi.mlp_from_arrays(a)
+
+
+def _zero_output(net):
+    a = abi.mlp_to_arrays(net)
+    a["w3"][:] = 0.0
+    a["b3"][:] = 0.0
+    return abi.mlp_from_arrays(a)
+
+
+@pytest.mark.parametrize("extra", [0, 1])
+def test_warm_started_clouds_steps_match_oracle(extra):
+    sc = scenes.clouds_cumulus(n=32768, noise=True, seed=1)
+    c = oracle.derive_constants(abi.CLOUDS, sc["model_params"])
+    fp, cp = sc["fluid_params"], sc["cloud_params"]
+    L = box_size(sc["model_params"])
+    with clouds_model(sc, iters=1) as m:
+        m.update(2)
+        net = _omega_net(np.random.default_rng(9), _features(sc, gpu_state(m, abi.CLOUDS)))
+        m.setWarmStart(net, extra_iterations=extra)
+        for step in range(3):
+            st = gpu_state(m, abi.CLOUDS)
+            _, om = oracle.clouds_ws_step(c, fp, cp, sc["env"], sc["ground"], net, extra, st)
+            if step == 0:
+                assert om.std() > 0.05, om.std()  # the network does relax lambda
+            m.update(1)
+            g = gpu_state(m, abi.CLOUDS)
+            assert np.array_equal(g["id"], st["id"])
+            assert_close_by_id(g["id"], g["pos"], st["id"], st["pos"], REL_BOX * L, "pos step %d" % step)
+            assert_close_by_id(g["id"], g["vel"], st["id"], st["vel"], REL_BOX * L / fp.timeStep, "vel")
+            assert_close_by_id(g["id"], g["temp"], st["id"], st["temp"], 1e-3, "temp")
+            assert_close_by_id(g["id"], g["vapor"], st["id"], st["vapor"], 1e-4, "vapor")
+
+
+@pytest.mark.parametrize("extra", [0, 1])
+def test_untrained_network_is_the_plain_clouds_solver(extra):
+    sc = scenes.clouds_cumulus(n=131072, noise=True)
+    with clouds_model(sc, iters=extra + 1) as plain, clouds_model(sc, iters=1) as warm:
+        net = _zero_output(_omega_net(np.random.default_rng(4), _features(sc, gpu_state(warm, abi.CLOUDS))))
+        warm.setWarmStart(net, extra_iterations=extra)
+        for _ in range(3):
+            plain.update(1)
+            warm.update(1)
+        a, b = gpu_state(plain, abi.CLOUDS), gpu_state(warm, abi.CLOUDS)
+        for k in ("id", "pos", "vel", "temp", "vapor", "cloud"):
+            assert np.array_equal(a[k], b[k]), k
+
+
+def test_guard_and_relax_all_are_refused_for_clouds():
+    sc = scenes.clouds_cumulus(n=4096)
+    net = abi.Mlp()
+    with clouds_model(sc) as m:
+        with pytest.raises(Exception):
+            m.setWarmStart(net, extra_iterations=0, guard_tolerance=0.01)
+        with pytest.raises(Exception):
+            m.setWarmStart(net, extra_iterations=0, relax_all=True)
+
+
+def test_clouds_loss_and_gradient_through_the_solve():
+    """The loss (mean squared density constraint after the relaxed first correction) against
+    the oracle's (oracle.clouds_ws_loss, BF16 network emulated), and dL/dy projected on the
+    output layer's parameters (the network's backward) against central differences of the
+    oracle's loss in double precision.  The state does not advance, and a second call gives
+    the same loss and gradient."""
+    sc = scenes.clouds_cumulus(n=32768, noise=True, seed=2)
+    c = oracle.derive_constants(abi.CLOUDS, sc["model_params"])
+    fp, cp, env, ground = sc["fluid_params"], sc["cloud_params"], sc["env"], sc["ground"]
+    with clouds_model(sc, iters=1) as m:
+        m.update(3)
+        st = gpu_state(m, abi.CLOUDS)
+        net = _omega_net(np.random.default_rng(7), _features(sc, st))
+        keep = {b: m.download(b) for b in (abi.BUF_POS, abi.BUF_VEL, abi.BUF_TEMP, abi.BUF_VAPOR, abi.BUF_CLOUD)}
+        loss, dy = warmstart.loss_grad_solve(m, net)
+        for b, v in keep.items():
+            assert np.array_equal(m.download(b), v), "the state must not advance (buffer %d)" % b
+        loss2, dy2 = warmstart.loss_grad_solve(m, net)
+    dy = dy.cpu().numpy()
+    assert loss2 == loss and np.array_equal(dy, dy2.cpu().numpy())
+    s = _copy(st)
+    l_emu, feats = oracle.clouds_ws_loss(c, fp, cp, env, ground, net, s, emulate=True)
+    assert abs(loss - l_emu) <= 2e-3 * l_emu, (loss, l_emu)
+    rows = np.zeros((dy.shape[0], 4), np.float32)
+    rows[:, 0] = dy[s["id"]]  # dL/dy by sorted row
+    grad = oracle.mlp_backward(net, feats, rows, emulate=False)
+    checks = []
+    for name, idx in (("b3", (0,)), ("w3", (0, 5)), ("w3", (0, 17)), ("w3", (0, 40))):
+        eps = 1e-3
+        vals = []
+        for sgn in (1, -1):
+            a = abi.mlp_to_arrays(net)
+            a[name][idx] += sgn * eps
+            lv, _ = oracle.clouds_ws_loss(c, fp, cp, env, ground, abi.mlp_from_arrays(a), _copy(st))
+            vals.append(lv)
+        checks.append((name, idx, (vals[0] - vals[1]) / (2 * eps), float(grad[name][idx])))
+    scale = max(abs(fd) for _, _, fd, _ in checks)
+    assert scale > 0
+    for name, idx, fd, an in checks:
+        assert abs(fd - an) <= 3e-2 * scale, (name, idx, fd, an, checks)
+
+
+def _solver_error(sc, iters, net=None, extra=0, steps=200):
+    with clouds_model(sc, iters=iters) as m:
+        m.enableSolverStats(True)
+        if net is not None:
+            m.setWarmStart(net, extra_iterations=extra)
+        m.update(steps)
+        return m.solverStats()["mean"]
+
+
+def test_network_trained_through_the_clouds_solve_beats_the_plain_iteration():
+    n = 32768
+    sc = scenes.clouds_cumulus(n=n, noise=True, seed=1)
+    with clouds_model(sc, iters=1) as m:
+        net, hist = warmstart.train_rollout(m, 300, extra_iterations=0, seed=1)
+    assert np.all(np.isfinite(hist))
+    assert np.mean(hist[-30:]) < np.mean(hist[:30]), (hist[:5], hist[-5:])
+    test = scenes.clouds_cumulus(n=n, noise=True, seed=3)
+    errs = {"plain1": _solver_error(test, 1), "plain2": _solver_error(test, 2),
+            "learned+0": _solver_error(test, 1, net, 0), "learned+1": _solver_error(test, 1, net, 1)}
+    print("clouds solver-output mean |rho/rho0 - 1| on a held-out column: %s"
+          % {k: round(v, 5) for k, v in errs.items()})
+    assert errs["learned+0"] < errs["plain1"], errs

@@ -96,3 +96,39 @@ def test_zero_output_layer_is_the_plain_solver():
     oracle.ws_step(c, fp, abi.mlp_from_arrays(z), 0, 0.0, 1, a, np.zeros(n, np.float32))
     oracle.fluids_step(c, fp, 1, b)
     assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+
+
+def _clouds_state(n=4000, steps=2):
+    sc = scenes.clouds_cumulus(n=n, noise=True, seed=5)
+    c = oracle.derive_constants(abi.CLOUDS, sc["model_params"])
+    st = oracle.new_state(n, c, abi.CLOUDS)
+    st["pos"][:] = sc["pos"]
+    st["vel"][:] = sc["vel"]
+    oracle.clouds_init(c, sc["cloud_params"], sc["env"], sc["ground"], st)
+    for _ in range(steps):
+        oracle.clouds_step(c, sc["fluid_params"], sc["cloud_params"], sc["env"], sc["ground"], 1, st)
+    return sc, c, st
+
+
+@pytest.mark.parametrize("extra", [0, 1])
+def test_clouds_zero_output_layer_is_the_plain_solver(extra):
+    """The clouds warm start with a zero output layer and `extra` plain iterations after it is
+    the plain clouds step with extra + 1 iterations, bit for bit; a network that does relax
+    lambda changes the step."""
+    sc, c, st = _clouds_state()
+    fp, cp, env, gr = sc["fluid_params"], sc["cloud_params"], sc["env"], sc["ground"]
+    a, b, r = _copy(st), _copy(st), _copy(st)
+    z = abi.mlp_to_arrays(_net())
+    z["w3"][:] = 0.0
+    z["b3"][:] = 0.0
+    feats, om = oracle.clouds_ws_step(c, fp, cp, env, gr, abi.mlp_from_arrays(z), extra, a)
+    oracle.clouds_step(c, fp, cp, env, gr, extra + 1, b)
+    for k in ("pos", "vel", "temp", "vapor", "cloud", "id"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.all(om == 1.0)
+    # the features: integer neighbour counts, the plain lambda, the y-wall proximity in [-2, 2]
+    assert np.all(feats[:, 0] == np.round(feats[:, 0])) and feats[:, 0].max() > 0
+    assert np.all(np.abs(feats[:, 8]) <= 2.0) and np.any(feats[:, 8] > 0)  # particles start at the floor
+    assert np.all(np.isfinite(feats))
+    _, om_r = oracle.clouds_ws_step(c, fp, cp, env, gr, _net(), extra, r)
+    assert om_r.std() > 0.01 and not np.array_equal(r["pos"], b["pos"])
