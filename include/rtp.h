@@ -400,7 +400,17 @@ int rtp_fill_grid_detector(void* handle);
  * or (relaxAllIterations) relaxed by the same omega.
  * Guard: the solver output's mean |rho_i/rho0 - 1| is measured in the vorticity sweep; a
  * step above `guardTolerance` reruns from the same predicted positions with the plain
- * iteration count (rtp_set_jacobi_iterations) before vorticity confinement and XSPH. */
+ * iteration count (rtp_set_jacobi_iterations) before vorticity confinement and XSPH.
+ *
+ * Clouds handles (the clouds Jacobi loop, Clouds.cpp:570-587) take the same network in the
+ * first cld_computeDensity / cld_computeConstraintFactor sweep, with neighbours over the
+ * periodic x and z images and the y walls (clouds.cl:305-436), and features 7 and 9 (the x
+ * and z wall proximities, always 0 under the periodic boundary) replaced by
+ *   7 b_i dt^2 / h      (the step's buoyancy, cld_computeBuoyancy, as a displacement)
+ *   9 (T_i - T_env(x_i)) / 10   (the smoothed temperature above the environment, K / 10)
+ * feature 8 being the y-wall proximity with the box walls +-W_y.  The relaxed first
+ * correction is cld_computeConstraintCorrection + the mixed boundary; then `extraIterations`
+ * plain iterations.  No guard and no relaxation of every iteration on clouds. */
 #define RTP_MLP_IN 12
 #define RTP_MLP_HIDDEN 64
 #define RTP_MLP_OUT 4
@@ -432,9 +442,11 @@ typedef struct rtp_solver_stats {
   double sumFirstError;      /* sum over steps of the warm-started output's mean (before reruns) */
 } rtp_solver_stats;
 
-/* Installs (or with cfg->enabled == 0 removes) the warm start on a fluids handle. */
+/* Installs (or with cfg->enabled == 0 removes) the warm start on a fluids or clouds handle
+ * (clouds: guardTolerance > 0 or relaxAllIterations give RTP_ERR_NOT_SUPPORTED). */
 int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_config* cfg);
-/* Also measure the plain solver's output error per step (warm-started steps always do). */
+/* Also measure the plain solver's output error per step (fluids: warm-started steps always
+ * do; clouds: only while enabled).  Fluids and clouds handles. */
 int rtp_enable_solver_stats(void* handle, int enable);
 int rtp_get_solver_stats(void* handle, rtp_solver_stats* out);
 int rtp_reset_solver_stats(void* handle);
@@ -471,6 +483,9 @@ int rtp_train_warm_start(const float* d_features, const float* d_targets, uint64
  *   x* = the step's predicted positions, clamped (fld_predictPosition, fld_applyBoundaryCondition),
  *   x' = clamp(x* + dp(omega(y) lambda)) with y = network(features at x*),
  *   L  = 1/n sum_i (rho_i(x') / rho0 - 1)^2, rho(x') over the 27 cells of the step's table.
+ * Clouds: x* = the predicted positions after the step's thermodynamics and temperature
+ * smoothing, x' = the mixed boundary of x* + dp(omega(y) lambda), rho over the periodic images;
+ * the thermodynamic state (temperature, vapour, cloud, buoyancy) is restored afterwards.
  * rtp_warm_start_loss_grad evaluates L and dL/dy for the handle's current state (it runs the next
  * step's predict, sort and cell table; the model's positions and velocities are not changed):
  * d_dy (device, optional) receives dL/dy_i at index = particle id (RTP_BUF_ID), n floats. */
@@ -484,7 +499,7 @@ int rtp_warm_start_loss_grad(void* handle, const rtp_mlp* net, float* d_dy, doub
  * init != 0 starts a new network: input normalisation from the first step's features,
  * Xavier-uniform hidden layers (cfg->seed), a zero output layer (omega = 1) and unit output
  * scales; init == 0 continues from *net.  loss_history (host, `steps` floats, may be NULL)
- * receives each step's L before its update.  Single fluids scenes only. */
+ * receives each step's L before its update.  Single fluids or clouds scenes (not batches). */
 int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint32_t steps, uint32_t extraIterations,
                                  int init, rtp_mlp* net, float* loss_history);
 /* Loss and gradient of `net` over n samples (forward and backward kernels of the trainer):
