@@ -8,8 +8,9 @@ Metric: particle-steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-* autotune (fluids workloads): the launch shape (list-sweep lanes; for a batch also the cell
-  factor) is picked by the library's autotuner before warm-up; candidates and times reported.
+* autotune (fluids workloads): the launch shape (list-sweep lanes; for one scene whether the
+  lambda sweep runs tiled by bricks of cells, for a batch the cell factor) is picked by the
+  library's autotuner before warm-up; candidates (lanes/factor/tiled) and times reported.
 * value: K device-timed steps (CUDA events around each graph replay on the model's
   stream), inputs resident in HBM, L2 flushed before every step by a 256 MiB write.
 * e2e: K steps through the public API with host buffers: one rtp_update_host call per step
@@ -72,6 +73,8 @@ WORKLOADS = {
                               metric="PBF particle-steps/s @16k (plain, 3 Jacobi iterations)"),
     # 16.7M particles (256^3 lattice, box 6.4 = 256 cells of h per axis): the grid/sort path
     # at a size where its HBM traffic, not launch latency, sets the time.
+    "pbf_dam_break_1m": dict(kind="fluids", lattice=(64, 128, 128), box=1.6, iters=3, max_steps=50,
+                             metric="PBF particle-steps/s @1M (plain, 3 Jacobi iterations)"),
     "pbf_dam_break_4m": dict(kind="fluids", lattice=(128, 256, 128), box=3.2, iters=3, max_steps=20,
                              metric="PBF particle-steps/s @4.2M (plain, 3 Jacobi iterations)"),
     "pbf_dam_break_16m": dict(kind="fluids", lattice=(256, 256, 256), box=6.4, iters=3, max_steps=10,
@@ -579,7 +582,7 @@ def batch_study(m, w, steps, warmup):
     plain against warm-started solver error on the batch."""
     from realtimeparticles_gb300 import model, warmstart
     sc = m._scene_set
-    lanes, factor = m.tuning()
+    lanes, factor, _ = m.tuning()
     n_total = sc["pos"].shape[0]
     ms_sum = 0.0
     for s, (n, box) in enumerate(sc["scenes"]):
@@ -594,19 +597,20 @@ def batch_study(m, w, steps, warmup):
             one.update(warmup)
             ms_sum += one.timeSteps(steps, flush_bytes=L2_FLUSH_BYTES) / steps
     separate = n_total / (ms_sum / 1000.0)
-    # Plain and warm-started solver error on the batch (network trained on the 131k dam break).
-    feats, targets = warmstart.generate_samples(seeds=range(1, 9), lattice=(32, 64, 64), steps=400,
-                                                record_every=25, stride=8, reference_iterations=8)
-    net, hist = warmstart.train(feats, targets, epochs=16, batch=8192, seed=0)
-    del feats, targets
+    # Plain and warm-started solver error on the batch: the network trained through the solve
+    # on the rollouts of two seeded 131k dam breaks (as the warm_start study trains it).
+    net = None
+    for seed in WS_TRAIN_SEEDS[:2]:
+        with fluids_model((32, 64, 64), seed, 2) as mt:
+            net, _ = warmstart.train_rollout(mt, WS_TRAIN_STEPS, extra_iterations=1, net=net, seed=0)
     errs = {}
-    for name, use in (("plain", False), ("learned_extra1", True)):
+    for name, extra in (("plain", None), ("learned_extra1", 1), ("learned_extra2", 2)):
         mb, _ = make_model(w)
         with mb:
             mb.setTuning(lanes, factor)
             mb.enableSolverStats(True)
-            if use:
-                mb.setWarmStart(net, extra_iterations=1, guard_tolerance=0.0)
+            if extra is not None:
+                mb.setWarmStart(net, extra_iterations=extra, guard_tolerance=0.0)
             mb.update(warmup)
             mb.resetSolverStats()
             ms = mb.timeSteps(steps, flush_bytes=L2_FLUSH_BYTES) / steps
@@ -639,8 +643,8 @@ def run_ours(args):
     tune = None
     if w["kind"] in ("batch", "fluids"):
         best, cands = m.autotune(steps=5)
-        tune = {"best": {"lanes": best[0], "cell_factor": best[1]},
-                "candidates_ms_per_step": {"%d/%.2f" % k: v for k, v in sorted(cands.items())}}
+        tune = {"best": {"lanes": best[0], "cell_factor": best[1], "tiled_sweeps": best[2]},
+                "candidates_ms_per_step": {"%d/%.2f/%d" % k: v for k, v in sorted(cands.items())}}
 
     # Warm-up (graph capture happens here).
     m.update(max(3, args.warmup))
@@ -670,6 +674,10 @@ def run_ours(args):
     alg = KERNEL_BYTES.get(dom_name, 0) * n
     achieved = alg / (dom_avg_ms / 1000.0) / 1e9
     share = {k: round(v[1] / sum(x[1] for x in kt.values()), 4) for k, v in kt.items()}
+    # Sum of the kernels' own durations per step (events around each kernel inside the same
+    # graph replays): the step time minus this is the launch and drain gaps between kernels,
+    # the most a single persistent launch over the step's stages could take back.
+    kernels_ms = sum(v[1] for v in kt.values()) / max(1, args.steps)
     grid_sort = sweep = None
     if w["kind"] == "fluids":  # (a batch has one grid per scene)
         tab = m.download(abi.BUF_CELL_TABLE)
@@ -734,6 +742,7 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": alg,
                          "mean_launch_ms": dom_avg_ms},
             "kernel_share": share,
+            "kernels_ms_per_step": kernels_ms,
             "clocks": clk,
         }
         if grid_sort:

@@ -540,13 +540,18 @@ int rtp_batch_scene_constants(void* handle, uint32_t scene, rtp_grid_constants* 
 int rtp_batch_scene_key_base(void* handle, uint32_t scene, uint32_t* base);
 
 /* Launch shape of a fluids handle: lanes per particle in the sweeps that walk recorded pair
- * lists (2, 4 or 8; default 4) and, for a batch, the cell size as a multiple of h (>= 1;
- * default 1; a single scene keeps the reference's grid).  rtp_autotune times every candidate
- * (lanes x {1, 1.25, 1.5, 2} cell factors for a batch) over `steps` steps, L2 flushed before
+ * lists (2, 4 or 8; default 4); for a batch, the cell size as a multiple of h (>= 1;
+ * default 1; a single scene keeps the reference's grid); and tiledSweeps (0 or 1): the
+ * lambda sweep of a single scene of more than 49,152 particles on a grid of at least 6 cells
+ * per axis runs tiled by bricks of 4 x 4 x 4 cells, each brick's particles and one-cell halo
+ * staged in shared memory (same pairs, same order, same results bit for bit; no effect on a
+ * batch).  rtp_autotune times every candidate (lanes x tiledSweeps {0, 1} for a single scene,
+ * lanes x {1, 1.25, 1.5, 2} cell factors for a batch) over `steps` steps, L2 flushed before
  * each, and keeps the fastest; the simulation advances meanwhile. */
 typedef struct rtp_tuning {
   uint32_t lanes;
   float cellFactor;
+  uint32_t tiledSweeps;
 } rtp_tuning;
 #define RTP_TUNE_MAX_CANDIDATES 32
 typedef struct rtp_tune_result {

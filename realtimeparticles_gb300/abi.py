@@ -181,7 +181,7 @@ class BatchScene(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("lanes", C.c_uint32), ("cellFactor", C.c_float)]
+    _fields_ = [("lanes", C.c_uint32), ("cellFactor", C.c_float), ("tiledSweeps", C.c_uint32)]
 
 
 TUNE_MAX_CANDIDATES = 32

@@ -75,33 +75,10 @@ __global__ void __launch_bounds__(kKeyThreads) k_fluid_predict(GridK g0, FluidK 
   th.store(hist0);
 }
 
-// fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor; records
-// the pairs within h for k_fluid_deltap.  One thread per particle: a filter pass over the
-// 27 cells writes the pairs within h to the device list (kept for k_fluid_deltap), then
-// the SPH terms are summed over that list.
-template <bool BATCH, bool MASK>
-__global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
-                                                                const uint2* __restrict__ table, uint32_t n,
-                                                                float* __restrict__ lambda,
-                                                                float* __restrict__ density, PairList pl,
-                                                                float* __restrict__ lamTot, int totMode,
-                                                                float4* __restrict__ packed,
-                                                                const float* __restrict__ omega) {
-  pdl_enter();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  scene_of<BATCH>(i, g, p);
-  const Sph k(g);
-  const float4 xi = ld4(pred + i);
-  uint32_t cnt = 0;
-  uint32_t* lst = pl.idx + i;
-  filter_fluid_neighbours_to<MASK>(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
-    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
-    ++cnt;
-  });
+// The sums of fld_computeDensity / fld_computeConstraintFactor over the pairs of particle i.
+struct LambdaSums {
   float rho = 0.0f, sgx = 0.0f, sgy = 0.0f, sgz = 0.0f, ssq = 0.0f;
-  auto ldp = [&](uint32_t j) { return ld4(pred + j); };
-  auto body = [&](uint32_t, float4 xj) {
+  __device__ __forceinline__ void add(const Sph& k, float4 xi, float4 xj) {
     const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
     const float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 < k.h2) {
@@ -114,23 +91,243 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
       sgz += gzz;
       ssq += gxx * gxx + gyy * gyy + gzz * gzz;
     }
-  };
+  }
+};
+
+// lambda_i from the sums (fld_computeConstraintFactor) and the sweep's outputs.
+__device__ __forceinline__ void lambda_finish(const FluidK& p, uint32_t i, float4 xi, LambdaSums sm,
+                                              float* __restrict__ lambda, float* __restrict__ density,
+                                              float* __restrict__ lamTot, int totMode, float4* __restrict__ packed,
+                                              const float* __restrict__ omega) {
+  const float C = sm.rho / p.rho0 - 1.0f;
+  float ssq = sm.ssq + (sm.sgx * sm.sgx + sm.sgy * sm.sgy + sm.sgz * sm.sgz);
+  ssq *= p.invRho0Sq;
+  float lam = -C / (ssq + p.relaxCFM);
+  if (omega) lam *= __ldg(omega + i);  // warm start relaxing every iteration
+  lambda[i] = lam;
+  density[i] = sm.rho;
+  if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
+  // Total lambda of the step (warm start): kTotWrite starts it, kTotAdd accumulates.
+  if (totMode == kTotWrite) lamTot[i] = lam;
+  else if (totMode == kTotAdd) lamTot[i] += lam;
+}
+
+// The lambda sweep of particle i at xi from global memory: a filter pass over the 27 cells
+// writes the pairs within h to the device list, then the sums run over that list (over the
+// 27 cells again when the list overflowed).
+template <bool MASK>
+__device__ __forceinline__ void fluid_lambda_global(const GridK& g, const FluidK& p, const float4* __restrict__ pred,
+                                                    const uint2* __restrict__ table, uint32_t i, float4 xi,
+                                                    const PairList& pl, float* __restrict__ lambda,
+                                                    float* __restrict__ density, float* __restrict__ lamTot,
+                                                    int totMode, float4* __restrict__ packed,
+                                                    const float* __restrict__ omega) {
+  const Sph k(g);
+  uint32_t cnt = 0;
+  uint32_t* lst = pl.idx + i;
+  filter_fluid_neighbours_to<MASK>(g, table, xi, k.h2, [&](uint32_t j) { return ld4(pred + j); }, [&](uint32_t j) {
+    if (cnt < pl.K) lst[(size_t)cnt * pl.stride] = j;
+    ++cnt;
+  });
+  LambdaSums sm;
+  auto ldp = [&](uint32_t j) { return ld4(pred + j); };
+  auto body = [&](uint32_t, float4 xj) { sm.add(k, xi, xj); };
   if (cnt <= pl.K)
     visit_list_x4(0, cnt, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ldp, body);
   else
     for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ldp(j)); });
   pl.count[i] = cnt <= pl.K ? cnt : kListOverflow;
-  const float C = rho / p.rho0 - 1.0f;
-  ssq += sgx * sgx + sgy * sgy + sgz * sgz;
-  ssq *= p.invRho0Sq;
-  float lam = -C / (ssq + p.relaxCFM);
-  if (omega) lam *= __ldg(omega + i);  // warm start relaxing every iteration
-  lambda[i] = lam;
-  density[i] = rho;
-  if (packed) packed[i] = f4(xi.x, xi.y, xi.z, lam);
-  // Total lambda of the step (warm start): kTotWrite starts it, kTotAdd accumulates.
-  if (totMode == kTotWrite) lamTot[i] = lam;
-  else if (totMode == kTotAdd) lamTot[i] += lam;
+  lambda_finish(p, i, xi, sm, lambda, density, lamTot, totMode, packed, omega);
+}
+
+// fld_applyBoundaryCondition + fld_computeDensity + fld_computeConstraintFactor; records
+// the pairs within h for k_fluid_deltap.  One thread per particle (fluid_lambda_global).
+template <bool BATCH, bool MASK>
+__global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda(GridK g, FluidK p, const float4* __restrict__ pred,
+                                                                const uint2* __restrict__ table, uint32_t n,
+                                                                float* __restrict__ lambda,
+                                                                float* __restrict__ density, PairList pl,
+                                                                float* __restrict__ lamTot, int totMode,
+                                                                float4* __restrict__ packed,
+                                                                const float* __restrict__ omega) {
+  pdl_enter();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  scene_of<BATCH>(i, g, p);
+  fluid_lambda_global<MASK>(g, p, pred, table, i, ld4(pred + i), pl, lambda, density, lamTot, totMode, packed, omega);
+}
+
+// ---- the lambda sweep tiled by bricks of cells (one scene, every grid axis >= 6 cells) ------
+// The grid is cut into bricks of kBrick^3 cells; one CTA per brick stages the sorted
+// positions of the brick and its one-cell halo (kHalo^3 cells, each cell's capped range, in
+// the key order: x, then y, then z fastest) in shared memory with coalesced loads, then runs
+// the filter pass of the particles stored in the brick's cells from there (the sums walk the
+// recorded list, whose positions the staging brought into L1).  The
+// three z cells of a halo row around a particle are consecutive in shared memory, so every
+// particle visits its 27 cells in the order of fluid_lambda_global and writes the same list
+// and the same sums bit for bit.  A particle whose current cell (positions move between
+// Jacobi iterations) is not inside its brick, and every particle of a brick whose halo holds
+// more than kBrickCap particles, takes fluid_lambda_global.  The extra last CTA takes the
+// particles stored in no cell's range: the first sorted one (left out of its cell as
+// fillStartCell does) and those with keys past the grid.
+constexpr int kBrick = 4;
+constexpr int kHalo = kBrick + 2;
+constexpr int kHaloCells = kHalo * kHalo * kHalo;
+constexpr int kOwnCells = kBrick * kBrick * kBrick;
+constexpr uint32_t kBrickThreads = 256;
+constexpr uint32_t kBrickCap = 2560;
+constexpr size_t kBrickSmem =
+    (size_t)kBrickCap * sizeof(float4) + (size_t)(kHaloCells + 1 + kHaloCells + kOwnCells + 1 + kOwnCells) * sizeof(uint32_t);
+
+__device__ __forceinline__ int wrap_halo(int v, int R) { return v < 0 ? v + R : (v >= R ? v - R : v); }
+
+// Exclusive scan of a (threads < 256) over the CTA: returns the prefix; *total gets the sum.
+__device__ __forceinline__ uint32_t brick_scan(uint32_t a, uint32_t* s_warp, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  uint32_t x = a;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) s_warp[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t v = lane < kBrickThreads / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= (uint32_t)o) v += y;
+    }
+    if (lane < kBrickThreads / 32) s_warp[lane] = v;
+  }
+  __syncthreads();
+  const uint32_t before = w ? s_warp[w - 1] : 0u;
+  *total = s_warp[kBrickThreads / 32 - 1];
+  __syncthreads();
+  return before + x - a;
+}
+
+// Largest c in [0, count) with beg[c] <= s (beg ascending, beg[0] <= s).
+__device__ __forceinline__ uint32_t brick_find(const uint32_t* beg, uint32_t count, uint32_t s) {
+  uint32_t lo = 0, hi = count;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (beg[mid] <= s) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <bool MASK>
+__global__ void __launch_bounds__(kBrickThreads, 4)
+    k_fluid_lambda_brick(GridK g, FluidK p, const float4* __restrict__ pred, const uint2* __restrict__ table,
+                         const uint32_t* __restrict__ keys, uint32_t n, int nbx, int nby, int nbz,
+                         float* __restrict__ lambda, float* __restrict__ density, PairList pl,
+                         float* __restrict__ lamTot, int totMode, float4* __restrict__ packed,
+                         const float* __restrict__ omega) {
+  extern __shared__ __align__(16) unsigned char brick_smem[];
+  float4* s_pos = reinterpret_cast<float4*>(brick_smem);
+  uint32_t* s_beg = reinterpret_cast<uint32_t*>(s_pos + kBrickCap);
+  uint32_t* s_glob = s_beg + (kHaloCells + 1);
+  uint32_t* s_own = s_glob + kHaloCells;
+  uint32_t* s_ownStart = s_own + (kOwnCells + 1);
+  __shared__ uint32_t s_warp[kBrickThreads / 32];
+  pdl_enter();
+  const uint32_t t = threadIdx.x;
+  const uint32_t nBricks = (uint32_t)(nbx * nby * nbz);
+  if (blockIdx.x == nBricks) {
+    if (t == 0 && n > 0 && __ldg(keys) < g.nc)
+      fluid_lambda_global<MASK>(g, p, pred, table, 0, ld4(pred), pl, lambda, density, lamTot, totMode, packed, omega);
+    for (int64_t i = (int64_t)n - 1 - t; i >= 0; i -= kBrickThreads) {
+      if (__ldg(keys + i) < g.nc) break;
+      fluid_lambda_global<MASK>(g, p, pred, table, (uint32_t)i, ld4(pred + i), pl, lambda, density, lamTot, totMode,
+                                packed, omega);
+    }
+    return;
+  }
+  const int bz = (int)(blockIdx.x % (uint32_t)nbz), by = (int)((blockIdx.x / (uint32_t)nbz) % (uint32_t)nby);
+  const int bx = (int)(blockIdx.x / (uint32_t)(nbz * nby));
+  const int x0 = bx * kBrick, y0 = by * kBrick, z0 = bz * kBrick;
+  // Halo cells (capped ranges, staged) and own cells (full ranges, processed).
+  uint32_t cnt = 0, own = 0;
+  if (t < (uint32_t)kHaloCells) {
+    const int hz = (int)t % kHalo, hy = ((int)t / kHalo) % kHalo, hx = (int)t / (kHalo * kHalo);
+    const int x = wrap_halo(x0 - 1 + hx, g.R[0]), y = wrap_halo(y0 - 1 + hy, g.R[1]), z = wrap_halo(z0 - 1 + hz, g.R[2]);
+    uint32_t b, e;
+    cell_range(table, g.base + ((uint32_t)x * g.R[1] + (uint32_t)y) * g.R[2] + (uint32_t)z, g.cap, b, e);
+    cnt = e - b;
+    s_glob[t] = b;
+  }
+  if (t < (uint32_t)kOwnCells) {
+    const int rz = (int)t % kBrick, ry = ((int)t / kBrick) % kBrick, rx = (int)t / (kBrick * kBrick);
+    const int x = x0 + rx, y = y0 + ry, z = z0 + rz;
+    uint32_t st = 0;
+    if (x < g.R[0] && y < g.R[1] && z < g.R[2]) {
+      const uint2 se = __ldg(table + g.base + ((uint32_t)x * g.R[1] + (uint32_t)y) * g.R[2] + (uint32_t)z);
+      own = se.y > se.x ? se.y - se.x : 0u;
+      st = se.x;
+    }
+    s_ownStart[t] = st;
+  }
+  uint32_t haloTotal, ownTotal;
+  const uint32_t hb = brick_scan(cnt, s_warp, &haloTotal);
+  const uint32_t ob = brick_scan(own, s_warp, &ownTotal);
+  if (t < (uint32_t)kHaloCells) s_beg[t] = hb;
+  if (t == 0) s_beg[kHaloCells] = haloTotal;
+  if (t < (uint32_t)kOwnCells) s_own[t] = ob;
+  if (t == 0) s_own[kOwnCells] = ownTotal;
+  if (ownTotal == 0) return;  // uniform over the CTA
+  const bool staged = haloTotal <= kBrickCap;
+  __syncthreads();
+  if (staged)
+    for (uint32_t s = t; s < haloTotal; s += kBrickThreads) {
+      const uint32_t c = brick_find(s_beg, kHaloCells, s);
+      const uint32_t j = s_glob[c] + (s - s_beg[c]);
+      const float4 v = ld4(pred + j);
+      s_pos[s] = f4(v.x, v.y, v.z, __uint_as_float(j));
+    }
+  __syncthreads();
+  const Sph k(g);
+  for (uint32_t o = t; o < ownTotal; o += kBrickThreads) {
+    const uint32_t c = brick_find(s_own, kOwnCells, o);
+    const uint32_t i = s_ownStart[c] + (o - s_own[c]);
+    const float4 xi = ld4(pred + i);
+    int cx, cy, cz;
+    cell3(g, xi, cx, cy, cz);
+    const int rx = cx - x0, ry = cy - y0, rz = cz - z0;
+    if (!staged || (uint32_t)rx >= (uint32_t)kBrick || (uint32_t)ry >= (uint32_t)kBrick ||
+        (uint32_t)rz >= (uint32_t)kBrick) {
+      fluid_lambda_global<MASK>(g, p, pred, table, i, xi, pl, lambda, density, lamTot, totMode, packed, omega);
+      continue;
+    }
+    uint32_t m = 0;
+    uint32_t* lst = pl.idx + i;
+    auto test = [&](uint32_t, float4 xj) {
+      if (within_radius(xi, xj, k.h2)) {
+        if (m < pl.K) lst[(size_t)m * pl.stride] = __float_as_uint(xj.w);
+        ++m;
+      }
+    };
+    auto lds = [&](uint32_t s) { return s_pos[s]; };
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a)
+#pragma unroll 1
+      for (int b = 0; b < 3; ++b) {
+        const int row = ((rx + a) * kHalo + (ry + b)) * kHalo + rz;
+        visit_range_x8(s_beg[row], s_beg[row + 3], lds, test);
+      }
+    // The sums over the list from global memory (the positions this CTA staged are in L1).
+    LambdaSums sm;
+    auto ldp = [&](uint32_t j) { return ld4(pred + j); };
+    auto body = [&](uint32_t, float4 xj) { sm.add(k, xi, xj); };
+    if (m <= pl.K)
+      visit_list_x4(0, m, 1, [&](uint32_t kk) { return lst[(size_t)kk * pl.stride]; }, ldp, body);
+    else
+      for_each_fluid_neighbour(g, table, xi, [&](uint32_t j) { body(j, ldp(j)); });
+    pl.count[i] = m <= pl.K ? m : kListOverflow;
+    lambda_finish(p, i, xi, sm, lambda, density, lamTot, totMode, packed, omega);
+  }
 }
 
 // k_fluid_lambda with a group of LW lanes per particle (particle counts too small to keep the
@@ -629,13 +826,30 @@ int fluid_iteration(const GridK& g, const FluidK& p, const float4* predIn, float
   return fluid_deltap(g, p, predIn, predOut, lambda, table, n, last, posS, velS, pl, nullptr, L, packed);
 }
 
+// The brick-tiled sweep runs for one scene of enough particles whose grid has at least 6
+// cells on every axis (so that the halo cells of a brick are distinct cells).
+static bool brick_sweep_applies(const GridK& g, const FluidK& p, uint32_t n) {
+  return p.tiles && !p.bt.scenes && p.sortedKeys && n > 49152u && g.R[0] >= kHalo && g.R[1] >= kHalo &&
+         g.R[2] >= kHalo;
+}
+
 int fluid_lambda_sweep(const GridK& g, const FluidK& p, const float4* predIn, const uint2* table, uint32_t n,
                        float* lambda, float* density, const PairList& pl, Launcher& L, float* lamTot, int totMode,
                        float4* packed, const float* omega) {
   L.begin("fld_lambda");
   const dim3 nb(blocks(n, kSweepThreads)), nt(kSweepThreads);
   const bool mask = n >= kMaskFilterParticles;
-  if (const int lw = sweep_group_lanes(n)) {
+  if (brick_sweep_applies(g, p, n)) {
+    const int nbx = (g.R[0] + kBrick - 1) / kBrick, nby = (g.R[1] + kBrick - 1) / kBrick,
+              nbz = (g.R[2] + kBrick - 1) / kBrick;
+    const dim3 bg((unsigned)(nbx * nby * nbz + 1)), bt(kBrickThreads);
+    if (mask)
+      launch_smem(L, k_fluid_lambda_brick<true>, bg, bt, kBrickSmem, g, p, predIn, table, p.sortedKeys, n, nbx, nby, nbz,
+                  lambda, density, pl, lamTot, totMode, packed, omega);
+    else
+      launch_smem(L, k_fluid_lambda_brick<false>, bg, bt, kBrickSmem, g, p, predIn, table, p.sortedKeys, n, nbx, nby,
+                  nbz, lambda, density, pl, lamTot, totMode, packed, omega);
+  } else if (const int lw = sweep_group_lanes(n)) {
     dispatch_group(lw, [&](auto LW) {
       const dim3 gb(blocks(n, 128 / LW)), gt(128);
       if (p.bt.scenes)

@@ -21,6 +21,8 @@ struct FluidK {
   float xsph;
   BatchK bt;        // batched scenes (bt.scenes == nullptr: one scene, the fields above)
   int lanes = 4;    // lanes per particle of the list sweeps: 2, 4 or 8
+  int tiles = 0;    // 1: the lambda sweep tiled by bricks of cells where the grid allows
+  const uint32_t* sortedKeys = nullptr;  // the step's sorted cell keys (the brick sweep's leftovers)
 };
 
 FluidK make_fluidk(const rtp_grid_constants& c, const rtp_fluid_params& p);

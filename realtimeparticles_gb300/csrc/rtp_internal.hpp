@@ -50,6 +50,27 @@ inline void launch(const Launcher& L, void (*k)(P...), dim3 grid, dim3 block, A&
   (void)cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(a)...);
 }
 
+// Raises kernel k's dynamic shared memory limit to `bytes` on the current device (once per
+// kernel and device).
+void ensure_dynamic_smem(const void* k, size_t bytes);
+
+// launch() with `smem` bytes of dynamic shared memory.
+template <class... P, class... A>
+inline void launch_smem(const Launcher& L, void (*k)(P...), dim3 grid, dim3 block, size_t smem, A&&... a) {
+  ensure_dynamic_smem(reinterpret_cast<const void*>(k), smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = L.pdl ? 1u : 0u;
+  (void)cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(a)...);
+}
+
 // ---- Radix sort ---------------------------------------------------------------------
 struct SortPlan {
   uint32_t n = 0;

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -39,6 +40,17 @@ int cuda_fail(cudaError_t e, const char* what) {
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return RTP_ERR_NO_DEVICE;
   if (e == cudaErrorMemoryAllocation) return RTP_ERR_OUT_OF_MEMORY;
   return RTP_ERR_CUDA;
+}
+
+void ensure_dynamic_smem(const void* k, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = done[{k, dev}];
+  if (have >= bytes) return;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) have = bytes;
 }
 
 constexpr float PI_F = 3.1415927f;  // utils/Math.hpp:69
@@ -224,6 +236,7 @@ struct Handle {
 
   // Tuning (fluids): lanes per particle of the list sweeps; batch cell size = cellFactor * h.
   uint32_t lanes = 4;
+  uint32_t tiles = 0;  // brick-tiled lambda sweep (rtp_tuning.tiledSweeps)
   float cellFactor = 1.0f;
 
   // Batched scenes (fluids): scene s owns slots [sceneOff[s], sceneOff[s] + desc[s].nbParticles).
@@ -262,6 +275,8 @@ static bool target_on(const Handle* h) { return h->model == RTP_MODEL_BOIDS && h
 static FluidK fluidk_of(const Handle* h) {
   FluidK k = make_fluidk(h->gc, h->fp);
   k.lanes = (int)h->lanes;
+  k.tiles = (int)h->tiles;
+  k.sortedKeys = h->cellId;
   if (h->isBatch) {
     k.bt.scenes = h->dScenes;
     k.bt.sceneOf = h->dSceneOf;
@@ -2284,6 +2299,7 @@ int rtp_set_tuning(void* handle, const rtp_tuning* t) {
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: a single scene keeps the reference's grid (cellFactor 1)");
   if (!(t->cellFactor >= 1.0f && t->cellFactor <= 4.0f))
     return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: cellFactor in [1, 4]");
+  if (t->tiledSweeps > 1) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_tuning: tiledSweeps 0 or 1");
   RTP_CUDA(cudaStreamSynchronize(h->stream));
   if (h->isBatch && t->cellFactor != h->cellFactor) {
     const float old = h->cellFactor;
@@ -2298,6 +2314,7 @@ int rtp_set_tuning(void* handle, const rtp_tuning* t) {
     h->hasStep = false;
   }
   h->lanes = t->lanes;
+  h->tiles = t->tiledSweeps;
   invalidate(h);
   return RTP_OK;
   RTP_GUARD_END
@@ -2307,6 +2324,7 @@ int rtp_get_tuning(void* handle, rtp_tuning* t) {
   if (!handle || !t) return fail(RTP_ERR_INVALID_ARGUMENT, "null argument");
   t->lanes = H(handle)->lanes;
   t->cellFactor = H(handle)->cellFactor;
+  t->tiledSweeps = H(handle)->tiles;
   return RTP_OK;
 }
 
@@ -2320,26 +2338,28 @@ int rtp_autotune(void* handle, uint32_t steps, rtp_tune_result* out) {
   const uint32_t lanes[3] = {2, 4, 8};
   const float factors[4] = {1.0f, 1.25f, 1.5f, 2.0f};
   const int nf = h->isBatch ? 4 : 1;
+  const uint32_t nt = h->isBatch ? 1u : 2u;  // tiled sweeps: single scenes only
   double best = 1e300;
-  rtp_tuning bestT{4, 1.0f};
+  rtp_tuning bestT{4, 1.0f, 0u};
   for (int f = 0; f < nf; ++f)
-    for (int l = 0; l < 3; ++l) {
-      rtp_tuning t{lanes[l], factors[f]};
-      if (rtp_set_tuning(handle, &t) != RTP_OK) continue;
-      RTP_TRY(run_steps(h, 2));
-      double ms = 0.0;
-      RTP_TRY(rtp_time_steps(handle, steps, 256ull << 20, &ms));
-      ms /= steps;
-      if (out->tried < RTP_TUNE_MAX_CANDIDATES) {
-        out->candidates[out->tried] = t;
-        out->msPerStep[out->tried] = ms;
-        out->tried += 1;
+    for (uint32_t tl = 0; tl < nt; ++tl)
+      for (int l = 0; l < 3; ++l) {
+        rtp_tuning t{lanes[l], factors[f], tl};
+        if (rtp_set_tuning(handle, &t) != RTP_OK) continue;
+        RTP_TRY(run_steps(h, 2));
+        double ms = 0.0;
+        RTP_TRY(rtp_time_steps(handle, steps, 256ull << 20, &ms));
+        ms /= steps;
+        if (out->tried < RTP_TUNE_MAX_CANDIDATES) {
+          out->candidates[out->tried] = t;
+          out->msPerStep[out->tried] = ms;
+          out->tried += 1;
+        }
+        if (ms < best) {
+          best = ms;
+          bestT = t;
+        }
       }
-      if (ms < best) {
-        best = ms;
-        bestT = t;
-      }
-    }
   RTP_TRY(rtp_set_tuning(handle, &bestT));
   out->best = bestT;
   out->bestMsPerStep = best;

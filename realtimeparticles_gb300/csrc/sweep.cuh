@@ -26,6 +26,14 @@ constexpr uint32_t kPairListK = 64;        // entries per particle in the device
 constexpr uint32_t kSweepThreads = 64;     // block size of the two-phase sweeps (one wave at 131k)
 constexpr uint32_t kQuad = 4;              // default lanes per particle in the list sweeps
 
+// The filter passes' pair test |xi - xj|^2 < h2 with the rounding spelled out (two fused
+// multiply-adds), so that every filter pass (one lane, lane group, brick-tiled) accepts the
+// same pairs whatever code the compiler generates around it.
+__device__ __forceinline__ bool within_radius(float4 xi, float4 xj, float h2) {
+  const float vx = __fsub_rn(xi.x, xj.x), vy = __fsub_rn(xi.y, xj.y), vz = __fsub_rn(xi.z, xj.z);
+  return __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx))) < h2;
+}
+
 // Visits [b0,e0) [b1,e1) [b2,e2) in that order, joining ranges that touch so that the
 // usual case (three consecutive non-empty cells of one z column) is a single loop.
 template <class F>
@@ -207,10 +215,7 @@ __device__ __forceinline__ void for_each_fluid_neighbour(const GridK& g, const u
 template <bool MASK = false, class LD, class ADD>
 __device__ __forceinline__ void filter_fluid_neighbours_to(const GridK& g, const uint2* __restrict__ table, float4 xi,
                                                            float h2, LD&& ld, ADD&& add) {
-  auto hit = [&](float4 xj) {
-    const float vx = xi.x - xj.x, vy = xi.y - xj.y, vz = xi.z - xj.z;
-    return vx * vx + vy * vy + vz * vz < h2;
-  };
+  auto hit = [&](float4 xj) { return within_radius(xi, xj, h2); };
   auto test = [&](uint32_t j, float4 xj) {
     if (hit(xj)) add(j);
   };
@@ -275,10 +280,7 @@ __device__ __forceinline__ uint32_t filter_fluid_group(const GridK& g, const uin
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         bool hit = false;
-        if (c0 + u * LW + q < tot) {
-          const float vx = xi.x - x[u].x, vy = xi.y - x[u].y, vz = xi.z - x[u].z;
-          hit = vx * vx + vy * vy + vz * vz < h2;
-        }
+        if (c0 + u * LW + q < tot) hit = within_radius(xi, x[u], h2);
         const uint32_t m = (__ballot_sync(0xffffffffu, hit) >> first) & gbits;
         if (hit) {
           const uint32_t at = cnt + __popc(m & below);
