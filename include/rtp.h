@@ -25,7 +25,8 @@
 extern "C" {
 #endif
 
-#define RTP_ABI_VERSION 1
+/* 2: rtp_tuning gained tiledSweeps (12 bytes; version 1 had 8). */
+#define RTP_ABI_VERSION 2
 
 /* Status codes.  The reference reports errors as `bool` + log lines and throws
  * std::runtime_error on bad JSON paths (physics/ocl/Fluids.cpp:245-250); across a C ABI

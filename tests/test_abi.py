@@ -54,7 +54,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
 
 
 def test_abi_version(rtp_lib):
-    assert rtp_lib.rtp_abi_version() == 1
+    assert rtp_lib.rtp_abi_version() == 2
 
 
 @pytest.mark.parametrize("mtype,box,res", [(abi.FLUIDS, 1.0, 40), (abi.BOIDS, 2.0, 40), (abi.CLOUDS, (1.0, 2.0, 1.0),
