@@ -20,7 +20,8 @@ Metric: particle-steps/s.
   (captured event nodes inside the same graph replays), against MEASURED_PEAKS.json.
 * sweep (fluids, when the dominant kernel is the density/lambda sweep): candidates tested and
   pairs within h evaluated per second by that kernel (it is bound by dependent loads, so its
-  HBM fraction says little).
+  HBM fraction says little), with its L1 data-pipe fraction of peak from a committed ncu capture
+  and the candidate-test rate that fraction extrapolates to at the L1 ceiling.
 * cpu_baseline: the reference's own kernels (physics/ocl/kernels/*.cl compiled for the
   CPU by oracle/ref/build_ref.py, OpenMP over the host cores) on a bounded sample of the
   same workload; the oracle's restatement when those are not built.
@@ -152,6 +153,12 @@ def clouds_model(n, seed, iters):
 KERNEL_TRAFFIC = {
     ("pbf_dam_break_131k", "fld_lambda"): (6600021, "profiles/k_fluid_lambda_131k_traffic.md"),
     ("pbf_dam_break_16k", "fld_lambda"): (523520, "profiles/k_fluid_lambda_group_16k_traffic.md"),
+}
+
+# The dominant sweep's L1 data-pipe (LSU wavefront) fraction of peak from one ncu capture: the
+# ceiling the sweep's candidate-test rate is judged against (it is bound by L1 and issue, not HBM).
+SWEEP_L1 = {
+    ("pbf_dam_break_131k", "fld_lambda"): (0.5654, "profiles/k_fluid_lambda_131k_l1.md"),
 }
 
 KERNEL_BYTES = {
@@ -690,6 +697,10 @@ def run_ours(args):
             sweep = {"kernel": dom_name, "candidates_per_particle": cand, "neighbours_per_particle": nbr,
                      "candidate_tests_per_s": n * cand / (dom_avg_ms / 1000.0),
                      "pair_evaluations_per_s": n * nbr / (dom_avg_ms / 1000.0)}
+            l1 = SWEEP_L1.get((args.workload, dom_name))
+            if l1:
+                sweep.update(l1_wavefront_frac=l1[0], l1_source=l1[1],
+                             candidate_tests_per_s_at_l1_ceiling=sweep["candidate_tests_per_s"] / l1[0])
 
     # End to end through the public API with pinned host buffers.
     try:
