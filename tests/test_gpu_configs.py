@@ -7,7 +7,7 @@
   the oracle run on that scene alone (Fluids::update, Fluids.cpp:400-457, once per scene).
 * Long runs judged on statistics, since independent trajectories of a chaotic system diverge
   after a few hundred steps: boids, 131,072 particles over 1,000 steps (Boids::update,
-  Boids.cpp:323-384), and clouds over 4,000 steps.  The clouds run uses 8,192 particles (the
+  Boids.cpp:323-384), the 131,072-particle dam break over 500 steps, and clouds over 4,000 steps.  The clouds run uses 8,192 particles (the
   same box, grid and per-particle density law as the 131k workload): 4,000 oracle steps at
   131,072 particles would take over an hour of CPU time.
 
@@ -118,6 +118,40 @@ def test_boids_131k_long_run_statistics():
     assert sg["mean_nbr"] == pytest.approx(so["mean_nbr"], rel=0.01)
     tv = 0.5 * np.abs(sg["hist"] - so["hist"]).sum()
     assert tv < 0.05, tv
+
+
+def test_pbf_131k_long_run_statistics():
+    """The benchmark's 131k dam break (32 x 64 x 64, I = 3) over 500 steps on each side: solver
+    mean density error, kinetic energy, mean neighbour count and the neighbour histogram
+    (Fluids::update, Fluids.cpp:400-457).  The oracle against itself from positions perturbed
+    by 1e-6 and 3e-6 spreads by up to 1.9 % in the density error, 7 % in kinetic energy (the
+    splash), 0.05 % in neighbours and 0.009 in histogram total variation; the bounds are about
+    twice that."""
+    sc = scenes.dam_break(lattice=(32, 64, 64))
+    fp = sc["fluid_params"]
+    c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    steps = 500
+    ost = oracle.new_state(sc["pos"].shape[0], c)
+    ost["pos"][:] = sc["pos"]
+    ost["vel"][:] = sc["vel"]
+    for _ in range(steps):
+        oracle.fluids_step(c, fp, 3, ost)
+    om = oracle.fluid_metrics(c, fp, ost["predPos"], ost["vel"], ost["table"])
+    from helpers import fluids_model
+    with fluids_model(sc, 3) as m:
+        m.update(steps)
+        gm = m.metrics()
+    print("pbf 131k after %d steps: gpu err %.5f ke %.1f nbr %.3f, oracle err %.5f ke %.1f nbr %.3f"
+          % (steps, gm.meanDensityError, gm.kineticEnergy, gm.meanNeighbours, om.meanDensityError,
+             om.kineticEnergy, om.meanNeighbours))
+    assert gm.pairListOverflows == 0
+    assert gm.meanDensityError == pytest.approx(om.meanDensityError, rel=0.05)
+    assert gm.kineticEnergy == pytest.approx(om.kineticEnergy, rel=0.15)
+    assert gm.meanNeighbours == pytest.approx(om.meanNeighbours, rel=0.005)
+    hg = np.array(gm.neighbourHist, np.float64)
+    ho = np.array(om.neighbourHist, np.float64)
+    tv = 0.5 * np.abs(hg / hg.sum() - ho / ho.sum()).sum()
+    assert tv < 0.03, tv
 
 
 def clouds_statistics(st, c, rho0):
