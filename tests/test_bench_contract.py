@@ -26,6 +26,7 @@ def test_reference_arm_prints_one_contract_line():
     assert d["value"] > 0 and d["steps"] >= 1 and d["warmup"] == 3
     cfg = d["config"]
     assert cfg["workload"] == bench.WORKLOAD and cfg["particles"] == 131072 and cfg["jacobi_iterations"] == 3
+    assert cfg["l2"] == bench.L2_NOTE  # the same "l2" entry as the GPU arm's config
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"]
