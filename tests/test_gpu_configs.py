@@ -121,37 +121,52 @@ def test_boids_131k_long_run_statistics():
 
 
 def test_pbf_131k_long_run_statistics():
-    """The benchmark's 131k dam break (32 x 64 x 64, I = 3) over 500 steps on each side: solver
-    mean density error, kinetic energy, mean neighbour count and the neighbour histogram
-    (Fluids::update, Fluids.cpp:400-457).  The oracle against itself from positions perturbed
-    by 1e-6 and 3e-6 spreads by up to 1.9 % in the density error, 7 % in kinetic energy (the
-    splash), 0.05 % in neighbours and 0.009 in histogram total variation; the bounds are about
-    twice that."""
+    """The benchmark's 131k dam break (32 x 64 x 64, I = 3) over 500 steps: solver mean density
+    error, kinetic energy, mean neighbour count and the neighbour histogram (Fluids::update,
+    Fluids.cpp:400-457).  After 500 steps the splash makes single trajectories differ widely
+    (twelve GPU runs from positions perturbed by up to 1.1e-5 spread over 17.6k-22.8k in kinetic
+    energy, 32.09-32.18 mean neighbours; three oracle runs over 18.2k-19.5k), so the oracle's
+    run is compared with an ensemble of six GPU runs (the unperturbed one and five perturbed by
+    k x 1e-6): the oracle must lie within the ensemble's range widened by half its width, and
+    the ensemble mean must agree with it (kinetic energy within 15 %, density error 4 %,
+    neighbours 0.3 %, histogram total variation 0.02)."""
+    from helpers import fluids_model
     sc = scenes.dam_break(lattice=(32, 64, 64))
     fp = sc["fluid_params"]
     c = oracle.derive_constants(abi.FLUIDS, sc["model_params"])
+    n = sc["pos"].shape[0]
     steps = 500
-    ost = oracle.new_state(sc["pos"].shape[0], c)
+    ost = oracle.new_state(n, c)
     ost["pos"][:] = sc["pos"]
     ost["vel"][:] = sc["vel"]
     for _ in range(steps):
         oracle.fluids_step(c, fp, 3, ost)
     om = oracle.fluid_metrics(c, fp, ost["predPos"], ost["vel"], ost["table"])
-    from helpers import fluids_model
-    with fluids_model(sc, 3) as m:
-        m.update(steps)
-        gm = m.metrics()
-    print("pbf 131k after %d steps: gpu err %.5f ke %.1f nbr %.3f, oracle err %.5f ke %.1f nbr %.3f"
-          % (steps, gm.meanDensityError, gm.kineticEnergy, gm.meanNeighbours, om.meanDensityError,
-             om.kineticEnergy, om.meanNeighbours))
-    assert gm.pairListOverflows == 0
-    assert gm.meanDensityError == pytest.approx(om.meanDensityError, rel=0.05)
-    assert gm.kineticEnergy == pytest.approx(om.kineticEnergy, rel=0.15)
-    assert gm.meanNeighbours == pytest.approx(om.meanNeighbours, rel=0.005)
-    hg = np.array(gm.neighbourHist, np.float64)
     ho = np.array(om.neighbourHist, np.float64)
-    tv = 0.5 * np.abs(hg / hg.sum() - ho / ho.sum()).sum()
-    assert tv < 0.03, tv
+    ho /= ho.sum()
+    runs = []
+    for k in range(6):
+        pos = sc["pos"].copy()
+        if k:
+            rng = np.random.default_rng(100 + k)
+            pos[:, :3] += (rng.uniform(-1, 1, (n, 3)) * (1e-6 * k)).astype(np.float32)
+        with fluids_model(dict(sc, pos=pos), 3) as m:
+            m.update(steps)
+            g = m.metrics()
+        assert g.pairListOverflows == 0 and np.isfinite(g.kineticEnergy)
+        hg = np.array(g.neighbourHist, np.float64)
+        runs.append((g.meanDensityError, g.kineticEnergy, g.meanNeighbours, hg / hg.sum()))
+    print("pbf 131k after %d steps: gpu runs %s; oracle err %.5f ke %.1f nbr %.3f"
+          % (steps, [tuple(round(float(x), 5) for x in r[:3]) for r in runs], om.meanDensityError,
+             om.kineticEnergy, om.meanNeighbours))
+    for q, ref, rel in ((0, om.meanDensityError, 0.04), (1, om.kineticEnergy, 0.15), (2, om.meanNeighbours, 0.003)):
+        v = np.array([r[q] for r in runs])
+        lo, hi = v.min(), v.max()
+        pad = 0.5 * (hi - lo)
+        assert lo - pad <= ref <= hi + pad, (q, ref, v)
+        assert v.mean() == pytest.approx(ref, rel=rel), (q, ref, v)
+    tv = 0.5 * np.abs(np.mean([r[3] for r in runs], axis=0) - ho).sum()
+    assert tv < 0.02, tv
 
 
 def clouds_statistics(st, c, rho0):
