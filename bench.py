@@ -195,7 +195,9 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms while running.  start() returns
+    once the first sample has arrived (nvidia-smi takes a while to start), and only the samples
+    after that point count, so they cover the timed region rather than the idle start-up."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -206,16 +208,22 @@ class ClockSampler:
         self.proc = None
         self.lines = []
         self.t = None
+        self.mark = 0
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.005)
+        self.mark = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -233,7 +241,8 @@ class ClockSampler:
             self.t.join(timeout=2)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lines = self.lines[self.mark:] or self.lines[-1:]
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -648,7 +657,7 @@ def run_ours(args):
     m, n = make_model(w, rank)
     n_all = sum_over_ranks(n, ws)  # a batch's ranks hold different scene sets
     tune = None
-    if w["kind"] in ("batch", "fluids"):
+    if w["kind"] in ("batch", "fluids") and not args.no_autotune:
         best, cands = m.autotune(steps=5)
         tune = {"best": {"lanes": best[0], "cell_factor": best[1], "tiled_sweeps": best[2]},
                 "candidates_ms_per_step": {"%d/%.2f/%d" % k: v for k, v in sorted(cands.items())}}
@@ -790,6 +799,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true", help="skip the learned warm-start study")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shape (for profiler runs, whose timings would mislead the autotuner)")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.warmup < 3:
