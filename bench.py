@@ -156,7 +156,7 @@ KERNEL_TRAFFIC = {
 }
 
 # The dominant sweep's L1 data-pipe (LSU wavefront) fraction of peak from one ncu capture: the
-# ceiling the sweep's candidate-test rate is judged against (it is bound by L1 and issue, not HBM).
+# ceiling the sweep's candidate-test rate is measured against (it is bound by L1 and issue, not HBM).
 SWEEP_L1 = {
     ("pbf_dam_break_131k", "fld_lambda"): (0.5654, "profiles/k_fluid_lambda_131k_l1.md"),
 }

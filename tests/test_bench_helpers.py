@@ -1,0 +1,50 @@
+"""The equal-error comparison of bench.py's warm-start studies (CPU only): the Pareto front of the
+plain solver's (error, throughput) points, the log-log interpolation of the plain throughput at a
+given error, and the fastest-configuration pick under an error bound."""
+import math
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def test_pareto_front_drops_dominated_points():
+    # (error, particle-steps/s): I = 4 is dominated by I = 3 (worse error and slower), and the
+    # last point (error growing again at many iterations) by every point before it that is faster
+    curve = [(0.28, 380.0), (0.045, 515.0), (0.033, 402.0), (0.0329, 343.0), (0.034, 300.0), (0.009, 78.0),
+             (0.018, 65.0)]
+    front = bench._pareto(curve)
+    assert front == [(0.045, 515.0), (0.033, 402.0), (0.0329, 343.0), (0.009, 78.0)]
+    assert all(e1 < e0 for (e0, _), (e1, _) in zip(front, front[1:]))  # error decreasing
+
+
+def test_plain_throughput_interpolated_log_log_on_the_front():
+    curve = [(0.04, 400.0), (0.01, 100.0), (0.02, 50.0)]  # the last point is off the front
+    # halfway in log error between 0.04 and 0.01 -> halfway in log throughput
+    v = bench._plain_at(curve, 0.02)
+    assert v == pytest.approx(200.0, rel=1e-12)
+    assert bench._plain_at(curve, 0.04) == pytest.approx(400.0)
+    assert bench._plain_at(curve, 0.01) == pytest.approx(100.0)
+    assert bench._plain_at(curve, 0.05) is None and bench._plain_at(curve, 0.005) is None
+    # monotone between the endpoints
+    xs = [0.039, 0.03, 0.02, 0.011]
+    ys = [bench._plain_at(curve, x) for x in xs]
+    assert all(a > b for a, b in zip(ys, ys[1:]))
+    assert math.log(ys[1]) == pytest.approx(math.log(400.0) + (math.log(0.03) - math.log(0.04))
+                                            / (math.log(0.01) - math.log(0.04)) * (math.log(100.0) - math.log(400.0)))
+
+
+def test_threshold_pick_takes_the_fastest_under_the_bound():
+    plain = [{"iterations": i, "particle_steps_per_s": v, "mean_density_error": e}
+             for i, v, e in ((3, 400.0, 0.033), (16, 113.0, 0.0124), (24, 78.0, 0.009), (32, 65.0, 0.0183))]
+    learned = [{"extra_iterations": k, "particle_steps_per_s": v, "mean_density_error": e}
+               for k, v, e in ((2, 380.0, 0.028), (7, 199.0, 0.0102), (9, 166.0, 0.0084), (11, 142.0, 0.0073))]
+    r = bench._at_threshold(plain, learned, 0.01)
+    assert r["plain"]["iterations"] == 24 and r["learned"]["extra_iterations"] == 9
+    assert r["speedup"] == pytest.approx(166.0 / 78.0)
+    none = bench._at_threshold(plain, learned, 0.005)
+    assert none["speedup"] is None and none["plain"] is None

@@ -5,7 +5,7 @@
 * The exact 48-scene batch the batched benchmark steps (`batched_dam_breaks(count=48, seed=0)`,
   1,134,509 particles, 4,127-65,031 per scene, aspect 0.5-2): one step, every scene against
   the oracle run on that scene alone (Fluids::update, Fluids.cpp:400-457, once per scene).
-* Long runs judged on statistics, since independent trajectories of a chaotic system diverge
+* Long runs compared on statistics, since independent trajectories of a chaotic system diverge
   after a few hundred steps: boids, 131,072 particles over 1,000 steps (Boids::update,
   Boids.cpp:323-384), the 131,072-particle dam break over 500 steps, and clouds over 4,000 steps.  The clouds run uses 8,192 particles (the
   same box, grid and per-particle density law as the 131k workload): 4,000 oracle steps at
