@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(kSweepThreads, BATCH ? 12 : 16) k_fluid_lambda
 // recorded list, whose positions the staging brought into L1).  The
 // three z cells of a halo row around a particle are consecutive in shared memory, so every
 // particle visits its 27 cells in the order of fluid_lambda_global and writes the same list
-// and the same sums bit for bit.  A particle whose current cell (positions move between
+// (its sums can differ from the one-lane sweep's in the last bit where the compiler fuses the
+// two kernels' multiply-adds differently).  A particle whose current cell (positions move between
 // Jacobi iterations) is not inside its brick, and every particle of a brick whose halo holds
 // more than kBrickCap particles, takes fluid_lambda_global.  The extra last CTA takes the
 // particles stored in no cell's range: the first sorted one (left out of its cell as
