@@ -164,8 +164,14 @@ def test_network_trained_through_the_clouds_solve_beats_the_plain_iteration():
     with clouds_model(sc, iters=1) as m:
         net, hist = warmstart.train_rollout(m, 300, extra_iterations=0, seed=1)
     assert np.all(np.isfinite(hist))
-    assert np.mean(hist[-30:]) < np.mean(hist[:30]), (hist[:5], hist[-5:])
     test = scenes.clouds_cumulus(n=n, noise=True, seed=3)
+    # At the same held-out states the trained network's loss is below the untrained one's.
+    with clouds_model(test, iters=1) as m:
+        for _ in range(3):
+            m.update(40)
+            l_trained, _ = warmstart.loss_grad_solve(m, net)
+            l_plain, _ = warmstart.loss_grad_solve(m, _zero_output(net))
+            assert l_trained < l_plain, (l_trained, l_plain)
     errs = {"plain1": _solver_error(test, 1), "plain2": _solver_error(test, 2),
             "learned+0": _solver_error(test, 1, net, 0), "learned+1": _solver_error(test, 1, net, 1)}
     print("clouds solver-output mean |rho/rho0 - 1| on a held-out column: %s"

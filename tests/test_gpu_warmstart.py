@@ -247,15 +247,23 @@ def test_network_trained_through_the_solve_beats_the_plain_first_iteration():
     """Train on the rollout of one seeded dam break (16,384 particles) under the warm start with
     no extra iteration, evaluate on a held-out seed: the solver-output mean density error of the
     warm start with no extra iteration must be below the plain solver's with one iteration (the
-    solve the warm start replaces), and the training loss must fall.  The comparison with more
-    iterations is printed."""
+    solve the warm start replaces), and on held-out states the trained network's training loss
+    must be below the untrained one's.  The comparison with more iterations is printed."""
     lattice = (16, 32, 32)
     sc = scenes.dam_break(lattice=lattice, seed=1)
     with fluids_model(sc, 2) as m:
         net, hist = warmstart.train_rollout(m, 300, extra_iterations=0, seed=1)
     assert np.all(np.isfinite(hist))
-    assert np.mean(hist[-30:]) < np.mean(hist[:30]), (hist[:5], hist[-5:])
     test = scenes.dam_break(lattice=lattice, seed=3)
+    # The training loss falls: at the same held-out states, the trained network's loss is below
+    # the untrained one's (a zero output layer: the plain first iteration).  (The rollout's own
+    # loss history mixes learning with the flow's development, so it is not compared.)
+    with fluids_model(test, 2) as m:
+        for _ in range(3):
+            m.update(40)
+            l_trained, _ = warmstart.loss_grad_solve(m, net)
+            l_plain, _ = warmstart.loss_grad_solve(m, _zero_output(net))
+            assert l_trained < l_plain, (l_trained, l_plain)
     errs = {"plain1": _solver_error(test, 1), "plain2": _solver_error(test, 2), "plain3": _solver_error(test, 3),
             "learned+0": _solver_error(test, 3, net, 0), "learned+1": _solver_error(test, 3, net, 1)}
     print("solver-output mean |rho/rho0 - 1| on a held-out scene: %s" % {k: round(v, 5) for k, v in errs.items()})
