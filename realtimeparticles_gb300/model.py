@@ -496,33 +496,6 @@ class Clouds(Model):
     def setJacobiIterations(self, it):
         call("rtp_set_jacobi_iterations", self._h, int(it))
 
-    # launch shape (new; rtp.h rtp_set_tuning) --------------------------------------------
-    def setTuning(self, lanes=4, cell_factor=1.0, tiled=None):
-        """Launch shape (rtp_set_tuning); tiled=None keeps the handle's tiled-sweep setting."""
-        t = abi.Tuning()
-        if tiled is None:
-            call("rtp_get_tuning", self._h, C.byref(t))
-        else:
-            t.tiledSweeps = 1 if tiled else 0
-        t.lanes = int(lanes)
-        t.cellFactor = float(cell_factor)
-        call("rtp_set_tuning", self._h, C.byref(t))
-
-    def tuning(self):
-        """(lanes, cell factor, tiled sweeps)."""
-        t = abi.Tuning()
-        call("rtp_get_tuning", self._h, C.byref(t))
-        return int(t.lanes), float(t.cellFactor), int(t.tiledSweeps)
-
-    def autotune(self, steps=5):
-        """Times every launch-shape candidate over `steps` steps and keeps the fastest.
-        Returns (best (lanes, cell factor, tiled), {(lanes, cell factor, tiled): ms per step})."""
-        r = abi.TuneResult()
-        call("rtp_autotune", self._h, int(steps), C.byref(r))
-        key = lambda t: (int(t.lanes), round(float(t.cellFactor), 3), int(t.tiledSweeps))
-        cands = {key(r.candidates[i]): float(r.msPerStep[i]) for i in range(r.tried)}
-        return (int(r.best.lanes), float(r.best.cellFactor), int(r.best.tiledSweeps)), cands
-
     # learned warm start (new; rtp.h rtp_set_warm_start) --------------------------------
     def setWarmStart(self, net, extra_iterations=0, guard_tolerance=0.0, relax_all=False):
         """Warm-start the Jacobi solve with `net` (abi.Mlp); net=None switches it off.
