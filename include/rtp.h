@@ -411,7 +411,8 @@ int rtp_fill_grid_detector(void* handle);
  *   9 (T_i - T_env(x_i)) / 10   (the smoothed temperature above the environment, K / 10)
  * feature 8 being the y-wall proximity with the box walls +-W_y.  The relaxed first
  * correction is cld_computeConstraintCorrection + the mixed boundary; then `extraIterations`
- * plain iterations.  No guard and no relaxation of every iteration on clouds. */
+ * plain iterations.  The guard works as for fluids (a rerun restores the step's total
+ * correction, clouds' cld_updateVel input); there is no relaxation of every iteration. */
 #define RTP_MLP_IN 12
 #define RTP_MLP_HIDDEN 64
 #define RTP_MLP_OUT 4
@@ -444,7 +445,7 @@ typedef struct rtp_solver_stats {
 } rtp_solver_stats;
 
 /* Installs (or with cfg->enabled == 0 removes) the warm start on a fluids or clouds handle
- * (clouds: guardTolerance > 0 or relaxAllIterations give RTP_ERR_NOT_SUPPORTED). */
+ * (clouds: relaxAllIterations gives RTP_ERR_NOT_SUPPORTED). */
 int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_config* cfg);
 /* Also measure the plain solver's output error per step (fluids: warm-started steps always
  * do; clouds: only while enabled).  Fluids and clouds handles. */

@@ -588,6 +588,47 @@ static int record_fluids_step(Handle* h, Launcher& L) {
                     h->io, h->predLam);
 }
 
+// The warm-start guard's conditional graph node, in three parts around ws_guard: a handle in
+// the step graph being captured on L.stream; then an if-node on it, whose body is captured on
+// stream2 (conditional bodies take kernels, memsets and copies only: no profiling events);
+// then the end of that capture.
+static int guard_handle(Launcher& L, cudaGraphConditionalHandle* hnd) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t capGraph = nullptr;
+  RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive) return fail(RTP_ERR_STATE, "warm-start guard needs a captured step");
+  RTP_CUDA(cudaGraphConditionalHandleCreate(hnd, capGraph, 0, cudaGraphCondAssignDefault));
+  return RTP_OK;
+}
+
+static int guard_body_begin(Handle* h, Launcher& L, cudaGraphConditionalHandle hnd) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t capGraph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, &deps, &edges, &nd));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = hnd;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  RTP_CUDA(cudaGraphAddNode(&node, capGraph, deps, edges, nd, &np));
+  RTP_CUDA(cudaStreamUpdateCaptureDependencies(L.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  RTP_CUDA(cudaStreamBeginCaptureToGraph(h->stream2, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  return RTP_OK;
+}
+
+static int guard_body_end(Handle* h, int rc) {
+  cudaGraph_t bodyOut = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(h->stream2, &bodyOut);
+  if (rc) return rc;
+  if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(guard body)");
+  return RTP_OK;
+}
+
 // Warm-started substep: the network's lambda and residual give the first correction, then
 // wsExtra plain iterations; the guard reruns the solve with the plain iteration count from
 // the same predicted positions (predA) inside a conditional graph node.  The solver output
@@ -603,33 +644,12 @@ static int record_fluids_ws_step(Handle* h, Launcher& L) {
   RTP_TRY(solver_error(h, L, fk, h->predB, &vortDone));
   const bool guard = h->wsTol > 0.0f;
   cudaGraphConditionalHandle hnd = 0;
-  cudaGraph_t capGraph = nullptr;
-  if (guard) {
-    cudaStreamCaptureStatus st;
-    RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, nullptr, nullptr, nullptr));
-    if (st != cudaStreamCaptureStatusActive) return fail(RTP_ERR_STATE, "warm-start guard needs a captured step");
-    RTP_CUDA(cudaGraphConditionalHandleCreate(&hnd, capGraph, 0, cudaGraphCondAssignDefault));
-  }
+  if (guard) RTP_TRY(guard_handle(L, &hnd));
   RTP_TRY(ws_guard(h->errPartial, n, h->wsTol, h->solverStats, hnd, guard, false, L));
   if (guard) {
-    cudaStreamCaptureStatus st;
-    const cudaGraphNode_t* deps = nullptr;
-    const cudaGraphEdgeData* edges = nullptr;
-    size_t nd = 0;
-    RTP_CUDA(cudaStreamGetCaptureInfo(L.stream, &st, nullptr, &capGraph, &deps, &edges, &nd));
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = hnd;
-    np.conditional.type = cudaGraphCondTypeIf;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    RTP_CUDA(cudaGraphAddNode(&node, capGraph, deps, edges, nd, &np));
-    RTP_CUDA(cudaStreamUpdateCaptureDependencies(L.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    // Conditional bodies take kernels, memsets and copies only: no profiling events there.
+    RTP_TRY(guard_body_begin(h, L, hnd));
     Launcher L2;
     L2.stream = h->stream2;
-    RTP_CUDA(cudaStreamBeginCaptureToGraph(h->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int rc = RTP_OK;
     if (h->iters > 0) {
       rc = plain_iterations(h, L2, fk, h->predA, h->iters, h->predB, h->predTmp, true, false);
@@ -645,10 +665,7 @@ static int record_fluids_ws_step(Handle* h, Launcher& L) {
     bool vd2 = false;
     if (!rc) rc = solver_error(h, L2, fk, h->predB, &vd2);
     if (!rc) rc = ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, true, L2);
-    cudaGraph_t bodyOut = nullptr;
-    const cudaError_t ec = cudaStreamEndCapture(h->stream2, &bodyOut);
-    if (rc) return rc;
-    if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(guard body)");
+    RTP_TRY(guard_body_end(h, rc));
   }
   return fluid_post(g, fk, h->predB, h->velS, h->vort, h->table, n, h->idsS, h->pos, h->vel, h->ids, h->pairs, L,
                     vortDone, h->io, h->predLam);
@@ -785,35 +802,79 @@ static int clouds_presort(Handle* h, Launcher& L) {
   return RTP_OK;
 }
 
+// Clouds.cpp:570-587 from predA: `count` plain iterations, the last landing in dest (spare is
+// the other buffer) and updating the velocities; with no iteration the velocities come from
+// the step's total correction alone and dest is not written (returns the output buffer).
+static int cloud_plain_iterations(Handle* h, Launcher& L, const FluidK& fk, const float4* in, uint32_t count,
+                                  float4* dest, float4* spare) {
+  const uint32_t n = (uint32_t)h->curN;
+  const float4* cur = in;
+  for (uint32_t it = 0; it < count; ++it) {
+    float4* out = ((count - it) % 2 == 1) ? dest : spare;
+    RTP_TRY(cloud_iteration(h->g, fk, cur, out, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == count,
+                            h->velS, h->pairs, L, h->predLam));
+    cur = out;
+  }
+  return RTP_OK;
+}
+
 // Clouds.cpp:570-590 from predA: the plain Jacobi loop, or with `block` the warm-started first
-// iteration (the network relaxes the plain lambda) and E plain iterations; then (statistics)
-// the solver output's density error, then Clouds.cpp:592-605.
-static int clouds_solve_post(Handle* h, Launcher& L, const void* block, uint32_t E) {
+// iteration (the network relaxes the plain lambda) and E plain iterations; the solver output
+// ends in predB (predA with no iteration at all).  With `guarded` and a guard tolerance the
+// step's solver-output density error decides, inside a conditional graph node, whether the
+// solve reruns plain (the handle's iteration count) from predA with the step's total
+// correction restored.  Then (statistics) the solver output's density error, then
+// Clouds.cpp:592-605.
+static int clouds_solve_post(Handle* h, Launcher& L, const void* block, uint32_t E, bool guarded) {
   const uint32_t n = (uint32_t)h->curN;
   const GridK& g = h->g;
   const FluidK fk = fluidk_of(h);
   const CloudK ck = make_cloudk(h);
-  float4* cur = h->predA;
-  float4* nxt = h->predB;
-  uint32_t iters = h->iters;
+  const bool guard = guarded && block && h->wsTol > 0.0f;
+  float4* out = h->predB;
   if (block) {
+    // The total correction at the start of the solve, for a rerun (vort is free until the post).
+    if (guard)
+      RTP_CUDA(cudaMemcpyAsync(h->vort, h->totCorrS, sizeof(float4) * n, cudaMemcpyDeviceToDevice, L.stream));
+    float4* warmOut = (E % 2 == 0) ? h->predB : h->predTmp;
     RTP_TRY(cloud_ws_lambda(g, fk, ck, h->predA, h->velS, h->tempS, h->buoyS, h->table, n, h->lambda, h->density,
                             h->pairs, h->predLam, nullptr, block, L));
-    RTP_TRY(cloud_deltap(g, fk, cur, nxt, h->totCorrS, h->lambda, h->table, n, E == 0, h->velS, h->pairs, L,
+    RTP_TRY(cloud_deltap(g, fk, h->predA, warmOut, h->totCorrS, h->lambda, h->table, n, E == 0, h->velS, h->pairs, L,
                          h->predLam));
-    std::swap(cur, nxt);
-    iters = E;
+    RTP_TRY(cloud_plain_iterations(h, L, fk, warmOut, E, h->predB, h->predTmp));
+  } else if (h->iters > 0) {
+    RTP_TRY(cloud_plain_iterations(h, L, fk, h->predA, h->iters, h->predB, h->predTmp));
+  } else {
+    RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
+    out = h->predA;
   }
-  for (uint32_t it = 0; it < iters; ++it) {
-    RTP_TRY(cloud_iteration(g, fk, cur, nxt, h->totCorrS, h->table, n, h->lambda, h->density, it + 1 == iters,
-                            h->velS, h->pairs, L, h->predLam));
-    std::swap(cur, nxt);
-  }
-  if (!block && h->iters == 0) RTP_TRY(cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L));
-  h->predFinal = cur;
-  if (h->statsOn) {
-    RTP_TRY(cloud_density_error(g, fk, cur, h->table, n, h->errPartial, L));
-    RTP_TRY(ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, false, L));
+  h->predFinal = out;
+  if (h->statsOn || guard) {
+    RTP_TRY(cloud_density_error(g, fk, out, h->table, n, h->errPartial, L));
+    cudaGraphConditionalHandle hnd = 0;
+    if (guard) RTP_TRY(guard_handle(L, &hnd));
+    RTP_TRY(ws_guard(h->errPartial, n, guard ? h->wsTol : 0.0f, h->solverStats, hnd, guard, false, L));
+    if (guard) {
+      RTP_TRY(guard_body_begin(h, L, hnd));
+      Launcher L2;
+      L2.stream = h->stream2;
+      int rc = cudaMemcpyAsync(h->totCorrS, h->vort, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream2) ==
+                       cudaSuccess
+                   ? RTP_OK
+                   : fail(RTP_ERR_CUDA, "cudaMemcpyAsync(guard)");
+      if (!rc && h->iters > 0) {
+        rc = cloud_plain_iterations(h, L2, fk, h->predA, h->iters, h->predB, h->predTmp);
+      } else if (!rc) {
+        rc = cudaMemcpyAsync(h->predB, h->predA, sizeof(float4) * n, cudaMemcpyDeviceToDevice, h->stream2) ==
+                     cudaSuccess
+                 ? RTP_OK
+                 : fail(RTP_ERR_CUDA, "cudaMemcpyAsync(guard)");
+        if (!rc) rc = cloud_update_vel(g, fk, h->totCorrS, n, h->velS, L2);
+      }
+      if (!rc) rc = cloud_density_error(g, fk, h->predB, h->table, n, h->errPartial, L2);
+      if (!rc) rc = ws_guard(h->errPartial, n, 0.0f, h->solverStats, 0, false, true, L2);
+      RTP_TRY(guard_body_end(h, rc));
+    }
   }
   // Clouds.cpp:592-605.
   CloudState s;
@@ -829,7 +890,7 @@ static int clouds_solve_post(Handle* h, Launcher& L, const void* block, uint32_t
   s.buoyS = h->buoyS;
   s.ids = h->ids;
   s.idsS = h->idsS;
-  return cloud_post(g, fk, ck, cur, h->velS, h->vort, h->table, n, s, h->pairs, L, h->predLam);
+  return cloud_post(g, fk, ck, out, h->velS, h->vort, h->table, n, s, h->pairs, L, h->predLam);
 }
 
 // clouds_presort for rtp_warm_start_loss_grad: the thermodynamics it runs change temp, vapor,
@@ -851,7 +912,7 @@ static int clouds_presort_keep_state(Handle* h, Launcher& L) {
 int record_clouds_step(Handle* h, Launcher& L) {
   if (h->curN == 0) return RTP_OK;
   RTP_TRY(clouds_presort(h, L));
-  return clouds_solve_post(h, L, h->wsOn ? h->mlpBlock : nullptr, h->wsExtra);
+  return clouds_solve_post(h, L, h->wsOn ? h->mlpBlock : nullptr, h->wsExtra, true);
 }
 
 // Training through the clouds solve after clouds_presort (x* = predA): as ws_train_pass, with
@@ -1926,8 +1987,8 @@ int rtp_set_warm_start(void* handle, const rtp_mlp* net, const rtp_warm_start_co
   if (!handle || !cfg) return fail(RTP_ERR_INVALID_ARGUMENT, "rtp_set_warm_start: null argument");
   Handle* h = H(handle);
   if (h->model == RTP_MODEL_BOIDS) return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: fluids and clouds only");
-  if (h->model == RTP_MODEL_CLOUDS && cfg->enabled && (cfg->guardTolerance > 0.0f || cfg->relaxAllIterations))
-    return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: clouds take no guard and no relaxation of every iteration");
+  if (h->model == RTP_MODEL_CLOUDS && cfg->enabled && cfg->relaxAllIterations)
+    return fail(RTP_ERR_NOT_SUPPORTED, "rtp_set_warm_start: clouds take no relaxation of every iteration");
   if (!cfg->enabled) {
     h->wsOn = false;
     invalidate(h);
@@ -2091,7 +2152,7 @@ int rtp_train_warm_start_rollout(void* handle, const rtp_train_config* cfg, uint
     // The simulation advances with the updated network (the states it trains on are the ones
     // the warm-started solver itself produces).
     if (clouds) {
-      RTP_TRY(clouds_solve_post(h, L, ws_trainer_block(h->trainer), extraIterations));
+      RTP_TRY(clouds_solve_post(h, L, ws_trainer_block(h->trainer), extraIterations, false));
     } else {
       RTP_TRY(ws_first_iteration(h, L, fk, ws_trainer_block(h->trainer), extraIterations, false));
       h->predFinal = h->predB;

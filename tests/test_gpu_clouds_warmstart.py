@@ -8,6 +8,8 @@ and the temperature above the environment (clouds.cu k_cloud_ws_lambda).
 - warm-started steps (network + 0 or 1 extra iteration) against the oracle's restatement
   (oracle.clouds_ws_step) within the clouds step tolerances;
 - an untrained network (zero output layer) is the plain clouds solver bit for bit;
+- the guard: a tolerance every step exceeds reruns each step as the plain solver, bit for bit,
+  and one no step reaches leaves the warm start as it is;
 - the loss through the solve and its gradient dL/dy against the oracle, with the state left
   where it was;
 - a network trained through the clouds solve on one seeded column lowers the solver-output
@@ -97,14 +99,46 @@ def test_untrained_network_is_the_plain_clouds_solver(extra):
             assert np.array_equal(a[k], b[k]), k
 
 
-def test_guard_and_relax_all_are_refused_for_clouds():
+def test_relax_all_is_refused_for_clouds():
     sc = scenes.clouds_cumulus(n=4096)
-    net = abi.Mlp()
     with clouds_model(sc) as m:
         with pytest.raises(Exception):
-            m.setWarmStart(net, extra_iterations=0, guard_tolerance=0.01)
-        with pytest.raises(Exception):
-            m.setWarmStart(net, extra_iterations=0, relax_all=True)
+            m.setWarmStart(abi.Mlp(), extra_iterations=0, relax_all=True)
+
+
+@pytest.mark.parametrize("plain_iters", [1, 2])
+def test_clouds_guard_reruns_as_the_plain_solver(plain_iters):
+    """A guard tolerance every step exceeds reruns every step with the plain solver from the
+    same predicted positions and the step's total correction restored: the guarded warm start
+    equals the plain clouds solver bit for bit, and the statistics count a rerun per step."""
+    sc = scenes.clouds_cumulus(n=32768, noise=True, seed=4)
+    with clouds_model(sc, iters=plain_iters) as plain, clouds_model(sc, iters=plain_iters) as guarded:
+        net = _omega_net(np.random.default_rng(1), _features(sc, gpu_state(guarded, abi.CLOUDS)))
+        guarded.setWarmStart(net, extra_iterations=1, guard_tolerance=1e-12)
+        for _ in range(3):
+            plain.update(1)
+            guarded.update(1)
+        a, b = gpu_state(plain, abi.CLOUDS), gpu_state(guarded, abi.CLOUDS)
+        for k in ("id", "pos", "vel", "temp", "vapor", "cloud"):
+            assert np.array_equal(a[k], b[k]), k
+        s = guarded.solverStats()
+        assert s["steps"] == 3 and s["reruns"] == 3 and s["mean_first"] > 0.0
+
+
+def test_clouds_guard_that_never_fires_is_the_unguarded_warm_start():
+    sc = scenes.clouds_cumulus(n=32768, noise=True, seed=5)
+    with clouds_model(sc, iters=1) as free, clouds_model(sc, iters=1) as guarded:
+        net = _omega_net(np.random.default_rng(2), _features(sc, gpu_state(free, abi.CLOUDS)))
+        free.setWarmStart(net, extra_iterations=0)
+        guarded.setWarmStart(net, extra_iterations=0, guard_tolerance=1e6)
+        for _ in range(3):
+            free.update(1)
+            guarded.update(1)
+        a, b = gpu_state(free, abi.CLOUDS), gpu_state(guarded, abi.CLOUDS)
+        for k in ("id", "pos", "vel", "temp", "vapor", "cloud"):
+            assert np.array_equal(a[k], b[k]), k
+        s = guarded.solverStats()
+        assert s["steps"] == 3 and s["reruns"] == 0
 
 
 def test_clouds_loss_and_gradient_through_the_solve():
