@@ -508,20 +508,22 @@ CLOUD_EVAL_BLOCKS = 4
 CLOUD_EVAL_BLOCK_STEPS = 1000
 
 
-def _timed_blocks(open_model, iters, net, extra, blocks, block_steps):
-    """(ms per step, mean solver-output error, largest block mean, block means) of one
-    configuration run for blocks x block_steps device-timed steps from the seed-0 start, L2
-    flushed before every step, solver statistics reset per block."""
+def _timed_blocks(open_model, iters, net, extra, blocks, block_steps, tol=0.0):
+    """(ms per step, mean solver-output error, largest block mean, block means, guard reruns)
+    of one configuration run for blocks x block_steps device-timed steps from the seed-0
+    start, L2 flushed before every step, solver statistics reset per block."""
     with open_model(iters) as m:
         m.enableSolverStats(True)
         if net is not None:
-            m.setWarmStart(net, extra_iterations=extra)
-        total_ms, errs = 0.0, []
+            m.setWarmStart(net, extra_iterations=extra, guard_tolerance=tol)
+        total_ms, errs, reruns = 0.0, [], 0
         for _ in range(blocks):
             m.resetSolverStats()
             total_ms += m.timeSteps(block_steps, flush_bytes=L2_FLUSH_BYTES)
-            errs.append(m.solverStats()["mean"])
-    return total_ms / (blocks * block_steps), float(np.mean(errs)), float(max(errs)), errs
+            st = m.solverStats()
+            errs.append(st["mean"])
+            reruns += st["reruns"]
+    return total_ms / (blocks * block_steps), float(np.mean(errs)), float(max(errs)), errs, reruns
 
 
 def clouds_warm_start_study(w):
@@ -558,7 +560,7 @@ def clouds_warm_start_study(w):
            "eval": {"blocks": CLOUD_EVAL_BLOCKS, "steps_per_block": CLOUD_EVAL_BLOCK_STEPS}}
     plain, curve = [], []
     for it in CLOUD_PLAIN_ITERS:
-        ms, err, worst, blocks = _timed_blocks(open_model, it, None, 0, CLOUD_EVAL_BLOCKS, CLOUD_EVAL_BLOCK_STEPS)
+        ms, err, worst, blocks, _ = _timed_blocks(open_model, it, None, 0, CLOUD_EVAL_BLOCKS, CLOUD_EVAL_BLOCK_STEPS)
         v = n / (ms / 1000.0)
         plain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err,
                       "largest_block_error": worst, "block_errors": blocks})
@@ -566,15 +568,24 @@ def clouds_warm_start_study(w):
     learned = []
     for e in CLOUD_WARM_EXTRA:
         net = nets[0] if e == 0 else nets[1]
-        ms, err, worst, blocks = _timed_blocks(open_model, 1, net, e, CLOUD_EVAL_BLOCKS, CLOUD_EVAL_BLOCK_STEPS)
+        ms, err, worst, blocks, _ = _timed_blocks(open_model, 1, net, e, CLOUD_EVAL_BLOCKS, CLOUD_EVAL_BLOCK_STEPS)
         v = n / (ms / 1000.0)
         ref = _plain_at(curve, err)
         learned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
                         "mean_density_error": err, "largest_block_error": worst, "block_errors": blocks,
                         "plain_at_equal_error": ref, "speedup_at_equal_error": (v / ref) if ref else None})
     e2 = plain[1]["mean_density_error"]
+    # The guarded warm start: one solve per step (+ 0), and a step whose error exceeds 1.25 x the
+    # plain 2-iteration mean reruns with the plain 2 iterations.
+    tol = 1.25 * e2
+    ms, err, worst, blocks, rr = _timed_blocks(open_model, 2, nets[0], 0, CLOUD_EVAL_BLOCKS, CLOUD_EVAL_BLOCK_STEPS,
+                                               tol)
+    guarded = {"extra_iterations": 0, "guard_tolerance": tol, "plain_iterations": 2,
+               "particle_steps_per_s": n / (ms / 1000.0), "ms_per_step": ms, "mean_density_error": err,
+               "largest_block_error": worst, "block_errors": blocks, "reruns": rr,
+               "steps": CLOUD_EVAL_BLOCKS * CLOUD_EVAL_BLOCK_STEPS}
     v = [x["speedup_at_equal_error"] for x in learned if x["speedup_at_equal_error"]]
-    out.update(plain=plain, learned=learned, best_speedup_at_equal_error=max(v) if v else None,
+    out.update(plain=plain, learned=learned, guarded=guarded, best_speedup_at_equal_error=max(v) if v else None,
                at_error_le_plain2=_at_threshold(plain, learned, e2),
                at_error_le_1pct=_at_threshold(plain, learned, 0.01))
     return out
