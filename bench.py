@@ -32,7 +32,9 @@ Metric: particle-steps/s.
   run 100 device-timed steps of the seed-0 scene after 100 warm-up steps with the solver
   statistics on; the speed-up at equal error compares each warm-started configuration with
   the plain solver's Pareto front interpolated (log-log) at its error, and at_error_le_1pct
-  the fastest configurations of each whose mean error is at most 1 % of rho0.
+  the fastest configurations of each whose mean error is at most 1 % of rho0.  `long_run`
+  repeats the comparison over 2,000 steps from the start (plain 3-24 iterations, warm start
+  +2, +5, +9), the error averaged over the whole run.
 * warm_start (clouds_131k): the same comparison on the clouds solve over the clouds
   configuration's 4,000 steps: networks trained through the clouds solve on the rollouts of
   seeds 1-2 (1,500 steps each, under + 0 and under + 1), then the plain clouds solver (1-8
@@ -432,6 +434,10 @@ def _at_threshold(plain, learned, tol):
             "speedup": bq["particle_steps_per_s"] / bp["particle_steps_per_s"]}
 
 
+WS_LONG_PLAIN_ITERS = (3, 8, 16, 24)
+WS_LONG_EXTRA = (2, 5, 9)
+WS_LONG_BLOCKS = 4
+WS_LONG_BLOCK_STEPS = 500
 WS_TRAIN_SEEDS = (1, 2, 3, 4)
 WS_TRAIN_STEPS = 300
 WS_EVAL_WARMUP = 100
@@ -497,6 +503,26 @@ def warm_start_study(w, steps, warmup):
                best_speedup_at_or_below_plain3_error=best(lambda x: x["mean_density_error"] <= e3),
                at_error_le_1pct=_at_threshold(plain, learned, 0.01),
                at_error_le_plain3=_at_threshold(plain, learned, e3))
+    # The same comparison over a long run: WS_LONG_BLOCKS x WS_LONG_BLOCK_STEPS steps from the
+    # start (the collapse included), the error averaged over all of them.
+    lplain, lcurve = [], []
+    for it in WS_LONG_PLAIN_ITERS:
+        ms, err, worst, blocks, _ = _timed_blocks(open_model, it, None, 0, WS_LONG_BLOCKS, WS_LONG_BLOCK_STEPS)
+        v = n / (ms / 1000.0)
+        lplain.append({"iterations": it, "particle_steps_per_s": v, "ms_per_step": ms, "mean_density_error": err,
+                       "block_errors": blocks})
+        lcurve.append((err, v))
+    llearned = []
+    for e in WS_LONG_EXTRA:
+        ms, err, worst, blocks, _ = _timed_blocks(open_model, 3, net, e, WS_LONG_BLOCKS, WS_LONG_BLOCK_STEPS)
+        v = n / (ms / 1000.0)
+        ref = _plain_at(lcurve, err)
+        llearned.append({"extra_iterations": e, "particle_steps_per_s": v, "ms_per_step": ms,
+                         "mean_density_error": err, "block_errors": blocks, "plain_at_equal_error": ref,
+                         "speedup_at_equal_error": (v / ref) if ref else None})
+    out["long_run"] = {"steps": WS_LONG_BLOCKS * WS_LONG_BLOCK_STEPS, "blocks": WS_LONG_BLOCKS,
+                       "plain": lplain, "learned": llearned,
+                       "at_error_le_1pct": _at_threshold(lplain, llearned, 0.01)}
     return out
 
 
