@@ -485,6 +485,7 @@ __global__ void __launch_bounds__(128) k_cloud_ws_loss_grad_x(GridK g, FluidK p,
                                                               const uint2* __restrict__ table, uint32_t n, PairList pl2,
                                                               float invN, float4* __restrict__ gOut,
                                                               float* __restrict__ lossPart) {
+  pdl_enter();
   __shared__ float s_loss[128 / kQuad];
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
@@ -531,6 +532,7 @@ __global__ void __launch_bounds__(128) k_cloud_ws_grad_y(GridK g, FluidK p, cons
                                                          const float4* __restrict__ gIn,
                                                          const uint2* __restrict__ table, uint32_t n, PairList pl,
                                                          float* __restrict__ dy) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;

@@ -414,6 +414,7 @@ static int check_launch(const char* what) {
 // resetCellIDs (grid.cl:65-71): a key above every cell for each slot; the slots a step does not
 // fill keep theirs, so they stay at the tail of the sorted keys in slot order.
 __global__ void k_reset_cell_ids(uint32_t* __restrict__ keys, uint32_t n, uint32_t base) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) keys[i] = base + i;
 }

@@ -164,6 +164,7 @@ __global__ void __launch_bounds__(kSweepThreads, MODE == 0 ? 16 : 14)
 __global__ void k_ws_apply_omega(const float4* __restrict__ xs, const float* __restrict__ lam,
                                  const float* __restrict__ y, uint32_t n, float* __restrict__ lamOut,
                                  float4* __restrict__ packed) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 x = ld4(xs + i);
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(128) k_ws_loss_grad_x(GridK g, FluidK p, const
                                                         const float* __restrict__ rho2, const uint2* __restrict__ table,
                                                         uint32_t n, PairList pl2, float invN,
                                                         float4* __restrict__ gOut, float* __restrict__ lossPart) {
+  pdl_enter();
   __shared__ float s_loss[128 / kQuad];
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(128) k_ws_grad_y(GridK g, FluidK p, const floa
                                                    const float* __restrict__ lam, const float* __restrict__ y,
                                                    const float4* __restrict__ gIn, const uint2* __restrict__ table,
                                                    uint32_t n, PairList pl, float* __restrict__ dy) {
+  pdl_enter();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / kQuad, q = t % kQuad;
   const bool active = i < n;
@@ -255,6 +258,7 @@ __global__ void __launch_bounds__(128) k_ws_grad_y(GridK g, FluidK p, const floa
 // dst[ids[i]] = src[i * stride]: sorted order -> particle ids.
 __global__ void k_scatter_by_id(const uint32_t* __restrict__ ids, const float* __restrict__ src, uint32_t stride,
                                 uint32_t n, float* __restrict__ dst) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[__ldg(ids + i)] = __ldg(src + (size_t)i * stride);
 }
