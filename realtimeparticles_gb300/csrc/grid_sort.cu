@@ -279,12 +279,19 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
   // Stable rank within the warp's contiguous chunk, items in index order.
   const uint32_t wbase = tile * kSortTile + warp * (32 * ITEMS);
   const uint32_t ltmask = lanemask_lt();
-  uint32_t key[ITEMS], dig[ITEMS], rank[ITEMS];
+  uint32_t key[ITEMS], dig[ITEMS], rank[ITEMS], srcI[ITEMS];
+  // All of the lane's keys and source indices are loaded before the ranking starts.
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
     const uint32_t e = wbase + k * 32 + lane;
     const bool valid = e < n;
     key[k] = valid ? __ldg(keys_in + e) : 0u;
+    srcI[k] = (valid && idx_in) ? __ldg(idx_in + e) : e;
+  }
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const uint32_t e = wbase + k * 32 + lane;
+    const bool valid = e < n;
     dig[k] = valid ? ((key[k] >> shift) & mask) : 0xFFFFFFFFu;
     // The lowest lane of each digit's peer group adds the group to the warp's counter and
     // hands the previous count to its peers.
@@ -333,7 +340,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
     if (e < n) {
       const uint32_t d = dig[k];
       const uint32_t lp = s_lstart[d] + s_wc[warp][d] + rank[k];
-      s_ks[lp] = make_uint2(key[k], idx_in ? __ldg(idx_in + e) : e);
+      s_ks[lp] = make_uint2(key[k], srcI[k]);
     }
   }
   __syncthreads();
@@ -361,8 +368,23 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
       if (!LAST) {
         idx_out[pos] = src;
       } else {
-        for (int b = 0; b < g.n4; ++b) g.dst4[b][pos] = __ldg(g.src4[b] + src);
-        for (int b = 0; b < g.n1; ++b) g.dst1[b][pos] = __ldg(g.src1[b] + src);
+        // Every payload load of the element is issued before its stores: to the compiler the
+        // destinations may alias the sources, so interleaved load/store pairs would each wait
+        // for a full load round trip.
+        float4 v4[GatherList::kMax4];
+        uint32_t v1[GatherList::kMax1];
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax4; ++b)
+          if (b < g.n4) v4[b] = __ldg(g.src4[b] + src);
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax1; ++b)
+          if (b < g.n1) v1[b] = __ldg(g.src1[b] + src);
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax4; ++b)
+          if (b < g.n4) g.dst4[b][pos] = v4[b];
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax1; ++b)
+          if (b < g.n1) g.dst1[b][pos] = v1[b];
         if (g.perm) g.perm[pos] = src;
       }
     }
