@@ -244,9 +244,12 @@ __device__ __forceinline__ void block_scan2(uint32_t v0, uint32_t v1, uint32_t* 
 // placed in shared memory in tile-local digit order, and written out from there, so that
 // consecutive threads write consecutive addresses of each digit's run.  WARPS warps per
 // block, kSortTile / (32 WARPS) keys per lane: 16 warps at small tile counts (more threads
-// in flight over few tiles), 8 at large ones (smaller shared-memory footprint).
+// in flight over few tiles), 8 at large ones (smaller shared-memory footprint).  The 8-warp
+// plain pass is held to 48 registers so that five blocks fit an SM (measured at 16.7M keys:
+// 263 -> 221 us for two passes); the 8-warp gathering pass keeps more registers for its staged
+// loads; 16-warp blocks keep two per SM (64 registers).
 template <bool LAST, int WARPS>
-__global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
+__global__ void __launch_bounds__(32 * WARPS, WARPS == 16 ? 2 : (LAST ? 1 : 5)) k_sort_pass(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ idx_in, uint32_t n, int shift, int bits,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ idx_out, uint32_t* __restrict__ hist_next, int next_shift, int next_bits, GatherList g) {
@@ -346,6 +349,60 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
   __syncthreads();
 
   const uint32_t count = min((uint32_t)kSortTile, n - tile * kSortTile);
+  static_assert(ITEMS % 2 == 0, "the gathering pass takes elements in pairs");
+  if constexpr (LAST) {
+    // Two elements per round: all payload loads of both are issued before their stores (to the
+    // compiler the destinations may alias the sources, so interleaved load/store pairs would
+    // each wait for a full load round trip).
+#pragma unroll 1
+    for (int it = 0; it < ITEMS; it += 2) {
+      uint32_t kk[2], pos[2], src[2];
+      bool ok[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const uint32_t j = (it + u) * THREADS + tid;
+        const bool valid = j < count;
+        kk[u] = 0u;
+        pos[u] = 0u;
+        src[u] = 0u;
+        if (valid) {
+          const uint2 ks = s_ks[j];
+          kk[u] = ks.x;
+          src[u] = ks.y;
+          pos[u] = s_base[(kk[u] >> shift) & mask] + j;  // wraps back into [0, n) for a consistent histogram
+        }
+        // A consistent histogram gives pos < n.  An inconsistent one (a bug, or offsets supplied
+        // from outside) must not write out of bounds: the element is not written and the fault
+        // word is raised, which the handle reports at its next synchronisation.
+        ok[u] = valid && pos[u] < n;
+        if (valid && !ok[u] && g.fault) atomicOr(g.fault, 1u);
+      }
+      float4 v4[2][GatherList::kMax4];
+      uint32_t v1[2][GatherList::kMax1];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax4; ++b)
+          if (ok[u] && b < g.n4) v4[u][b] = __ldg(g.src4[b] + src[u]);
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax1; ++b)
+          if (ok[u] && b < g.n1) v1[u][b] = __ldg(g.src1[b] + src[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (!ok[u]) continue;
+        keys_out[pos[u]] = kk[u];
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax4; ++b)
+          if (b < g.n4) g.dst4[b][pos[u]] = v4[u][b];
+#pragma unroll
+        for (int b = 0; b < GatherList::kMax1; ++b)
+          if (b < g.n1) g.dst1[b][pos[u]] = v1[u][b];
+        if (g.perm) g.perm[pos[u]] = src[u];
+      }
+    }
+    return;
+  }
   const uint32_t nmask = (1u << next_bits) - 1u;
 #pragma unroll 2
   for (int it = 0; it < ITEMS; ++it) {
@@ -365,35 +422,12 @@ __global__ void __launch_bounds__(32 * WARPS) k_sort_pass(
     if (valid && !ok && g.fault) atomicOr(g.fault, 1u);
     if (ok) {
       keys_out[pos] = kk;
-      if (!LAST) {
-        idx_out[pos] = src;
-      } else {
-        // Every payload load of the element is issued before its stores: to the compiler the
-        // destinations may alias the sources, so interleaved load/store pairs would each wait
-        // for a full load round trip.
-        float4 v4[GatherList::kMax4];
-        uint32_t v1[GatherList::kMax1];
-#pragma unroll
-        for (int b = 0; b < GatherList::kMax4; ++b)
-          if (b < g.n4) v4[b] = __ldg(g.src4[b] + src);
-#pragma unroll
-        for (int b = 0; b < GatherList::kMax1; ++b)
-          if (b < g.n1) v1[b] = __ldg(g.src1[b] + src);
-#pragma unroll
-        for (int b = 0; b < GatherList::kMax4; ++b)
-          if (b < g.n4) g.dst4[b][pos] = v4[b];
-#pragma unroll
-        for (int b = 0; b < GatherList::kMax1; ++b)
-          if (b < g.n1) g.dst1[b][pos] = v1[b];
-        if (g.perm) g.perm[pos] = src;
-      }
+      idx_out[pos] = src;
     }
-    if (!LAST) {
-      // Next pass's tile histogram, aggregated over lanes hitting the same (tile, digit).
-      const uint32_t slot = ok ? (pos / kSortTile) * kMaxBins + ((kk >> next_shift) & nmask) : 0xFFFFFFFFu;
-      const uint32_t peers = __match_any_sync(0xffffffffu, slot);
-      if (ok && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
-    }
+    // Next pass's tile histogram, aggregated over lanes hitting the same (tile, digit).
+    const uint32_t slot = ok ? (pos / kSortTile) * kMaxBins + ((kk >> next_shift) & nmask) : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xffffffffu, slot);
+    if (ok && (peers & ltmask) == 0) atomicAdd(hist_next + slot, (uint32_t)__popc(peers));
   }
 }
 
@@ -500,6 +534,8 @@ int launch_sort_one_pass(const uint32_t* keys_in, uint32_t n, int shift, int bit
 
 int launch_sort_passes(const SortPlan& p, const uint32_t* keys_in, uint32_t* keys_out, const SortScratch& s,
                        const GatherList& g, Launcher& L) {
+  if (g.n4 < 0 || g.n4 > GatherList::kMax4 || g.n1 < 0 || g.n1 > GatherList::kMax1)
+    return fail(RTP_ERR_INVALID_ARGUMENT, "sort: too many gathered arrays");
   if (p.n == 0) return RTP_OK;
   const size_t per = (size_t)p.tiles * kMaxBins;
   const uint32_t* kin = keys_in;

@@ -100,8 +100,10 @@ void sort_scratch_carve(const SortPlan& p, void* base, SortScratch& s);
 
 // Values carried by the last sort pass: dst[pos] = src[perm[pos]].
 struct GatherList {
-  static constexpr int kMax4 = 6;
-  static constexpr int kMax1 = 6;
+  // The most any step gathers (clouds: pos, vel, predicted pos, total correction; temperature,
+  // buoyancy, vapour, cloud, id).  The gathering pass stages every entry in registers.
+  static constexpr int kMax4 = 4;
+  static constexpr int kMax1 = 5;
   const float4* src4[kMax4];
   float4* dst4[kMax4];
   const uint32_t* src1[kMax1];
