@@ -59,7 +59,11 @@ __device__ __forceinline__ void image_shift(const GridK& g, uint32_t code, float
 // Filter pass over the clouds neighbourhood: add(entry) for each candidate within h2, in
 // visiting order.  Each (x, y) row's three z cells are read from the table together and
 // visited as one range where they are contiguous with the same image shift (all but the
-// z-wrapped cells at the box faces), eight position loads in flight.
+// z-wrapped cells at the box faces), eight position loads in flight.  The pair test rounds
+// every operation explicitly (xi - xj, minus the image shift, then two fused multiply-adds, as
+// within_radius does), so every kernel this is inlined into records the same pairs.  (A
+// separate loop without the shift subtractions for unshifted runs was measured: 6 % slower
+// clouds steps.)
 template <class ADD>
 __device__ __forceinline__ void filter_cloud_neighbours(const GridK& g, const uint2* __restrict__ table,
                                                         const float4* __restrict__ pos, float4 xi, float h2,
@@ -87,8 +91,9 @@ __device__ __forceinline__ void filter_cloud_neighbours(const GridK& g, const ui
       auto run = [&](uint32_t b, uint32_t e, float shz) {
         const uint32_t code = image_code(shx, shz) << 28;
         visit_range_x8(b, e, [&](uint32_t j) { return ld4(pos + j); }, [&](uint32_t j, float4 xj) {
-          const float vx = xi.x - xj.x - shx, vy = xi.y - xj.y, vz = xi.z - xj.z - shz;
-          if (vx * vx + vy * vy + vz * vz < h2) add(j | code);
+          const float4 xs = f4(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z), 0.0f);
+          const float vx = __fsub_rn(xs.x, shx), vz = __fsub_rn(xs.z, shz);
+          if (__fmaf_rn(vz, vz, __fmaf_rn(xs.y, xs.y, __fmul_rn(vx, vx))) < h2) add(j | code);
         });
       };
       // Cells in visiting order, joined while contiguous with the same shift.
