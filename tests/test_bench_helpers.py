@@ -1,6 +1,7 @@
-"""The equal-error comparison of bench.py's warm-start studies (CPU only): the Pareto front of the
-plain solver's (error, throughput) points, the log-log interpolation of the plain throughput at a
-given error, and the fastest-configuration pick under an error bound."""
+"""bench.py helpers (CPU only): the equal-error comparison of the warm-start studies (the Pareto
+front of the plain solver's (error, throughput) points, the log-log interpolation of the plain
+throughput at a given error, the fastest-configuration pick under an error bound) and the byte
+accounting of the grid/sort roofline."""
 import math
 import os
 import sys
@@ -48,3 +49,25 @@ def test_threshold_pick_takes_the_fastest_under_the_bound():
     assert r["speedup"] == pytest.approx(166.0 / 78.0)
     none = bench._at_threshold(plain, learned, 0.005)
     assert none["speedup"] is None and none["plain"] is None
+
+
+def test_grid_sort_roofline_counts_the_algorithmic_bytes_of_each_kernel():
+    class C:  # the grid constants grid_sort_summary reads
+        keyBits = 18  # two 9-bit passes
+        numCells = 64000
+    n, nonempty, steps = 131072, 16000, 4
+    # kernel -> (launches, total ms) over `steps` steps, as Model.kernelTimes() reports
+    kt = {"fld_predict": (4, 0.04), "sort_scan": (8, 0.05), "sort_pass": (4, 0.04), "sort_pass_gather": (4, 0.056),
+          "cellTable": (4, 0.024), "fld_lambda": (12, 0.7)}
+    r = bench.grid_sort_summary(kt, steps, n, C, nonempty, 6800.0)
+    expect = 52 * n + 12 * n + 112 * n + 8 * C.numCells + 4 * n + 8 * nonempty
+    assert r["algorithmic_bytes_per_step"] == expect
+    assert r["sort_passes"] == 2
+    assert r["ms_per_step"] == pytest.approx((0.04 + 0.05 + 0.04 + 0.056 + 0.024) / steps)  # fld_lambda left out
+    assert r["achieved_gbs"] == pytest.approx(expect / (r["ms_per_step"] / 1000.0) / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved_gbs"] / 6800.0)
+    assert "fld_lambda" not in r["kernels"]
+    C.keyBits = 26  # three passes: the middle one moves keys and indices in and out
+    r3 = bench.grid_sort_summary(kt, steps, n, C, nonempty, 6800.0)
+    assert r3["sort_passes"] == 3
+    assert r3["algorithmic_bytes_per_step"] == expect + 16 * n
